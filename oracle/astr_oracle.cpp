@@ -1,0 +1,1323 @@
+// ORACLE — test infrastructure only (see astr_oracle.h).
+//
+// CPU FP64 restatement of the ASTR right-hand-side hot path.  Every routine
+// below names the reference routine it restates (file:line, paths relative to
+// the ASTR source tree).  Operation order inside each expression follows the
+// Fortran left-to-right evaluation of the reference so that, built with
+// -ffp-contract=off, the arithmetic is the reference's own.
+#include "astr_oracle.h"
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+const int HM = 5;                 // halo width, src/commvar.F90:184
+const double PI = 4.0 * std::atan(1.0);   // src/constdef.F90:12
+const double NUM1D3 = 1.0 / 3.0, NUM2D3 = 2.0 / 3.0;
+const double NUM7D9 = 7.0 / 9.0, NUM1D36 = 1.0 / 36.0, NUM1D60 = 1.0 / 60.0;
+
+// compact_scheme (src/commtype.F90:13-23) with the Thomas factors of
+// tridiagonal_thomas_proprocess (src/commfunc.F90:752-774).
+struct Scheme {
+  int first = 0, last = 0, dim = 0, ntype = 3;
+  std::vector<double> a, c, ac1, ac2, ac3;  // index node-first
+  int n() const { return last - first + 1; }
+  void alloc() {
+    int m = n();
+    a.assign(m, 0.0); c.assign(m, 0.0);
+    ac1.assign(m, 0.0); ac2.assign(m, 0.0); ac3.assign(m, 0.0);
+  }
+  // src/commfunc.F90:752-774
+  void preprocess() {
+    int m = n();
+    ac1[0] = c[0];
+    for (int i = 1; i < m; ++i) {
+      ac1[i] = c[i] / (1.0 - a[i] * ac1[i - 1]);
+      ac2[i] = 1.0 / (1.0 - a[i] * ac1[i - 1]);
+      ac3[i] = a[i] / (1.0 - a[i] * ac1[i - 1]);
+    }
+  }
+  // src/commfunc.F90:790-813 (d is overwritten, x returned in x)
+  void solve(double* d, double* x) const {
+    int m = n();
+    for (int i = 1; i < m; ++i) d[i] = d[i] * ac2[i] - d[i - 1] * ac3[i];
+    x[m - 1] = d[m - 1];
+    for (int i = m - 2; i >= 0; --i) x[i] = d[i] - ac1[i] * x[i + 1];
+  }
+};
+
+struct FilterTables {  // src/filter.F90:299-432
+  double c2i[2], c4i[3], c6i[4], c8i[5], c10i[6];
+  double cb[5][9];   // coefb(0:4,0:8)
+  double ch[5][11];  // coefh(0:4,0:10)
+};
+
+}  // namespace
+
+struct orc_ctx {
+  orc_config cfg;
+  int im, jm, km, ndims;
+  long NI, NJ, NK, nh, n0;
+  int is, ie, js, je, ks, ke;
+  double const1, const2, const3, const4, const5, const6, const7;
+  double tempconst, tempconst1, pinf, roinf, uinf, tinf;
+  double dxm, dym, dzm;  // mini-app uniform spacings
+  Scheme fd[3], flt[3];
+  FilterTables ft;
+  // halo arrays
+  std::vector<double> q, rho, vel, prs, tmp, x, dxi, jacob, sigma, qflux;
+  // interior arrays
+  std::vector<double> qrhs, qsave, dvel, dtmp;
+  double force[3] = {0, 0, 0};
+  double massflux_target = 0.0;
+
+  inline long h(int i, int j, int k) const {
+    return (long)(i + HM) + NI * ((long)(j + HM) + NJ * (long)(k + HM));
+  }
+  inline long z(int i, int j, int k) const {
+    return (long)i + (long)(im + 1) * ((long)j + (long)(jm + 1) * (long)k);
+  }
+  int dimof(int d) const { return d == 0 ? im : (d == 1 ? jm : km); }
+  int npdc(int d) const { return d == 0 ? cfg.npdci : (d == 1 ? cfg.npdcj : cfg.npdck); }
+  bool homo(int d) const { return npdc(d) == 3; }
+  // stride (in elements) of a halo array along direction d
+  long hstride(int d) const { return d == 0 ? 1 : (d == 1 ? NI : NI * NJ); }
+  long zstride(int d) const {
+    return d == 0 ? 1 : (d == 1 ? (long)(im + 1) : (long)(im + 1) * (jm + 1));
+  }
+};
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Scheme set-up
+// ---------------------------------------------------------------------------
+
+// fd_scheme_initiate, src/derivative.F90:63-158 (scheme '643c')
+void fd_scheme_initiate(Scheme& s, int ntype, int dim) {
+  int i0 = 0, imx = 0;
+  switch (ntype) {
+    case 1: i0 = 0; imx = dim + 1; break;
+    case 2: i0 = -1; imx = dim; break;
+    case 3: i0 = -1; imx = dim + 1; break;
+    default: i0 = 0; imx = dim; break;
+  }
+  s.first = i0; s.last = imx; s.dim = dim; s.ntype = ntype;
+  s.alloc();
+  for (int i = 0; i < s.n(); ++i) { s.a[i] = NUM1D3; s.c[i] = NUM1D3; }
+  s.a[0] = 0.0; s.c[0] = 0.0;
+  s.a[imx - i0] = 0.0; s.c[imx - i0] = 0.0;
+  if (ntype == 1 || ntype == 4) {
+    s.a[0] = 2.0; s.c[0] = 2.0;
+    s.a[1] = 0.25; s.c[1] = 0.25;
+  }
+  if (ntype == 2 || ntype == 4) {
+    s.a[imx - i0] = 2.0; s.c[imx - i0] = 2.0;
+    s.a[imx - 1 - i0] = 0.25; s.c[imx - 1 - i0] = 0.25;
+  }
+  s.preprocess();
+}
+
+// compact_filter_initiate, src/filter.F90:31-100
+void compact_filter_initiate(Scheme& s, int ntype, int dim, double alfa) {
+  int i0 = 0, imx = 0;
+  double b0 = 0, bm = 0;
+  switch (ntype) {
+    case 1: i0 = 0; imx = dim + 3; b0 = 0.98; bm = 1.11; break;
+    case 2: i0 = -3; imx = dim; b0 = 1.11; bm = 0.98; break;
+    case 3: i0 = -3; imx = dim + 3; b0 = 1.11; bm = 1.11; break;
+    default: i0 = 0; imx = dim; b0 = 0.98; bm = 0.98; break;
+  }
+  s.first = i0; s.last = imx; s.dim = dim; s.ntype = ntype;
+  s.alloc();
+  for (int i = 0; i < s.n(); ++i) { s.a[i] = alfa; s.c[i] = alfa; }
+  s.a[0] = b0; s.c[0] = b0;
+  s.a[imx - i0] = bm; s.c[imx - i0] = bm;
+  s.preprocess();
+}
+
+// filter_coefficient_cal, src/filter.F90:299-432
+void filter_coefficient_cal(FilterTables& t, double alfa, double bh, double bb) {
+  t.c2i[0] = (1.0 + 2.0 * alfa) / 4.0;
+  t.c2i[1] = (1.0 + 2.0 * alfa) / 4.0;
+  t.c4i[0] = (5.0 + 6.0 * alfa) / 16.0;
+  t.c4i[1] = (1.0 + 2.0 * alfa) / 4.0;
+  t.c4i[2] = (-1.0 + 2.0 * alfa) / 16.0;
+  t.c6i[0] = (11.0 + 10.0 * alfa) / 32.0;
+  t.c6i[1] = (15.0 + 34.0 * alfa) / 64.0;
+  t.c6i[2] = (-3.0 + 6.0 * alfa) / 32.0;
+  t.c6i[3] = (1.0 - 2.0 * alfa) / 64.0;
+  t.c8i[0] = (93.0 + 70.0 * alfa) / 256.0;
+  t.c8i[1] = (7.0 + 18.0 * alfa) / 32.0;
+  t.c8i[2] = (-7.0 + 14.0 * alfa) / 64.0;
+  t.c8i[3] = (1.0 - 2.0 * alfa) / 32.0;
+  t.c8i[4] = (-1.0 + 2.0 * alfa) / 256.0;
+  t.c10i[0] = (193.0 + 126.0 * alfa) / 512.0;
+  t.c10i[1] = (105.0 + 302.0 * alfa) / 512.0;
+  t.c10i[2] = (-15.0 + 30.0 * alfa) / 128.0;
+  t.c10i[3] = (45.0 - 90.0 * alfa) / 1024.0;
+  t.c10i[4] = (-5.0 + 10.0 * alfa) / 512.0;
+  t.c10i[5] = (1.0 - 2.0 * alfa) / 1024.0;
+  std::memset(t.cb, 0, sizeof(t.cb));
+  t.cb[3][0] = (1.0 - 2.0 * alfa) / 256.0;
+  t.cb[3][1] = (-1.0 + 2.0 * alfa) / 32.0;
+  t.cb[3][2] = (7.0 + 50.0 * alfa) / 64.0;
+  t.cb[3][3] = (25.0 + 14.0 * alfa) / 32.0;
+  t.cb[3][4] = (35.0 + 58.0 * alfa) / 128.0;
+  t.cb[3][5] = (-7.0 + 14.0 * alfa) / 32.0;
+  t.cb[3][6] = (7.0 - 14.0 * alfa) / 64.0;
+  t.cb[3][7] = (-1.0 + 2.0 * alfa) / 32.0;
+  t.cb[3][8] = (1.0 - 2.0 * alfa) / 256.0;
+  t.cb[2][0] = (-1.0 + 2.0 * alfa) / 64.0;
+  t.cb[2][1] = (3.0 + 26.0 * alfa) / 32.0;
+  t.cb[2][2] = (49.0 + 30.0 * alfa) / 64.0;
+  t.cb[2][3] = (5.0 + 6.0 * alfa) / 16.0;
+  t.cb[2][4] = (-15.0 + 30.0 * alfa) / 64.0;
+  t.cb[2][5] = (3.0 - 6.0 * alfa) / 32.0;
+  t.cb[2][6] = (-1.0 + 2.0 * alfa) / 64.0;
+  t.cb[1][0] = (1.0 + 62.0 * alfa) / 64.0;
+  t.cb[1][1] = (29.0 + 6.0 * alfa) / 32.0;
+  t.cb[1][2] = (15.0 + 34.0 * alfa) / 64.0;
+  t.cb[1][3] = (-5.0 + 10.0 * alfa) / 16.0;
+  t.cb[1][4] = (15.0 - 30.0 * alfa) / 64.0;
+  t.cb[1][5] = (-3.0 + 6.0 * alfa) / 32.0;
+  t.cb[1][6] = (1.0 - 2.0 * alfa) / 64.0;
+  t.cb[0][0] = (63.0 + 1.0 * bb) / 64.0;
+  t.cb[0][1] = (3.0 + 29.0 * bb) / 32.0;
+  t.cb[0][2] = (-15.0 + 15.0 * bb) / 64.0;
+  t.cb[0][3] = (5.0 - 5.0 * bb) / 16.0;
+  t.cb[0][4] = (-15.0 + 15.0 * bb) / 64.0;
+  t.cb[0][5] = (3.0 - 3.0 * bb) / 32.0;
+  t.cb[0][6] = (-1.0 + 1.0 * bb) / 64.0;
+  std::memset(t.ch, 0, sizeof(t.ch));
+  t.ch[0][0] = (-1.0 + 1.0 * bh) / 1024.0;
+  t.ch[0][1] = (5.0 - 5.0 * bh) / 512.0;
+  t.ch[0][2] = (979.0 + 45.0 * bh) / 1024.0;
+  t.ch[0][3] = (15.0 + 113.0 * bh) / 128.0;
+  t.ch[0][4] = (-105.0 + 105.0 * bh) / 512.0;
+  t.ch[0][5] = (63.0 - 63.0 * bh) / 256.0;
+  t.ch[0][6] = (-105.0 + 105.0 * bh) / 512.0;
+  t.ch[0][7] = (15.0 - 15.0 * bh) / 128.0;
+  t.ch[0][8] = (-45.0 + 45.0 * bh) / 1024.0;
+  t.ch[0][9] = (5.0 - 5.0 * bh) / 512.0;
+  t.ch[0][10] = (-1.0 + 1.0 * bh) / 1024.0;
+  t.ch[1][0] = (1.0 - 2.0 * alfa) / 1024.0;
+  t.ch[1][1] = (-5.0 + 10.0 * alfa) / 512.0;
+  t.ch[1][2] = (45.0 + 934.0 * alfa) / 1024.0;
+  t.ch[1][3] = (113.0 + 30.0 * alfa) / 128.0;
+  t.ch[1][4] = (105.0 + 302.0 * alfa) / 512.0;
+  t.ch[1][5] = (-63.0 + 126.0 * alfa) / 256.0;
+  t.ch[1][6] = (105.0 - 210.0 * alfa) / 512.0;
+  t.ch[1][7] = (-15.0 + 30.0 * alfa) / 128.0;
+  t.ch[1][8] = (45.0 - 90.0 * alfa) / 1024.0;
+  t.ch[1][9] = (-5.0 + 10.0 * alfa) / 512.0;
+  t.ch[1][10] = (1.0 - 2.0 * alfa) / 1024.0;
+  t.ch[2][0] = (-1.0 + 2.0 * alfa) / 1024.0;
+  t.ch[2][1] = (5.0 - 10.0 * alfa) / 512.0;
+  t.ch[2][2] = (-45.0 + 90.0 * alfa) / 1024.0;
+  t.ch[2][3] = (15.0 + 98.0 * alfa) / 128.0;
+  t.ch[2][4] = (407.0 + 210.0 * alfa) / 512.0;
+  t.ch[2][5] = (63.0 + 130.0 * alfa) / 256.0;
+  t.ch[2][6] = (-105.0 + 210.0 * alfa) / 512.0;
+  t.ch[2][7] = (15.0 - 30.0 * alfa) / 128.0;
+  t.ch[2][8] = (-45.0 + 90.0 * alfa) / 1024.0;
+  t.ch[2][9] = (5.0 - 10.0 * alfa) / 512.0;
+  t.ch[2][10] = (-1.0 + 2.0 * alfa) / 1024.0;
+}
+
+// ---------------------------------------------------------------------------
+// Line kernels.  f points at node 0 of a contiguous line with valid entries
+// f[-HM .. dim+HM].
+// ---------------------------------------------------------------------------
+
+// compact_fd_rhs, src/derivative.F90:210-306 ; df_compact 171-198
+void df_compact(const Scheme& s, const double* f, double* df, double* d, double* xx) {
+  const int i0 = s.first, imx = s.last, nt = s.ntype;
+  auto D = [&](int j) -> double& { return d[j - i0]; };
+  int is_, ie_;
+  if (nt == 1 || nt == 4) {
+    is_ = i0 + 2;
+    int j = i0 + 1;
+    double v1 = f[j + 1] - f[j - 1];
+    D(j) = 0.75 * v1;
+    j = i0;
+    D(j) = -2.5 * f[j] + 2.0 * f[j + 1] + 0.5 * f[j + 2];
+  } else {
+    is_ = i0 + 1;
+    int j = i0;
+    double v1 = f[j + 1] - f[j - 1], v2 = f[j + 2] - f[j - 2], v3 = f[j + 3] - f[j - 3];
+    D(j) = 0.75 * v1 - 0.15 * v2 + NUM1D60 * v3;
+  }
+  if (nt == 2 || nt == 4) {
+    ie_ = imx - 2;
+    int j = imx - 1;
+    double v1 = f[j + 1] - f[j - 1];
+    D(j) = 0.75 * v1;
+    j = imx;
+    D(j) = 2.5 * f[j] - 2.0 * f[j - 1] - 0.5 * f[j - 2];
+  } else {
+    ie_ = imx - 1;
+    int j = imx;
+    double v1 = f[j + 1] - f[j - 1], v2 = f[j + 2] - f[j - 2], v3 = f[j + 3] - f[j - 3];
+    D(j) = 0.75 * v1 - 0.15 * v2 + NUM1D60 * v3;
+  }
+  for (int j = is_; j <= ie_; ++j) {
+    double v1 = f[j + 1] - f[j - 1], v2 = f[j + 2] - f[j - 2];
+    D(j) = NUM7D9 * v1 + NUM1D36 * v2;
+  }
+  s.solve(d, xx);
+  for (int j = 0; j <= s.dim; ++j) df[j] = xx[j - i0];
+}
+
+// compact_filter_rhs, src/filter.F90:156-285 ; compact_filter 112-144
+void compact_filter(const Scheme& s, const FilterTables& t, const double* f, double* ff,
+                    double* d, double* xx) {
+  const int i0 = s.first, imx = s.last, nt = s.ntype;
+  auto D = [&](int j) -> double& { return d[j - i0]; };
+  int is_, ie_;
+  if (nt == 1 || nt == 4) {
+    is_ = i0 + 5;
+    for (int k = i0; k <= i0 + 2; ++k) {
+      double v0 = 0.0;
+      for (int j = 0; j <= 6; ++j) v0 = v0 + t.cb[k - i0][j] * f[i0 + j];
+      D(k) = v0;
+    }
+    int j = i0 + 3;
+    double v0 = f[j] + f[j], v1 = f[j + 1] + f[j - 1], v2 = f[j + 2] + f[j - 2], v3 = f[j + 3] + f[j - 3];
+    D(j) = t.c6i[0] * v0 + t.c6i[1] * v1 + t.c6i[2] * v2 + t.c6i[3] * v3;
+    j = i0 + 4;
+    v0 = f[j] + f[j]; v1 = f[j + 1] + f[j - 1]; v2 = f[j + 2] + f[j - 2]; v3 = f[j + 3] + f[j - 3];
+    double v4 = f[j + 4] + f[j - 4];
+    D(j) = t.c8i[0] * v0 + t.c8i[1] * v1 + t.c8i[2] * v2 + t.c8i[3] * v3 + t.c8i[4] * v4;
+  } else {
+    is_ = i0 + 3;
+    for (int k = i0; k <= i0 + 2; ++k) {
+      double v0 = 0.0;
+      for (int j = 0; j <= 10; ++j) v0 = v0 + t.ch[k - i0][j] * f[i0 - 2 + j];
+      D(k) = v0;
+    }
+  }
+  if (nt == 2 || nt == 4) {
+    ie_ = imx - 5;
+    for (int k = imx - 2; k <= imx; ++k) {
+      double v0 = 0.0;
+      for (int j = 0; j <= 6; ++j) v0 = v0 + t.cb[imx - k][j] * f[imx - j];
+      D(k) = v0;
+    }
+    int j = imx - 3;
+    double v0 = f[j] + f[j], v1 = f[j + 1] + f[j - 1], v2 = f[j + 2] + f[j - 2], v3 = f[j + 3] + f[j - 3];
+    D(j) = t.c6i[0] * v0 + t.c6i[1] * v1 + t.c6i[2] * v2 + t.c6i[3] * v3;
+    j = imx - 4;
+    v0 = f[j] + f[j]; v1 = f[j + 1] + f[j - 1]; v2 = f[j + 2] + f[j - 2]; v3 = f[j + 3] + f[j - 3];
+    double v4 = f[j + 4] + f[j - 4];
+    D(j) = t.c8i[0] * v0 + t.c8i[1] * v1 + t.c8i[2] * v2 + t.c8i[3] * v3 + t.c8i[4] * v4;
+  } else {
+    ie_ = imx - 3;
+    for (int k = imx - 2; k <= imx; ++k) {
+      double v0 = 0.0;
+      for (int j = 0; j <= 10; ++j) v0 = v0 + t.ch[imx - k][j] * f[imx + 2 - j];
+      D(k) = v0;
+    }
+  }
+  for (int j = is_; j <= ie_; ++j) {
+    double v0 = f[j] + f[j], v1 = f[j + 1] + f[j - 1], v2 = f[j + 2] + f[j - 2];
+    double v3 = f[j + 3] + f[j - 3], v4 = f[j + 4] + f[j - 4], v5 = f[j + 5] + f[j - 5];
+    D(j) = t.c10i[0] * v0 + t.c10i[1] * v1 + t.c10i[2] * v2 + t.c10i[3] * v3 +
+           t.c10i[4] * v4 + t.c10i[5] * v5;
+  }
+  s.solve(d, xx);
+  for (int j = 0; j <= s.dim; ++j) ff[j] = xx[j - i0];
+  if (nt == 1 || nt == 4) ff[0] = f[0];
+  if (nt == 2 || nt == 4) ff[s.dim] = f[s.dim];
+}
+
+// Per-thread scratch for one line.
+struct LineBuf {
+  std::vector<double> fb, ob, d, xx;
+  explicit LineBuf(int dim) : fb(dim + 2 * HM + 1), ob(dim + 1), d(dim + 16), xx(dim + 16) {}
+  double* f() { return fb.data() + HM; }
+};
+
+inline int nthreads_env() {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+// Iterate the lines of direction d over a rectangle of the two transverse
+// indices.  fn(a, b) gets the two transverse indices in (i,j,k) order with
+// the line index removed.
+template <typename Fn>
+void for_lines(const orc_ctx& c, int d, int a0, int a1, int b0, int b1, Fn fn) {
+  (void)c; (void)d;
+  long na = a1 - a0 + 1, nb = b1 - b0 + 1;
+  if (na <= 0 || nb <= 0) return;
+#pragma omp parallel
+  {
+    fn(-1, -1);  // per-thread init hook (allocates scratch)
+#pragma omp for collapse(2) schedule(static)
+    for (long b = 0; b < nb; ++b)
+      for (long a = 0; a < na; ++a) fn((int)(a0 + a), (int)(b0 + b));
+  }
+}
+
+// position of the (line index l, transverse a, b) node, halo layout
+inline long hpos(const orc_ctx& c, int d, int l, int a, int b) {
+  if (d == 0) return c.h(l, a, b);
+  if (d == 1) return c.h(a, l, b);
+  return c.h(a, b, l);
+}
+inline long zpos(const orc_ctx& c, int d, int l, int a, int b) {
+  if (d == 0) return c.z(l, a, b);
+  if (d == 1) return c.z(a, l, b);
+  return c.z(a, b, l);
+}
+// transverse ranges (interior) for direction d
+inline void trans_range(const orc_ctx& c, int d, int& a1, int& b1) {
+  if (d == 0) { a1 = c.jm; b1 = c.km; }
+  else if (d == 1) { a1 = c.im; b1 = c.km; }
+  else { a1 = c.im; b1 = c.jm; }
+}
+
+// ---------------------------------------------------------------------------
+// Halo swaps, single rank (src/parallel.F90)
+// ---------------------------------------------------------------------------
+
+// array4d_sendrecv single-rank branches, src/parallel.F90:4169-4174,
+// 4229-4238, 4294-4303: periodic copy of nvar components of a halo array.
+void dataswap(orc_ctx& c, double* var, int nvar, int dir) {
+  const int im = c.im, jm = c.jm, km = c.km;
+  if ((dir == 1 || dir == 0) && c.homo(0)) {
+#pragma omp parallel for collapse(2)
+    for (int n = 0; n < nvar; ++n)
+      for (int k = 0; k <= km; ++k) {
+        double* v = var + (long)n * c.nh;
+        for (int j = 0; j <= jm; ++j) {
+          for (int i = -HM; i <= -1; ++i) v[c.h(i, j, k)] = v[c.h(im + i, j, k)];
+          for (int i = im + 1; i <= im + HM; ++i) v[c.h(i, j, k)] = v[c.h(i - im, j, k)];
+        }
+      }
+  }
+  if ((dir == 2 || dir == 0) && c.homo(1)) {
+#pragma omp parallel for collapse(2)
+    for (int n = 0; n < nvar; ++n)
+      for (int k = 0; k <= km; ++k) {
+        double* v = var + (long)n * c.nh;
+        if (c.cfg.ja == 0) {
+          for (int j = -HM; j <= HM; ++j)
+            for (int i = 0; i <= im; ++i) v[c.h(i, j, k)] = v[c.h(i, 0, k)];
+        } else {
+          for (int j = -HM; j <= -1; ++j)
+            for (int i = 0; i <= im; ++i) v[c.h(i, j, k)] = v[c.h(i, jm + j, k)];
+          for (int j = jm + 1; j <= jm + HM; ++j)
+            for (int i = 0; i <= im; ++i) v[c.h(i, j, k)] = v[c.h(i, j - jm, k)];
+        }
+      }
+  }
+  if ((dir == 3 || dir == 0) && c.homo(2)) {
+#pragma omp parallel for
+    for (int n = 0; n < nvar; ++n) {
+      double* v = var + (long)n * c.nh;
+      if (c.cfg.ka == 0) {
+        for (int k = -HM; k <= HM; ++k)
+          for (int j = 0; j <= jm; ++j)
+            for (int i = 0; i <= im; ++i) v[c.h(i, j, k)] = v[c.h(i, j, 0)];
+      } else {
+        for (int k = -HM; k <= -1; ++k)
+          for (int j = 0; j <= jm; ++j)
+            for (int i = 0; i <= im; ++i) v[c.h(i, j, k)] = v[c.h(i, j, km + k)];
+        for (int k = km + 1; k <= km + HM; ++k)
+          for (int j = 0; j <= jm; ++j)
+            for (int i = 0; i <= im; ++i) v[c.h(i, j, k)] = v[c.h(i, j, k - km)];
+      }
+    }
+  }
+}
+
+// q2fvar_3da (src/fludyna.F90:545-634, nondimensional, no species) at one node
+inline void q2fvar_node(orc_ctx& c, long p) {
+  const long nh = c.nh;
+  double ro = c.q[p];
+  c.rho[p] = ro;
+  double u = c.q[p + nh] / ro, v = c.q[p + 2 * nh] / ro, w = c.q[p + 3 * nh] / ro;
+  c.vel[p] = u; c.vel[p + nh] = v; c.vel[p + 2 * nh] = w;
+  double pr = (c.q[p + 4 * nh] - 0.5 * ro * (u * u + v * v + w * w)) / c.const6;
+  c.prs[p] = pr;
+  c.tmp[p] = pr / ro * c.const2;  // thermal_3d(pressure,density)
+}
+
+void q2fvar_box(orc_ctx& c, int i0, int i1, int j0, int j1, int k0, int k1) {
+#pragma omp parallel for collapse(2)
+  for (int k = k0; k <= k1; ++k)
+    for (int j = j0; j <= j1; ++j)
+      for (int i = i0; i <= i1; ++i) q2fvar_node(c, c.h(i, j, k));
+}
+
+// mini-app fvar2q with pressure (miniapps/tgv_solver_3d/tgvsolver.F90:48-71)
+inline void fvar2q_prs_node(orc_ctx& c, long p) {
+  const long nh = c.nh;
+  double ro = c.rho[p], u = c.vel[p], v = c.vel[p + nh], w = c.vel[p + 2 * nh];
+  c.q[p] = ro;
+  c.q[p + nh] = ro * u;
+  c.q[p + 2 * nh] = ro * v;
+  c.q[p + 3 * nh] = ro * w;
+  double var1 = 0.5 * (u * u + v * v + w * w);
+  c.q[p + 4 * nh] = c.prs[p] * c.const6 + ro * var1;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Public API
+// ---------------------------------------------------------------------------
+extern "C" {
+
+orc_ctx* orc_create(const orc_config* cfg) {
+  orc_ctx* c = new orc_ctx();
+  c->cfg = *cfg;
+  c->im = cfg->im; c->jm = cfg->jm; c->km = cfg->km;
+  c->ndims = (cfg->ka > 0) ? 3 : 2;
+  c->NI = c->im + 2 * HM + 1; c->NJ = c->jm + 2 * HM + 1; c->NK = c->km + 2 * HM + 1;
+  c->nh = c->NI * c->NJ * c->NK;
+  c->n0 = (long)(c->im + 1) * (c->jm + 1) * (c->km + 1);
+  // is..ke: periodic -> 0..dim (src/parallel.F90:1042-1046); a direction
+  // with a physical boundary at both ends on one rank is not assigned there;
+  // the wall-rank convention of the multi-rank branches (1080-1089) is used.
+  c->is = 0; c->ie = c->im; c->js = 0; c->je = c->jm; c->ks = 0; c->ke = c->km;
+  if (cfg->npdci == 4) { c->is = 1; c->ie = c->im - 1; }
+  if (cfg->npdcj == 4) { c->js = 1; c->je = c->jm - 1; }
+  if (cfg->npdck == 4) { c->ks = 1; c->ke = c->km - 1; }
+  // refcal, src/solver.F90:102-128 (nondimensional)
+  const double gamma = 1.4, mach = cfg->mach, pr = cfg->prandtl, re = cfg->reynolds;
+  c->const1 = 1.0 / (gamma * (gamma - 1.0) * (mach * mach));
+  c->const2 = gamma * (mach * mach);
+  c->const3 = (gamma - 1.0) / 3.0 * pr * (mach * mach);
+  c->const4 = (gamma - 1.0) * (mach * mach) * re * pr;
+  c->const5 = (gamma - 1.0) * (mach * mach);
+  c->const6 = 1.0 / (gamma - 1.0);
+  c->const7 = (gamma - 1.0) * (mach * mach) * re * pr;
+  c->roinf = 1.0; c->uinf = 1.0; c->tinf = 1.0;
+  c->pinf = c->roinf * c->tinf / c->const2;
+  c->tempconst = cfg->suth_const / cfg->ref_tem;
+  c->tempconst1 = 1.0 + c->tempconst;
+  c->dxm = 2.0 * PI / (double)c->im;
+  c->dym = 2.0 * PI / (double)c->jm;
+  c->dzm = (c->km > 0) ? 2.0 * PI / (double)c->km : 1.0;
+  // solvrinit, src/comsolver.F90:47-146
+  fd_scheme_initiate(c->fd[0], cfg->npdci, c->im);
+  fd_scheme_initiate(c->fd[1], cfg->npdcj, c->jm);
+  fd_scheme_initiate(c->fd[2], cfg->npdck, c->km);
+  filter_coefficient_cal(c->ft, cfg->alfa_filter, cfg->beter_halo, cfg->beter_bound);
+  compact_filter_initiate(c->flt[0], cfg->npdci, c->im, cfg->alfa_filter);
+  compact_filter_initiate(c->flt[1], cfg->npdcj, c->jm, cfg->alfa_filter);
+  compact_filter_initiate(c->flt[2], cfg->npdck, c->km, cfg->alfa_filter);
+  // commarray allocation (src/commarray.F90:56-108)
+  c->q.assign(5 * c->nh, 0.0);
+  c->rho.assign(c->nh, 0.0); c->prs.assign(c->nh, 0.0); c->tmp.assign(c->nh, 0.0);
+  c->vel.assign(3 * c->nh, 0.0);
+  c->x.assign(3 * c->nh, 0.0);
+  c->dxi.assign(9 * c->nh, 0.0);
+  c->jacob.assign(c->nh, 1.0);
+  c->sigma.assign(6 * c->nh, 0.0);
+  c->qflux.assign(3 * c->nh, 0.0);
+  c->qrhs.assign(5 * c->n0, 0.0);
+  c->qsave.assign(5 * c->n0, 0.0);
+  c->dvel.assign(9 * c->n0, 0.0);
+  c->dtmp.assign(3 * c->n0, 0.0);
+  return c;
+}
+
+void orc_destroy(orc_ctx* c) { delete c; }
+
+double* orc_field(orc_ctx* c, const char* name) {
+  std::string s(name);
+  if (s == "q") return c->q.data();
+  if (s == "rho") return c->rho.data();
+  if (s == "vel") return c->vel.data();
+  if (s == "prs") return c->prs.data();
+  if (s == "tmp") return c->tmp.data();
+  if (s == "x") return c->x.data();
+  if (s == "dxi") return c->dxi.data();
+  if (s == "jacob") return c->jacob.data();
+  if (s == "sigma") return c->sigma.data();
+  if (s == "qflux") return c->qflux.data();
+  if (s == "qrhs") return c->qrhs.data();
+  if (s == "qsave") return c->qsave.data();
+  if (s == "dvel") return c->dvel.data();
+  if (s == "dtmp") return c->dtmp.data();
+  return nullptr;
+}
+
+int orc_scheme(orc_ctx* c, int dir, int kind, int* first, double* out, int cap) {
+  const Scheme& s = kind == 0 ? c->fd[dir] : c->flt[dir];
+  int n = s.n();
+  *first = s.first;
+  if (cap < 5 * n) return -n;
+  for (int i = 0; i < n; ++i) {
+    out[i] = s.a[i]; out[n + i] = s.c[i];
+    out[2 * n + i] = s.ac1[i]; out[3 * n + i] = s.ac2[i]; out[4 * n + i] = s.ac3[i];
+  }
+  return n;
+}
+
+void orc_filter_tables(orc_ctx* c, double* c10, double* c8, double* c6, double* cb, double* ch) {
+  for (int i = 0; i < 6; ++i) c10[i] = c->ft.c10i[i];
+  for (int i = 0; i < 5; ++i) c8[i] = c->ft.c8i[i];
+  for (int i = 0; i < 4; ++i) c6[i] = c->ft.c6i[i];
+  for (int j = 0; j < 9; ++j)
+    for (int r = 0; r < 5; ++r) cb[r + 5 * j] = c->ft.cb[r][j];
+  for (int j = 0; j < 11; ++j)
+    for (int r = 0; r < 5; ++r) ch[r + 5 * j] = c->ft.ch[r][j];
+}
+
+void orc_constants(orc_ctx* c, double* o) {
+  o[0] = c->const1; o[1] = c->const2; o[2] = c->const3; o[3] = c->const4;
+  o[4] = c->const5; o[5] = c->const6; o[6] = c->const7; o[7] = c->tempconst;
+  o[8] = c->tempconst1;
+}
+
+void orc_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
+int orc_get_threads(void) { return nthreads_env(); }
+
+// gridcube, src/gridgeneration.F90:233-267 (single rank: ig0=jg0=kg0=0)
+void orc_gridcube(orc_ctx* c, double lx, double ly, double lz) {
+  const orc_config& g = c->cfg;
+  for (int k = 0; k <= c->km; ++k)
+    for (int j = 0; j <= c->jm; ++j)
+      for (int i = 0; i <= c->im; ++i) {
+        long p = c->h(i, j, k);
+        c->x[p] = lx / (double)g.ia * (double)i;
+        c->x[p + c->nh] = (g.ja == 0) ? ly : ly / (double)g.ja * (double)j;
+        c->x[p + 2 * c->nh] = (g.ka == 0) ? 0.0 : lz / (double)g.ka * (double)k;
+      }
+}
+
+// gridsendrecv single-rank branches, src/parallel.F90:2861-2866, 2930-2960,
+// 3010-3030
+static void gridsendrecv(orc_ctx* c) {
+  const int im = c->im, jm = c->jm, km = c->km;
+  const long nh = c->nh;
+  double* x = c->x.data();
+  if (c->cfg.ia > 0) {
+    for (int m = 0; m < 3; ++m)
+      for (int k = 0; k <= km; ++k)
+        for (int j = 0; j <= jm; ++j)
+          for (int n = 1; n <= HM; ++n) {
+            double* v = x + m * nh;
+            v[c->h(im + n, j, k)] = v[c->h(im, j, k)] + (v[c->h(n, j, k)] - v[c->h(0, j, k)]);
+            v[c->h(-n, j, k)] = v[c->h(0, j, k)] - (v[c->h(im, j, k)] - v[c->h(im - n, j, k)]);
+          }
+  }
+  if (c->cfg.ja == 0) {
+    for (int k = 0; k <= km; ++k)
+      for (int j = -HM; j <= HM; ++j)
+        for (int i = 0; i <= im; ++i) {
+          x[c->h(i, j, k)] = x[c->h(i, 0, k)];
+          x[c->h(i, j, k) + nh] = x[c->h(i, 0, k) + nh] + (double)j;
+          x[c->h(i, j, k) + 2 * nh] = x[c->h(i, 0, k) + 2 * nh];
+        }
+  } else {
+    for (int m = 0; m < 3; ++m)
+      for (int k = 0; k <= km; ++k)
+        for (int n = 1; n <= HM; ++n)
+          for (int i = 0; i <= im; ++i) {
+            double* v = x + m * nh;
+            v[c->h(i, jm + n, k)] = v[c->h(i, jm, k)] + (v[c->h(i, n, k)] - v[c->h(i, 0, k)]);
+            v[c->h(i, -n, k)] = v[c->h(i, 0, k)] - (v[c->h(i, jm, k)] - v[c->h(i, jm - n, k)]);
+          }
+  }
+  if (c->cfg.ka == 0) {
+    for (int k = -HM; k <= HM; ++k)
+      for (int j = 0; j <= jm; ++j)
+        for (int i = 0; i <= im; ++i) {
+          x[c->h(i, j, k)] = x[c->h(i, j, 0)];
+          x[c->h(i, j, k) + nh] = x[c->h(i, j, 0) + nh];
+          x[c->h(i, j, k) + 2 * nh] = x[c->h(i, j, 0) + 2 * nh] + (double)k;
+        }
+  } else {
+    for (int m = 0; m < 3; ++m)
+      for (int n = 1; n <= HM; ++n)
+        for (int j = 0; j <= jm; ++j)
+          for (int i = 0; i <= im; ++i) {
+            double* v = x + m * nh;
+            v[c->h(i, j, km + n)] = v[c->h(i, j, km)] + (v[c->h(i, j, n)] - v[c->h(i, j, 0)]);
+            v[c->h(i, j, -n)] = v[c->h(i, j, 0)] - (v[c->h(i, j, km)] - v[c->h(i, j, km - n)]);
+          }
+  }
+}
+
+// derivative of a halo-array line (direction d, transverse a,b) via the
+// context's compact scheme; out receives 0..dim.
+static void line_deriv(orc_ctx* c, int d, const double* var, int a, int b, LineBuf& lb, double* out) {
+  const int dim = c->dimof(d);
+  const long st = c->hstride(d);
+  const long p0 = hpos(*c, d, 0, a, b);
+  double* f = lb.f();
+  for (int l = -HM; l <= dim + HM; ++l) f[l] = var[p0 + st * l];
+  df_compact(c->fd[d], f, out, lb.d.data(), lb.xx.data());
+}
+
+// gridgeom, src/geom.F90:99-930 (the parts that produce dxi and jacob)
+void orc_gridgeom(orc_ctx* c) {
+  const int im = c->im, jm = c->jm, km = c->km;
+  const long nh = c->nh;
+  gridsendrecv(c);
+  std::vector<double> dx(9 * nh, 0.0);  // dx(:,:,:,m,d) -> comp m + 3*d
+  auto DX = [&](int m, int d) { return dx.data() + (long)(m + 3 * d) * nh; };
+  const double* x = c->x.data();
+  for (int d = 0; d < 3; ++d) {
+    int a1, b1;
+    trans_range(*c, d, a1, b1);
+    const int dim = c->dimof(d);
+    const long st = c->hstride(d);
+    for_lines(*c, d, 0, a1, 0, b1, [&](int a, int b) {
+      thread_local LineBuf* lb = nullptr;
+      thread_local std::vector<double>* ob = nullptr;
+      if (a < 0) {
+        delete lb; delete ob;
+        lb = new LineBuf(std::max(im, std::max(jm, km)));
+        ob = new std::vector<double>(std::max(im, std::max(jm, km)) + 1);
+        return;
+      }
+      for (int m = 0; m < 3; ++m) {
+        line_deriv(c, d, x + m * nh, a, b, *lb, ob->data());
+        long p0 = hpos(*c, d, 0, a, b);
+        for (int l = 0; l <= dim; ++l) DX(m, d)[p0 + st * l] = (*ob)[l];
+      }
+    });
+  }
+  for (int n = 0; n < 9; ++n) dataswap(*c, dx.data() + n * nh, 1, 0);
+  // Jacobian, src/geom.F90:350-385
+  double* J = c->jacob.data();
+  for (int k = 0; k <= km; ++k)
+    for (int j = 0; j <= jm; ++j)
+      for (int i = 0; i <= im; ++i) {
+        long p = c->h(i, j, k);
+        auto X = [&](int m, int d) { return DX(m - 1, d - 1)[p]; };
+        if (c->ndims == 3)
+          J[p] = X(1, 1) * X(2, 2) * X(3, 3) + X(1, 2) * X(2, 3) * X(3, 1) +
+                 X(1, 3) * X(2, 1) * X(3, 2) - X(1, 3) * X(2, 2) * X(3, 1) -
+                 X(1, 2) * X(2, 1) * X(3, 3) - X(1, 1) * X(2, 3) * X(3, 2);
+        else
+          J[p] = X(1, 1) * X(2, 2) - X(1, 2) * X(2, 1);
+      }
+  dataswap(*c, J, 1, 0);
+  // dxi, src/geom.F90:395-664 ; dxi(:,:,:,d,m) -> comp d + 3*m
+  std::fill(c->dxi.begin(), c->dxi.end(), 0.0);
+  auto DXI = [&](int d, int m) { return c->dxi.data() + (long)((d - 1) + 3 * (m - 1)) * nh; };
+  auto DXh = [&](int m, int d) { return DX(m - 1, d - 1); };
+  auto Xc = [&](int m) { return x + (long)(m - 1) * nh; };
+  if (c->ndims == 3) {
+    struct Term { int dd, mm; int am, ad, bm; int cm, cd, dm; };
+    // phi = 0.5*(dx(am,ad)*x(bm) - dx(cm,cd)*x(dm)), added to dxi(dd,mm)
+    const Term tx[6] = {{2, 1, 2, 3, 3, 3, 3, 2}, {2, 2, 3, 3, 1, 1, 3, 3}, {2, 3, 1, 3, 2, 2, 3, 1},
+                        {3, 1, 3, 2, 2, 2, 2, 3}, {3, 2, 1, 2, 3, 3, 2, 1}, {3, 3, 2, 2, 1, 1, 2, 2}};
+    const Term ty[6] = {{1, 1, 3, 3, 2, 2, 3, 3}, {1, 2, 1, 3, 3, 3, 3, 1}, {1, 3, 2, 3, 1, 1, 3, 2},
+                        {3, 1, 2, 1, 3, 3, 1, 2}, {3, 2, 3, 1, 1, 1, 1, 3}, {3, 3, 1, 1, 2, 2, 1, 1}};
+    const Term tz[6] = {{1, 1, 2, 2, 3, 3, 2, 2}, {1, 2, 3, 2, 1, 1, 2, 3}, {1, 3, 1, 2, 2, 2, 2, 1},
+                        {2, 1, 3, 1, 2, 2, 1, 3}, {2, 2, 1, 1, 3, 3, 1, 1}, {2, 3, 2, 1, 1, 1, 1, 2}};
+    const Term* tabs[3] = {tx, ty, tz};
+    for (int d = 0; d < 3; ++d) {
+      int a1, b1;
+      trans_range(*c, d, a1, b1);
+      const int dim = c->dimof(d);
+      const long st = c->hstride(d);
+      for_lines(*c, d, 0, a1, 0, b1, [&](int a, int b) {
+        thread_local LineBuf* lb = nullptr;
+        thread_local std::vector<double>* ob = nullptr;
+        if (a < 0) {
+          delete lb; delete ob;
+          lb = new LineBuf(std::max(im, std::max(jm, km)));
+          ob = new std::vector<double>(std::max(im, std::max(jm, km)) + 1);
+          return;
+        }
+        long p0 = hpos(*c, d, 0, a, b);
+        double* f = lb->f();
+        for (int t = 0; t < 6; ++t) {
+          const Term& T = tabs[d][t];
+          for (int l = -HM; l <= dim + HM; ++l) {
+            long p = p0 + st * l;
+            f[l] = 0.5 * (DXh(T.am, T.ad)[p] * Xc(T.bm)[p] - DXh(T.cm, T.cd)[p] * Xc(T.dm)[p]);
+          }
+          df_compact(c->fd[d], f, ob->data(), lb->d.data(), lb->xx.data());
+          double* o = DXI(T.dd, T.mm);
+          for (int l = 0; l <= dim; ++l) o[p0 + st * l] = o[p0 + st * l] + (*ob)[l];
+        }
+      });
+    }
+  } else {
+    for (int k = 0; k <= km; ++k)
+      for (int j = 0; j <= jm; ++j)
+        for (int i = 0; i <= im; ++i) {
+          long p = c->h(i, j, k);
+          DXI(1, 1)[p] = DXh(2, 2)[p];
+          DXI(1, 2)[p] = -DXh(1, 2)[p];
+          DXI(2, 1)[p] = -DXh(2, 1)[p];
+          DXI(2, 2)[p] = DXh(1, 1)[p];
+        }
+  }
+  for (int n = 0; n < 9; ++n) dataswap(*c, c->dxi.data() + n * nh, 1, 0);
+  for (int m = 1; m <= 3; ++m)
+    for (int d = 1; d <= 3; ++d)
+      for (int k = 0; k <= km; ++k)
+        for (int j = 0; j <= jm; ++j)
+          for (int i = 0; i <= im; ++i) {
+            long p = c->h(i, j, k);
+            DXI(d, m)[p] = DXI(d, m)[p] / J[p];
+          }
+  for (int n = 0; n < 9; ++n) dataswap(*c, c->dxi.data() + n * nh, 1, 0);
+}
+
+// tgvini + updateq (src/initialisation.F90:621-691 ; src/fludyna.F90:254-300)
+// or mini-app flowfield_init (miniapps/tgv_solver_3d/tgvsolver.F90:172-234).
+void orc_init_tgv(orc_ctx* c) {
+  const long nh = c->nh;
+  if (c->cfg.mode == ORC_MODE_MINIAPP) {
+    const double pinf = 1.0 / c->const2;
+    for (int k = 0; k <= c->km; ++k)
+      for (int j = 0; j <= c->jm; ++j)
+        for (int i = 0; i <= c->im; ++i) {
+          long p = c->h(i, j, k);
+          double x1 = 2.0 * PI / (double)c->im * (double)i;
+          double x2 = 2.0 * PI / (double)c->jm * (double)j;
+          double x3 = 2.0 * PI / (double)c->km * (double)k;
+          c->rho[p] = 1.0;
+          c->vel[p] = std::sin(x1) * std::cos(x2) * std::cos(x3);
+          c->vel[p + nh] = -std::cos(x1) * std::sin(x2) * std::cos(x3);
+          c->vel[p + 2 * nh] = 0.0;
+          c->prs[p] = pinf + 1.0 / 16.0 * (std::cos(2.0 * x1) + std::cos(2.0 * x2)) *
+                                 (std::cos(2.0 * x3) + 2.0);
+          c->tmp[p] = c->prs[p] / c->rho[p] * c->const2;
+          fvar2q_prs_node(*c, p);
+        }
+    return;
+  }
+  const double l0 = 1.0;
+  const double* x = c->x.data();
+  for (int k = 0; k <= c->km; ++k)
+    for (int j = 0; j <= c->jm; ++j)
+      for (int i = 0; i <= c->im; ++i) {
+        long p = c->h(i, j, k);
+        double X = x[p], Y = x[p + nh], Z = x[p + 2 * nh];
+        c->rho[p] = c->roinf;
+        c->vel[p] = c->uinf * std::sin(X / l0) * std::cos(Y / l0) * std::cos(Z / l0);
+        c->vel[p + nh] = -(c->uinf * std::cos(X / l0) * std::sin(Y / l0) * std::cos(Z / l0));
+        c->vel[p + 2 * nh] = 0.0;
+        c->prs[p] = c->pinf + c->rho[p] / 16.0 * (c->uinf * c->uinf) *
+                                  (std::cos(2.0 * X / l0) + std::cos(2.0 * Y / l0)) *
+                                  (std::cos(2.0 * Z / l0) + 2.0);
+        c->tmp[p] = c->prs[p] / c->rho[p] * c->const2;
+      }
+  orc_updateq(c);
+}
+
+// updateq -> fvar2q_3da with temperature (src/fludyna.F90:254-300, 480-533)
+void orc_updateq(orc_ctx* c) {
+  const long nh = c->nh;
+  for (int k = 0; k <= c->km; ++k)
+    for (int j = 0; j <= c->jm; ++j)
+      for (int i = 0; i <= c->im; ++i) {
+        long p = c->h(i, j, k);
+        double ro = c->rho[p], u = c->vel[p], v = c->vel[p + nh], w = c->vel[p + 2 * nh];
+        c->q[p] = ro;
+        c->q[p + nh] = ro * u;
+        c->q[p + 2 * nh] = ro * v;
+        c->q[p + 3 * nh] = ro * w;
+        c->q[p + 4 * nh] = ro * (c->tmp[p] * c->const1 + 0.5 * (u * u + v * v + w * w));
+      }
+}
+
+// ---------------------------------------------------------------------------
+// Hot path
+// ---------------------------------------------------------------------------
+
+// filterq, src/comsolver.F90:514-632 (mini-app: tgvsolver.F90:791-883).
+void orc_filterq(orc_ctx* c) {
+  const long nh = c->nh;
+  for (int d = 0; d < c->ndims; ++d) {
+    dataswap(*c, c->q.data(), 5, d + 1);
+    int a1, b1;
+    trans_range(*c, d, a1, b1);
+    const int dim = c->dimof(d);
+    const long st = c->hstride(d);
+    const int mx = std::max(c->im, std::max(c->jm, c->km));
+    for_lines(*c, d, 0, a1, 0, b1, [&](int a, int b) {
+      thread_local LineBuf* lb = nullptr;
+      if (a < 0) { delete lb; lb = new LineBuf(mx); return; }
+      long p0 = hpos(*c, d, 0, a, b);
+      double* f = lb->f();
+      std::vector<double>& out = lb->ob;
+      // filter all variables of the line first, then write back
+      // (q(0:dim,..,:) = fph), as the reference does
+      thread_local std::vector<double> res;
+      res.resize(5 * (dim + 1));
+      for (int n = 0; n < 5; ++n) {
+        const double* v = c->q.data() + n * nh;
+        for (int l = -HM; l <= dim + HM; ++l) f[l] = v[p0 + st * l];
+        compact_filter(c->flt[d], c->ft, f, out.data(), lb->d.data(), lb->xx.data());
+        for (int l = 0; l <= dim; ++l) res[n * (dim + 1) + l] = out[l];
+      }
+      for (int n = 0; n < 5; ++n) {
+        double* v = c->q.data() + n * nh;
+        for (int l = 0; l <= dim; ++l) v[p0 + st * l] = res[n * (dim + 1) + l];
+      }
+    });
+  }
+}
+
+// qswap single-rank periodic branches, src/parallel.F90:4876-4920,
+// 5018-5065, 5159-5206.  Non-periodic directions on one rank exchange
+// nothing (MPI_PROC_NULL neighbours).
+void orc_qswap(orc_ctx* c) {
+  const int im = c->im, jm = c->jm, km = c->km;
+  const long nh = c->nh;
+  double* q = c->q.data();
+  if (c->homo(0)) {
+    for (int n = 0; n < 5; ++n)
+      for (int k = 0; k <= km; ++k)
+        for (int j = 0; j <= jm; ++j) {
+          double* v = q + n * nh;
+          for (int i = -HM; i <= -1; ++i) v[c->h(i, j, k)] = v[c->h(im + i, j, k)];
+          for (int i = im + 1; i <= im + HM; ++i) v[c->h(i, j, k)] = v[c->h(i - im, j, k)];
+          v[c->h(0, j, k)] = 0.5 * (v[c->h(0, j, k)] + v[c->h(im, j, k)]);
+          v[c->h(im, j, k)] = v[c->h(0, j, k)];
+        }
+    q2fvar_box(*c, im, im + HM, 0, jm, 0, km);
+    q2fvar_box(*c, -HM, 0, 0, jm, 0, km);
+  }
+  if (c->homo(1)) {
+    for (int n = 0; n < 5; ++n)
+      for (int k = 0; k <= km; ++k) {
+        double* v = q + n * nh;
+        if (jm == 0) {
+          for (int j = -HM; j <= HM; ++j)
+            for (int i = 0; i <= im; ++i) v[c->h(i, j, k)] = v[c->h(i, 0, k)];
+        } else {
+          for (int j = -HM; j <= -1; ++j)
+            for (int i = 0; i <= im; ++i) v[c->h(i, j, k)] = v[c->h(i, jm + j, k)];
+          for (int j = jm + 1; j <= jm + HM; ++j)
+            for (int i = 0; i <= im; ++i) v[c->h(i, j, k)] = v[c->h(i, j - jm, k)];
+          for (int i = 0; i <= im; ++i) {
+            v[c->h(i, 0, k)] = 0.5 * (v[c->h(i, 0, k)] + v[c->h(i, jm, k)]);
+            v[c->h(i, jm, k)] = v[c->h(i, 0, k)];
+          }
+        }
+      }
+    q2fvar_box(*c, 0, im, -HM, 0, 0, km);
+    q2fvar_box(*c, 0, im, jm, jm + HM, 0, km);
+  }
+  if (c->homo(2)) {
+    for (int n = 0; n < 5; ++n) {
+      double* v = q + n * nh;
+      if (c->cfg.ka == 0) {
+        for (int k = -HM; k <= HM; ++k)
+          for (int j = 0; j <= jm; ++j)
+            for (int i = 0; i <= im; ++i) v[c->h(i, j, k)] = v[c->h(i, j, 0)];
+      } else {
+        for (int k = -HM; k <= -1; ++k)
+          for (int j = 0; j <= jm; ++j)
+            for (int i = 0; i <= im; ++i) v[c->h(i, j, k)] = v[c->h(i, j, km + k)];
+        for (int k = km + 1; k <= km + HM; ++k)
+          for (int j = 0; j <= jm; ++j)
+            for (int i = 0; i <= im; ++i) v[c->h(i, j, k)] = v[c->h(i, j, k - km)];
+        for (int j = 0; j <= jm; ++j)
+          for (int i = 0; i <= im; ++i) {
+            v[c->h(i, j, 0)] = 0.5 * (v[c->h(i, j, 0)] + v[c->h(i, j, km)]);
+            v[c->h(i, j, km)] = v[c->h(i, j, 0)];
+          }
+      }
+    }
+    q2fvar_box(*c, 0, im, 0, jm, -HM, 0);
+    q2fvar_box(*c, 0, im, 0, jm, km, km + HM);
+  }
+}
+
+void orc_boucon(orc_ctx* c) { (void)c; }
+
+// gradcal, src/comsolver.F90:244-497 (main) ; tgvsolver.F90:450-537 (mini-app)
+void orc_gradcal(orc_ctx* c) {
+  const long nh = c->nh, n0 = c->n0;
+  const bool mini = c->cfg.mode == ORC_MODE_MINIAPP;
+  if (!mini) {
+    std::fill(c->dvel.begin(), c->dvel.end(), 0.0);
+    std::fill(c->dtmp.begin(), c->dtmp.end(), 0.0);
+  }
+  const int mx = std::max(c->im, std::max(c->jm, c->km));
+  for (int d = 0; d < c->ndims; ++d) {
+    int a1, b1;
+    trans_range(*c, d, a1, b1);
+    const int dim = c->dimof(d);
+    const long sz = c->zstride(d);
+    const double hdx = d == 0 ? c->dxm : (d == 1 ? c->dym : c->dzm);
+    for_lines(*c, d, 0, a1, 0, b1, [&](int a, int b) {
+      thread_local LineBuf* lb = nullptr;
+      thread_local std::vector<double> df;
+      if (a < 0) { delete lb; lb = new LineBuf(mx); df.resize(4 * (mx + 1)); return; }
+      const double* src[4] = {c->vel.data(), c->vel.data() + nh, c->vel.data() + 2 * nh, c->tmp.data()};
+      for (int n = 0; n < 4; ++n) line_deriv(c, d, src[n], a, b, *lb, df.data() + n * (dim + 1));
+      long z0 = zpos(*c, d, 0, a, b);
+      long h0 = hpos(*c, d, 0, a, b);
+      const long hs = c->hstride(d);
+      for (int l = 0; l <= dim; ++l) {
+        long zp = z0 + sz * l, hp = h0 + hs * l;
+        if (mini) {
+          for (int n = 0; n < 3; ++n) c->dvel[zp + (n + 3 * d) * n0] = df[n * (dim + 1) + l] / hdx;
+          c->dtmp[zp + d * n0] = df[3 * (dim + 1) + l] / hdx;
+        } else {
+          for (int n = 0; n < 3; ++n)
+            for (int m = 0; m < 3; ++m) {
+              double& g = c->dvel[zp + (n + 3 * m) * n0];
+              g = g + df[n * (dim + 1) + l] * c->dxi[hp + (d + 3 * m) * nh];
+            }
+          for (int m = 0; m < 3; ++m) {
+            double& g = c->dtmp[zp + m * n0];
+            g = g + df[3 * (dim + 1) + l] * c->dxi[hp + (d + 3 * m) * nh];
+          }
+        }
+      }
+    });
+  }
+}
+
+// convrsdcal6, src/solver.F90:2173-2341 (main) ; convection,
+// tgvsolver.F90:539-633 (mini-app)
+void orc_convrsdcal6(orc_ctx* c) {
+  const long nh = c->nh, n0 = c->n0;
+  const bool mini = c->cfg.mode == ORC_MODE_MINIAPP;
+  const int mx = std::max(c->im, std::max(c->jm, c->km));
+  for (int d = 0; d < c->ndims; ++d) {
+    const int dim = c->dimof(d);
+    const long hs = c->hstride(d), sz = c->zstride(d);
+    int a0, a1, b0, b1, l0, l1;
+    if (mini) {
+      a0 = 0; b0 = 0; trans_range(*c, d, a1, b1); l0 = 0; l1 = dim;
+    } else if (d == 0) { a0 = c->js; a1 = c->je; b0 = c->ks; b1 = c->ke; l0 = c->is; l1 = c->ie; }
+    else if (d == 1) { a0 = c->is; a1 = c->ie; b0 = c->ks; b1 = c->ke; l0 = c->js; l1 = c->je; }
+    else { a0 = c->is; a1 = c->ie; b0 = c->js; b1 = c->je; l0 = c->ks; l1 = c->ke; }
+    const double hdx = d == 0 ? c->dxm : (d == 1 ? c->dym : c->dzm);
+    for_lines(*c, d, a0, a1, b0, b1, [&](int a, int b) {
+      thread_local LineBuf* lb = nullptr;
+      thread_local std::vector<double> fcs, dfc;
+      if (a < 0) {
+        delete lb; lb = new LineBuf(mx);
+        fcs.resize(5 * (mx + 2 * HM + 1)); dfc.resize(5 * (mx + 1));
+        return;
+      }
+      const long h0 = hpos(*c, d, 0, a, b);
+      const int L = dim + 2 * HM + 1;
+      const double* q = c->q.data();
+      const double* J = c->jacob.data();
+      for (int l = -HM; l <= dim + HM; ++l) {
+        long p = h0 + hs * l;
+        double* F = fcs.data() + (l + HM);
+        double q1 = q[p], q2 = q[p + nh], q3 = q[p + 2 * nh], q4 = q[p + 3 * nh], q5 = q[p + 4 * nh];
+        double pr = c->prs[p];
+        if (mini) {
+          double uu = c->vel[p + d * nh];
+          F[0] = q1 * uu;
+          F[L] = q2 * uu;
+          F[2 * L] = q3 * uu;
+          F[3 * L] = q4 * uu;
+          F[(1 + d) * L] = F[(1 + d) * L] + pr;
+          F[4 * L] = (q5 + pr) * uu;
+        } else {
+          const double* X = c->dxi.data() + p;
+          double x1 = X[(d + 0) * nh], x2 = X[(d + 3) * nh], x3 = X[(d + 6) * nh];
+          double uu = x1 * c->vel[p] + x2 * c->vel[p + nh] + x3 * c->vel[p + 2 * nh];
+          double jj = J[p];
+          F[0] = jj * q1 * uu;
+          F[L] = jj * (q2 * uu + x1 * pr);
+          F[2 * L] = jj * (q3 * uu + x2 * pr);
+          F[3 * L] = jj * (q4 * uu + x3 * pr);
+          F[4 * L] = jj * (q5 + pr) * uu;
+        }
+      }
+      for (int n = 0; n < 5; ++n)
+        df_compact(c->fd[d], fcs.data() + n * L + HM, dfc.data() + n * (dim + 1), lb->d.data(),
+                   lb->xx.data());
+      const long z0 = zpos(*c, d, 0, a, b);
+      for (int n = 0; n < 5; ++n)
+        for (int l = l0; l <= l1; ++l) {
+          double& r = c->qrhs[z0 + sz * l + n * n0];
+          if (mini) r = r + dfc[n * (dim + 1) + l] / hdx;
+          else r = r + dfc[n * (dim + 1) + l];
+        }
+    });
+  }
+}
+
+// diffrsdcal6, src/solver.F90:2354-2873 (turbmode none, no species) ;
+// diffusion, tgvsolver.F90:635-789 (mini-app)
+void orc_diffrsdcal6(orc_ctx* c) {
+  const long nh = c->nh, n0 = c->n0;
+  const bool mini = c->cfg.mode == ORC_MODE_MINIAPP;
+  std::fill(c->sigma.begin(), c->sigma.end(), 0.0);
+  std::fill(c->qflux.begin(), c->qflux.end(), 0.0);
+  const double re = c->cfg.reynolds, pr = c->cfg.prandtl;
+#pragma omp parallel for collapse(2)
+  for (int k = 0; k <= c->km; ++k)
+    for (int j = 0; j <= c->jm; ++j)
+      for (int i = 0; i <= c->im; ++i) {
+        long p = c->h(i, j, k), zp = c->z(i, j, k);
+        double T = c->tmp[p];
+        // miucal, src/fludyna.F90:791-820
+        double miu = T * std::sqrt(T) * c->tempconst1 / (T + c->tempconst) / re;
+        auto dv = [&](int n, int m) { return c->dvel[zp + ((n - 1) + 3 * (m - 1)) * n0]; };
+        double s11 = dv(1, 1);
+        double s12 = 0.5 * (dv(1, 2) + dv(2, 1));
+        double s13 = 0.5 * (dv(1, 3) + dv(3, 1));
+        double s22 = dv(2, 2);
+        double s23 = 0.5 * (dv(2, 3) + dv(3, 2));
+        double s33 = dv(3, 3);
+        double skk = NUM1D3 * (s11 + s22 + s33);
+        double miu2 = 2.0 * miu;
+        double hcc = (miu / pr) / c->const5;
+        double* S = c->sigma.data() + p;
+        S[0] = miu2 * (s11 - skk);
+        S[nh] = miu2 * s12;
+        S[2 * nh] = miu2 * s13;
+        S[3 * nh] = miu2 * (s22 - skk);
+        S[4 * nh] = miu2 * s23;
+        S[5 * nh] = miu2 * (s33 - skk);
+        double u = c->vel[p], v = c->vel[p + nh], w = c->vel[p + 2 * nh];
+        double* Q = c->qflux.data() + p;
+        const double* dT = c->dtmp.data() + zp;
+        Q[0] = hcc * dT[0] + S[0] * u + S[nh] * v + S[2 * nh] * w;
+        Q[nh] = hcc * dT[n0] + S[nh] * u + S[3 * nh] * v + S[4 * nh] * w;
+        Q[2 * nh] = hcc * dT[2 * n0] + S[2 * nh] * u + S[4 * nh] * v + S[5 * nh] * w;
+      }
+  dataswap(*c, c->sigma.data(), 6, 0);
+  dataswap(*c, c->qflux.data(), 3, 0);
+  // sigma components needed per direction: (1,2,3) (2,4,5) (3,5,6)
+  const int sidx[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+  const int mx = std::max(c->im, std::max(c->jm, c->km));
+  for (int d = 0; d < c->ndims; ++d) {
+    const int dim = c->dimof(d);
+    const long hs = c->hstride(d), sz = c->zstride(d);
+    int a1, b1;
+    trans_range(*c, d, a1, b1);
+    int l0, l1;
+    if (mini) { l0 = 0; l1 = dim; }
+    else if (d == 0) { l0 = c->is; l1 = c->ie; }
+    else if (d == 1) { l0 = c->js; l1 = c->je; }
+    else { l0 = c->ks; l1 = c->ke; }
+    const double hdx = d == 0 ? c->dxm : (d == 1 ? c->dym : c->dzm);
+    for_lines(*c, d, 0, a1, 0, b1, [&](int a, int b) {
+      thread_local LineBuf* lb = nullptr;
+      thread_local std::vector<double> ff, df;
+      if (a < 0) {
+        delete lb; lb = new LineBuf(mx);
+        ff.resize(4 * (mx + 2 * HM + 1)); df.resize(4 * (mx + 1));
+        return;
+      }
+      const long h0 = hpos(*c, d, 0, a, b);
+      const int L = dim + 2 * HM + 1;
+      const double* S = c->sigma.data();
+      const double* Q = c->qflux.data();
+      for (int l = -HM; l <= dim + HM; ++l) {
+        long p = h0 + hs * l;
+        double* F = ff.data() + (l + HM);
+        if (mini) {
+          F[0] = S[p + sidx[d][0] * nh];
+          F[L] = S[p + sidx[d][1] * nh];
+          F[2 * L] = S[p + sidx[d][2] * nh];
+          F[3 * L] = Q[p + d * nh];
+        } else {
+          const double* X = c->dxi.data() + p;
+          double x1 = X[(d + 0) * nh], x2 = X[(d + 3) * nh], x3 = X[(d + 6) * nh];
+          double jj = c->jacob[p];
+          F[0] = (S[p] * x1 + S[p + nh] * x2 + S[p + 2 * nh] * x3) * jj;
+          F[L] = (S[p + nh] * x1 + S[p + 3 * nh] * x2 + S[p + 4 * nh] * x3) * jj;
+          F[2 * L] = (S[p + 2 * nh] * x1 + S[p + 4 * nh] * x2 + S[p + 5 * nh] * x3) * jj;
+          F[3 * L] = (Q[p] * x1 + Q[p + nh] * x2 + Q[p + 2 * nh] * x3) * jj;
+        }
+      }
+      for (int n = 0; n < 4; ++n)
+        df_compact(c->fd[d], ff.data() + n * L + HM, df.data() + n * (dim + 1), lb->d.data(),
+                   lb->xx.data());
+      const long z0 = zpos(*c, d, 0, a, b);
+      for (int n = 0; n < 4; ++n)
+        for (int l = l0; l <= l1; ++l) {
+          double& r = c->qrhs[z0 + sz * l + (n + 1) * n0];
+          if (mini) r = r + df[n * (dim + 1) + l] / hdx;
+          else r = r + df[n * (dim + 1) + l];
+        }
+    });
+  }
+}
+
+// rhscal, src/solver.F90:185-282 (main) ; tgvsolver.F90:962-992 (mini-app)
+void orc_rhscal(orc_ctx* c) {
+  orc_convrsdcal6(c);
+  for (auto& r : c->qrhs) r = -r;
+  if (c->cfg.diffterm) orc_diffrsdcal6(c);
+}
+
+// updatefvar -> q2fvar_3da on 0:im (src/fludyna.F90:191-242)
+void orc_updatefvar(orc_ctx* c) { q2fvar_box(*c, 0, c->im, 0, c->jm, 0, c->km); }
+
+// bchomo, tgvsolver.F90:271-369
+void orc_bchomo(orc_ctx* c) {
+  const int im = c->im, jm = c->jm, km = c->km;
+  const long nh = c->nh;
+  auto copy = [&](long dst, long src) {
+    c->rho[dst] = c->rho[src];
+    for (int n = 0; n < 3; ++n) c->vel[dst + n * nh] = c->vel[src + n * nh];
+    c->tmp[dst] = c->tmp[src];
+    c->prs[dst] = c->prs[src];
+    fvar2q_prs_node(*c, dst);
+  };
+  for (int k = 0; k <= km; ++k)
+    for (int j = 0; j <= jm; ++j) {
+      for (int i = -HM; i <= -1; ++i) copy(c->h(i, j, k), c->h(im + i, j, k));
+      for (int i = im + 1; i <= im + HM; ++i) copy(c->h(i, j, k), c->h(i - im, j, k));
+    }
+  for (int k = 0; k <= km; ++k)
+    for (int i = 0; i <= im; ++i) {
+      for (int j = -HM; j <= -1; ++j) copy(c->h(i, j, k), c->h(i, jm + j, k));
+      for (int j = jm + 1; j <= jm + HM; ++j) copy(c->h(i, j, k), c->h(i, j - jm, k));
+    }
+  for (int j = 0; j <= jm; ++j)
+    for (int i = 0; i <= im; ++i) {
+      for (int k = -HM; k <= -1; ++k) copy(c->h(i, j, k), c->h(i, j, km + k));
+      for (int k = km + 1; k <= km + HM; ++k) copy(c->h(i, j, k), c->h(i, j, k - km));
+    }
+}
+
+// kenergycal / enstophycal, src/statistic.F90:871-992 ;
+// mini-app stacal, tgvsolver.F90:893-942
+double orc_kenergy(orc_ctx* c) {
+  const long nh = c->nh;
+  double s = 0.0;
+  const int k0 = c->ndims == 3 ? 1 : 0, k1 = c->ndims == 3 ? c->km : 0;
+  for (int k = k0; k <= k1; ++k)
+    for (int j = 1; j <= c->jm; ++j)
+      for (int i = 1; i <= c->im; ++i) {
+        long p = c->h(i, j, k);
+        double u = c->vel[p], v = c->vel[p + nh], w = c->vel[p + 2 * nh];
+        double var1 = u * u + v * v + w * w;
+        s = s + c->rho[p] * var1;
+      }
+  double npts = c->ndims == 3 ? (double)c->cfg.ia * c->cfg.ja * c->cfg.ka
+                              : (double)c->cfg.ia * c->cfg.ja;
+  if (c->cfg.mode == ORC_MODE_MINIAPP) return 0.5 * s / npts;
+  return 0.5 * s / npts / (c->roinf * c->uinf * c->uinf);
+}
+
+double orc_enstrophy(orc_ctx* c) {
+  const long n0 = c->n0;
+  double s = 0.0;
+  const int k0 = c->ndims == 3 ? 1 : 0, k1 = c->ndims == 3 ? c->km : 0;
+  for (int k = k0; k <= k1; ++k)
+    for (int j = 1; j <= c->jm; ++j)
+      for (int i = 1; i <= c->im; ++i) {
+        long zp = c->z(i, j, k);
+        auto dv = [&](int n, int m) { return c->dvel[zp + ((n - 1) + 3 * (m - 1)) * n0]; };
+        double o1 = dv(3, 2) - dv(2, 3), o2 = dv(1, 3) - dv(3, 1), o3 = dv(2, 1) - dv(1, 2);
+        double om = c->ndims == 3 ? o1 * o1 + o2 * o2 + o3 * o3 : o3 * o3;
+        s = s + c->rho[c->h(i, j, k)] * om;
+      }
+  double npts = c->ndims == 3 ? (double)c->cfg.ia * c->cfg.ja * c->cfg.ka
+                              : (double)c->cfg.ia * c->cfg.ja;
+  if (c->cfg.mode == ORC_MODE_MINIAPP) return 0.5 * s / npts;
+  double xmax = c->x[c->h(c->im, 0, 0)];
+  double l0 = xmax / (2.0 * PI);
+  return 0.5 * s / npts / (c->roinf * ((c->uinf / l0) * (c->uinf / l0)));
+}
+
+// One RK3 step.  Main ordering: time_integration_rk, src/mainloop.F90:396-486.
+// Mini-app ordering: rk3, tgvsolver.F90:994-1082.
+void orc_rk3_step(orc_ctx* c, double* stats) {
+  static const double rk[3][3] = {{1.0, 0.0, 1.0}, {0.75, 0.25, 0.25}, {NUM1D3, NUM2D3, NUM2D3}};
+  const long nh = c->nh, n0 = c->n0;
+  const int im = c->im, jm = c->jm, km = c->km;
+  const double dt = c->cfg.deltat;
+  const bool mini = c->cfg.mode == ORC_MODE_MINIAPP;
+  for (int s = 0; s < 3; ++s) {
+    if (mini) {
+      orc_bchomo(c);
+      std::fill(c->qrhs.begin(), c->qrhs.end(), 0.0);
+      orc_gradcal(c);
+      orc_rhscal(c);
+      if (s == 0) {
+        if (stats) { stats[0] = orc_kenergy(c); stats[1] = orc_enstrophy(c); }
+        for (int n = 0; n < 5; ++n)
+          for (int k = 0; k <= km; ++k)
+            for (int j = 0; j <= jm; ++j)
+              for (int i = 0; i <= im; ++i)
+                c->qsave[c->z(i, j, k) + n * n0] = c->q[c->h(i, j, k) + n * nh];
+      }
+#pragma omp parallel for collapse(2)
+      for (int n = 0; n < 5; ++n)
+        for (int k = 0; k <= km; ++k)
+          for (int j = 0; j <= jm; ++j)
+            for (int i = 0; i <= im; ++i) {
+              long p = c->h(i, j, k) + n * nh, zp = c->z(i, j, k) + n * n0;
+              c->q[p] = rk[s][0] * c->qsave[zp] + rk[s][1] * c->q[p] + rk[s][2] * c->qrhs[zp] * dt;
+            }
+      orc_filterq(c);
+      orc_updatefvar(c);
+    } else {
+      if (c->cfg.lfilter) orc_filterq(c);
+      std::fill(c->qrhs.begin(), c->qrhs.end(), 0.0);
+      orc_boucon(c);
+      orc_qswap(c);
+      orc_gradcal(c);
+      if (s == 0) {
+        for (int n = 0; n < 5; ++n)
+          for (int k = 0; k <= km; ++k)
+            for (int j = 0; j <= jm; ++j)
+              for (int i = 0; i <= im; ++i) {
+                long p = c->h(i, j, k);
+                c->qsave[c->z(i, j, k) + n * n0] = c->q[p + n * nh] * c->jacob[p];
+              }
+        if (stats) { stats[0] = orc_kenergy(c); stats[1] = orc_enstrophy(c); }
+      }
+      orc_rhscal(c);
+#pragma omp parallel for collapse(2)
+      for (int n = 0; n < 5; ++n)
+        for (int k = 0; k <= km; ++k)
+          for (int j = 0; j <= jm; ++j)
+            for (int i = 0; i <= im; ++i) {
+              long p = c->h(i, j, k), zp = c->z(i, j, k) + n * n0;
+              double J = c->jacob[p];
+              double v = rk[s][0] * c->qsave[zp] + rk[s][1] * c->q[p + n * nh] * J +
+                         rk[s][2] * c->qrhs[zp] * dt;
+              c->q[p + n * nh] = v / J;
+            }
+      orc_updatefvar(c);
+    }
+  }
+}
+
+void orc_rk3_steps(orc_ctx* c, int nsteps, double* stats) {
+  for (int s = 0; s < nsteps; ++s) orc_rk3_step(c, stats ? stats + 2 * s : nullptr);
+}
+
+void orc_line_derivative(orc_ctx* c, int dir, const double* f, double* df) {
+  LineBuf lb(c->dimof(dir));
+  df_compact(c->fd[dir], f + HM, df, lb.d.data(), lb.xx.data());
+}
+
+void orc_line_filter(orc_ctx* c, int dir, const double* f, double* ff) {
+  LineBuf lb(c->dimof(dir));
+  compact_filter(c->flt[dir], c->ft, f + HM, ff, lb.d.data(), lb.xx.data());
+}
+
+}  // extern "C"
