@@ -1,0 +1,168 @@
+"""ctypes binding of the C ABI in ``include/astr_gpu.h``.
+
+This is the same binding a Python or Fortran (ISO_C_BINDING) host makes: plain
+pointers to host arrays in the reference's Fortran layout.  The library is
+the in-tree sm_103a build (``astr_gb300/_build/libastr_gb300.so``); there is
+no CPU fallback, and loading fails loudly when it is missing.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libastr_gb300.so")
+
+ASTR_OK = 0
+ASTR_ERR_ARG = -1
+ASTR_ERR_OOM = -2
+ASTR_ERR_CUDA = -3
+ASTR_ERR_UNSUPPORTED = -4
+ASTR_ERR_NONFINITE = -5
+ASTR_ERR_STATE = -6
+
+ORDER_MAIN = 0
+ORDER_MINIAPP = 1
+FP64 = 0
+FP32_STORAGE = 1
+
+# Every symbol the header declares (checked by the CPU test suite).
+EXPORTS = [
+    "astr_gpu_create", "astr_gpu_destroy", "astr_gpu_set_metrics", "astr_gpu_upload_state",
+    "astr_gpu_download_state", "astr_gpu_download_rhs", "astr_gpu_rk3_step", "astr_gpu_filterq",
+    "astr_gpu_qswap", "astr_gpu_gradcal", "astr_gpu_rhscal", "astr_gpu_updatefvar",
+    "astr_gpu_reduce_stats", "astr_gpu_synchronize", "astr_gpu_last_error",
+    "astr_gpu_footprint", "astr_gpu_launch_count", "astr_gpu_set_metrics_diag",
+    "astr_gpu_host_alloc", "astr_gpu_host_free", "astr_gpu_timed_steps",
+    "astr_gpu_set_profiling", "astr_gpu_kernel_times", "astr_gpu_measure_fp64_peak",
+]
+KERNEL_CLASSES = ["filter", "halo", "convgrad", "visc", "pointwise", "stats"]
+
+
+class AstrDims(ctypes.Structure):
+    _fields_ = [("im", ctypes.c_int), ("jm", ctypes.c_int), ("km", ctypes.c_int),
+                ("ia", ctypes.c_int), ("ja", ctypes.c_int), ("ka", ctypes.c_int),
+                ("npdci", ctypes.c_int), ("npdcj", ctypes.c_int), ("npdck", ctypes.c_int)]
+
+
+class AstrParams(ctypes.Structure):
+    _fields_ = [("order", ctypes.c_int), ("precision", ctypes.c_int),
+                ("lfilter", ctypes.c_int), ("diffterm", ctypes.c_int),
+                ("alfa_filter", ctypes.c_double), ("beter_halo", ctypes.c_double),
+                ("beter_bound", ctypes.c_double), ("mach", ctypes.c_double),
+                ("reynolds", ctypes.c_double), ("prandtl", ctypes.c_double),
+                ("ref_tem", ctypes.c_double), ("suth_const", ctypes.c_double),
+                ("deltat", ctypes.c_double)]
+
+
+class AstrStatus(ctypes.Structure):
+    _fields_ = [("kenergy", ctypes.c_double), ("enstrophy", ctypes.c_double),
+                ("crash", ctypes.c_int)]
+
+
+class AstrError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"astr_gpu error {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load the C-ABI library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"astr_gb300 CUDA library not built: {path} "
+                           "(run python -c 'import __graft_entry__ as g; g.build()')")
+    L = ctypes.CDLL(path)
+    vp, dp, ip = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_int
+    L.astr_gpu_create.argtypes = [ctypes.POINTER(AstrDims), ctypes.POINTER(AstrParams),
+                                  ctypes.POINTER(vp)]
+    L.astr_gpu_create.restype = ip
+    L.astr_gpu_destroy.argtypes = [vp]
+    L.astr_gpu_destroy.restype = None
+    L.astr_gpu_set_metrics.argtypes = [vp, dp, dp]
+    L.astr_gpu_upload_state.argtypes = [vp, dp, dp, dp, dp, dp]
+    L.astr_gpu_download_state.argtypes = [vp, dp, dp, dp, dp, dp]
+    L.astr_gpu_download_rhs.argtypes = [vp, dp, dp, dp]
+    L.astr_gpu_rk3_step.argtypes = [vp, ip, dp, ctypes.POINTER(AstrStatus)]
+    for n in ("astr_gpu_filterq", "astr_gpu_qswap", "astr_gpu_gradcal", "astr_gpu_rhscal",
+              "astr_gpu_updatefvar", "astr_gpu_synchronize"):
+        getattr(L, n).argtypes = [vp]
+        getattr(L, n).restype = ip
+    L.astr_gpu_reduce_stats.argtypes = [vp, dp, dp]
+    L.astr_gpu_last_error.argtypes = [vp, ctypes.c_char_p, ip]
+    L.astr_gpu_footprint.argtypes = [ctypes.POINTER(AstrDims), ctypes.POINTER(AstrParams)]
+    L.astr_gpu_footprint.restype = ctypes.c_size_t
+    L.astr_gpu_launch_count.argtypes = [vp]
+    L.astr_gpu_launch_count.restype = ctypes.c_longlong
+    L.astr_gpu_set_metrics_diag.argtypes = [vp, dp, dp, dp, dp]
+    L.astr_gpu_set_metrics_diag.restype = ip
+    L.astr_gpu_host_alloc.argtypes = [ctypes.c_size_t]
+    L.astr_gpu_host_alloc.restype = vp
+    L.astr_gpu_host_free.argtypes = [vp]
+    L.astr_gpu_host_free.restype = None
+    L.astr_gpu_timed_steps.argtypes = [vp, ip, dp]
+    L.astr_gpu_timed_steps.restype = ip
+    L.astr_gpu_set_profiling.argtypes = [vp, ip]
+    L.astr_gpu_set_profiling.restype = ip
+    L.astr_gpu_kernel_times.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_longlong), ip]
+    L.astr_gpu_kernel_times.restype = ip
+    L.astr_gpu_measure_fp64_peak.argtypes = [dp]
+    L.astr_gpu_measure_fp64_peak.restype = ip
+    for n in ("astr_gpu_set_metrics", "astr_gpu_upload_state", "astr_gpu_download_state",
+              "astr_gpu_download_rhs", "astr_gpu_rk3_step", "astr_gpu_reduce_stats"):
+        getattr(L, n).restype = ip
+    _lib = L
+    return L
+
+
+def dptr(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float64
+    assert a.flags.f_contiguous or a.flags.c_contiguous
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class PinnedArray:
+    """A numpy array over page-locked host memory (astr_gpu_host_alloc)."""
+
+    def __init__(self, shape, dtype=np.float64, order="F"):
+        L = load()
+        self.nbytes = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        self.ptr = L.astr_gpu_host_alloc(self.nbytes)
+        if not self.ptr:
+            raise MemoryError(f"astr_gpu_host_alloc({self.nbytes}) failed")
+        buf = (ctypes.c_char * self.nbytes).from_address(self.ptr)
+        self.array = np.frombuffer(buf, dtype=dtype).reshape(shape, order=order)
+
+    def free(self):
+        if self.ptr:
+            self.array = None
+            load().astr_gpu_host_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def last_error(h) -> str:
+    L = load()
+    buf = ctypes.create_string_buffer(1024)
+    L.astr_gpu_last_error(h, buf, 1024)
+    return buf.value.decode(errors="replace")
+
+
+def check(h, rc: int):
+    if rc != ASTR_OK:
+        raise AstrError(rc, last_error(h))
+    return rc

@@ -1,0 +1,287 @@
+"""Host-side set-up of the configurations the hot path is measured on.
+
+Grid metrics and initial states are inputs of the hot path: a Fortran host
+passes its own (``astr_gpu_set_metrics``); the benchmark and the serving loop
+build them here.  ``rect_metrics`` restates ``gridgeom`` (src/geom.F90:
+99-930) for rectilinear grids, x = x(i), y = y(j), z = z(k), with the same
+floating-point operations in the same order: arrays are held with singleton
+axes where a field is constant, and numpy broadcasting applies the
+reference's element-wise arithmetic.  The compact derivative along an axis
+is ``fd_scheme_initiate`` + ``df_compact`` (src/derivative.F90:63-306) with
+the Thomas recurrences of src/commfunc.F90:752-813, vectorised over lines.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+HM = 5
+PI = 4.0 * np.arctan(1.0)
+NUM1D3 = 1.0 / 3.0
+NUM7D9 = 7.0 / 9.0
+NUM1D36 = 1.0 / 36.0
+NUM1D60 = 1.0 / 60.0
+
+
+# ---------------------------------------------------------------------------
+# compact first derivative along one axis (arrays hold halo nodes -5..dim+5)
+# ---------------------------------------------------------------------------
+def _scheme(ntype: int, dim: int):
+    """fd_scheme_initiate ('643c') + tridiagonal_thomas_proprocess."""
+    i0, imx = (0, dim) if ntype == 4 else (-1, dim + 1)
+    n = imx - i0 + 1
+    a = np.full(n, NUM1D3)
+    c = np.full(n, NUM1D3)
+    a[0] = c[0] = 0.0
+    a[-1] = c[-1] = 0.0
+    if ntype == 4:
+        a[0] = c[0] = 2.0
+        a[1] = c[1] = 0.25
+        a[-1] = c[-1] = 2.0
+        a[-2] = c[-2] = 0.25
+    ac1 = np.zeros(n)
+    ac2 = np.zeros(n)
+    ac3 = np.zeros(n)
+    ac1[0] = c[0]
+    for i in range(1, n):
+        ac1[i] = c[i] / (1.0 - a[i] * ac1[i - 1])
+        ac2[i] = 1.0 / (1.0 - a[i] * ac1[i - 1])
+        ac3[i] = a[i] / (1.0 - a[i] * ac1[i - 1])
+    return i0, n, ac1, ac2, ac3
+
+
+def compact_deriv(f: np.ndarray, axis: int, ntype: int, dim: int) -> np.ndarray:
+    """Index-space derivative of f along `axis` (length dim+11, halo first)
+    at nodes 0..dim, exactly as df_compact (src/derivative.F90:171-306)."""
+    f = np.moveaxis(np.asarray(f, dtype=np.float64), axis, 0)
+    i0, n, ac1, ac2, ac3 = _scheme(ntype, dim)
+
+    def F(j):  # node j -> array slab
+        return f[j + HM]
+
+    d = np.empty((n,) + f.shape[1:])
+    rows = range(n)
+    for r in rows:
+        j = i0 + r
+        if ntype == 4 and r == 0:
+            d[r] = -2.5 * F(j) + 2.0 * F(j + 1) + 0.5 * F(j + 2)
+        elif ntype == 4 and (r == 1 or r == n - 2):
+            d[r] = 0.75 * (F(j + 1) - F(j - 1))
+        elif ntype == 4 and r == n - 1:
+            d[r] = 2.5 * F(j) - 2.0 * F(j - 1) - 0.5 * F(j - 2)
+        elif ntype != 4 and (r == 0 or r == n - 1):
+            d[r] = 0.75 * (F(j + 1) - F(j - 1)) - 0.15 * (F(j + 2) - F(j - 2)) + \
+                NUM1D60 * (F(j + 3) - F(j - 3))
+        else:
+            d[r] = NUM7D9 * (F(j + 1) - F(j - 1)) + NUM1D36 * (F(j + 2) - F(j - 2))
+    for i in range(1, n):
+        d[i] = d[i] * ac2[i] - d[i - 1] * ac3[i]
+    x = np.empty_like(d)
+    x[n - 1] = d[n - 1]
+    for i in range(n - 2, -1, -1):
+        x[i] = d[i] - ac1[i] * x[i + 1]
+    out = x[-i0: -i0 + dim + 1]
+    return np.moveaxis(out, 0, axis)
+
+
+# ---------------------------------------------------------------------------
+# grids
+# ---------------------------------------------------------------------------
+def gridcube(ia, ja, ka, lx, ly, lz):
+    """gridcube (src/gridgeneration.F90:233-267), single rank: 1-D node
+    coordinates x(0:ia), y(0:ja), z(0:ka)."""
+    x = np.array([lx / float(ia) * float(i) for i in range(ia + 1)])
+    y = np.array([ly] if ja == 0 else [ly / float(ja) * float(j) for j in range(ja + 1)])
+    z = np.array([0.0] if ka == 0 else [lz / float(ka) * float(k) for k in range(ka + 1)])
+    return x, y, z
+
+
+def _extend(c: np.ndarray, dim: int, flat: bool) -> np.ndarray:
+    """gridsendrecv single-rank halo extension (src/parallel.F90:2861-2866,
+    2930-2960, 3010-3030): nodes -5..dim+5."""
+    h = np.zeros(dim + 2 * HM + 1)
+    if flat:
+        for n in range(-HM, HM + 1):
+            h[n + HM] = c[0] + float(n)
+        return h
+    h[HM:HM + dim + 1] = c
+    for n in range(1, HM + 1):
+        h[dim + n + HM] = c[dim] + (c[n] - c[0])
+        h[-n + HM] = c[0] - (c[dim] - c[dim - n])
+    return h
+
+
+def _wrap_halo(a: np.ndarray, dims, per) -> np.ndarray:
+    """dataswap of an interior-valued array onto halo layout: periodic axes
+    copy im-5..im-1 / 1..5 into the halos; other halos are zero."""
+    out = a
+    for ax in range(3):
+        n = out.shape[ax]
+        if n == 1:
+            continue
+        dim = dims[ax]
+        if per[ax]:
+            idx = np.concatenate([np.arange(dim - HM, dim), np.arange(0, dim + 1), np.arange(1, HM + 1)])
+            out = np.take(out, idx, axis=ax)
+        else:
+            pad = [(0, 0)] * out.ndim
+            pad[ax] = (HM, HM)
+            out = np.pad(out, pad)
+    return out
+
+
+def rect_metrics(x, y, z, npdc=(3, 3, 3), diag_only=False):
+    """gridgeom (src/geom.F90:99-930) for a rectilinear grid.
+
+    Returns (dxi, jacob) in the halo layout: dxi shape (im+11, jm+11, km+11,
+    3, 3) in Fortran order (or a tuple of the three diagonal components when
+    diag_only and every off-diagonal is zero), jacob (im+11, jm+11, km+11).
+    """
+    im, jm, km = len(x) - 1, len(y) - 1, len(z) - 1
+    ndims = 3 if km > 0 else 2
+    per = [p == 3 for p in npdc]
+    dims = (im, jm, km)
+    # coordinates with halos, broadcast along the axes they do not vary on
+    X = [
+        _extend(x, im, False).reshape(-1, 1, 1),
+        _extend(y, jm, jm == 0).reshape(1, -1, 1),
+        _extend(z, km, km == 0).reshape(1, 1, -1),
+    ]
+    full = (im + 2 * HM + 1, jm + 2 * HM + 1, km + 2 * HM + 1)
+
+    def D(f, axis):
+        """fds%central along `axis` for every transverse line: f holds nodes
+        -5..dim+5 along `axis` (or is constant there: singleton axis) and
+        interior nodes (or a singleton) on the other axes."""
+        f = np.asarray(f, dtype=np.float64)
+        if f.shape[axis] == 1:
+            if npdc[axis] == 3:
+                # every row of a periodic system differences equal values
+                return np.zeros(f.shape)
+            f = np.broadcast_to(f, tuple(full[axis] if a == axis else f.shape[a] for a in range(3)))
+        return compact_deriv(f, axis, npdc[axis], dims[axis])
+
+    def transverse_interior(a, axis):
+        sl = [slice(HM, HM + dims[b] + 1) if (b != axis and a.shape[b] > 1) else slice(None)
+              for b in range(3)]
+        return a[tuple(sl)]
+
+    # dx(m,d): derivative of coordinate m along d on interior lines, then dataswap
+    dxm = [[None] * 3 for _ in range(3)]
+    for d in range(3):
+        for m in range(3):
+            dxm[m][d] = D(transverse_interior(X[m], d), d)
+    dxh = [[_wrap_halo(dxm[m][d], dims, per) for d in range(3)] for m in range(3)]
+
+    def A(m, d):  # dx(m,d) on interior nodes, 1-based indices
+        return dxm[m - 1][d - 1]
+
+    if ndims == 3:
+        J = (A(1, 1) * A(2, 2) * A(3, 3) + A(1, 2) * A(2, 3) * A(3, 1) +
+             A(1, 3) * A(2, 1) * A(3, 2) - A(1, 3) * A(2, 2) * A(3, 1) -
+             A(1, 2) * A(2, 1) * A(3, 3) - A(1, 1) * A(2, 3) * A(3, 2))
+    else:
+        J = A(1, 1) * A(2, 2) - A(1, 2) * A(2, 1)
+    J = np.broadcast_to(J, (im + 1, jm + 1, km + 1))
+
+    dxi = [[0.0] * 3 for _ in range(3)]  # dxi[d][m], 0-based
+    if ndims == 3:
+        def Xh(m):
+            return X[m - 1]
+
+        def DXh(m, d):
+            return dxh[m - 1][d - 1]
+
+        terms = {
+            0: [(2, 1, 2, 3, 3, 3, 3, 2), (2, 2, 3, 3, 1, 1, 3, 3), (2, 3, 1, 3, 2, 2, 3, 1),
+                (3, 1, 3, 2, 2, 2, 2, 3), (3, 2, 1, 2, 3, 3, 2, 1), (3, 3, 2, 2, 1, 1, 2, 2)],
+            1: [(1, 1, 3, 3, 2, 2, 3, 3), (1, 2, 1, 3, 3, 3, 3, 1), (1, 3, 2, 3, 1, 1, 3, 2),
+                (3, 1, 2, 1, 3, 3, 1, 2), (3, 2, 3, 1, 1, 1, 1, 3), (3, 3, 1, 1, 2, 2, 1, 1)],
+            2: [(1, 1, 2, 2, 3, 3, 2, 2), (1, 2, 3, 2, 1, 1, 2, 3), (1, 3, 1, 2, 2, 2, 2, 1),
+                (2, 1, 3, 1, 2, 2, 1, 3), (2, 2, 1, 1, 3, 3, 1, 1), (2, 3, 2, 1, 1, 1, 1, 2)],
+        }
+        for s in range(3):
+            for (dd, mm, am, ad, bm, cm, cd, dm) in terms[s]:
+                # phi over nodes -hm..dim+hm of lines at interior transverse nodes
+                phi = 0.5 * (DXh(am, ad) * Xh(bm) - DXh(cm, cd) * Xh(dm))
+                dxi[dd - 1][mm - 1] = dxi[dd - 1][mm - 1] + D(transverse_interior(phi, s), s)
+    else:
+        dxi[0][0] = A(2, 2)
+        dxi[0][1] = -A(1, 2)
+        dxi[1][0] = -A(2, 1)
+        dxi[1][1] = A(1, 1)
+    out = [[None] * 3 for _ in range(3)]
+    for d in range(3):
+        for m in range(3):
+            v = np.asarray(dxi[d][m], dtype=np.float64)
+            if not np.any(v):
+                out[d][m] = np.zeros((1, 1, 1))  # 0/J is exactly 0
+            else:
+                out[d][m] = np.broadcast_to(v, (im + 1, jm + 1, km + 1)) / J
+    def to_halo(a):
+        return np.asfortranarray(np.broadcast_to(_wrap_halo(np.ascontiguousarray(a), dims, per), full))
+
+    Jh = to_halo(J)
+    offdiag_zero = all(not np.any(out[d][m]) for d in range(3) for m in range(3) if d != m)
+    if diag_only and offdiag_zero:
+        diag = tuple(to_halo(out[d][d]) for d in range(3))
+        return diag, Jh
+    dxi_h = np.zeros(full + (3, 3), order="F")
+    for d in range(3):
+        for m in range(3):
+            dxi_h[..., d, m] = _wrap_halo(np.ascontiguousarray(out[d][m]), dims, per)
+    return dxi_h, Jh
+
+
+# ---------------------------------------------------------------------------
+# initial states
+# ---------------------------------------------------------------------------
+def refcal(mach, reynolds, prandtl=0.72, gamma=1.4):
+    """Nondimensional constants of refcal (src/solver.F90:102-128)."""
+    c = {}
+    c["const1"] = 1.0 / (gamma * (gamma - 1.0) * (mach * mach))
+    c["const2"] = gamma * (mach * mach)
+    c["const6"] = 1.0 / (gamma - 1.0)
+    c["pinf"] = 1.0 * 1.0 / c["const2"]
+    return c
+
+
+def tgv_state(im, jm, km, mach=0.1, x=None, y=None, z=None):
+    """tgvini + updateq (src/initialisation.F90:621-691, src/fludyna.F90:
+    254-300): halo-layout q, rho, vel, prs, tmp with interior nodes set."""
+    c = refcal(mach, 1600.0)
+    if x is None:
+        L = 2.0 * PI
+        x, y, z = gridcube(im, jm, km, L, L, L)
+    X = x.reshape(-1, 1, 1)
+    Y = y.reshape(1, -1, 1)
+    Z = z.reshape(1, 1, -1)
+    rho = np.ones((im + 1, jm + 1, km + 1))
+    u = 1.0 * np.sin(X) * np.cos(Y) * np.cos(Z) * np.ones_like(rho)
+    v = -(1.0 * np.cos(X) * np.sin(Y) * np.cos(Z)) * np.ones_like(rho)
+    w = np.zeros_like(rho)
+    p = c["pinf"] + rho / 16.0 * (1.0 * 1.0) * (np.cos(2.0 * X) + np.cos(2.0 * Y)) * (np.cos(2.0 * Z) + 2.0)
+    T = p / rho * c["const2"]
+    q5 = rho * (T * c["const1"] + 0.5 * (u * u + v * v + w * w))
+    return _pack_state(im, jm, km, rho, u, v, w, p, T, q5)
+
+
+def _pack_state(im, jm, km, rho, u, v, w, p, T, q5):
+    full = (im + 2 * HM + 1, jm + 2 * HM + 1, km + 2 * HM + 1)
+    sl = (slice(HM, HM + im + 1), slice(HM, HM + jm + 1), slice(HM, HM + km + 1))
+    q = np.zeros(full + (5,), order="F")
+    vel = np.zeros(full + (3,), order="F")
+    out = {"q": q, "vel": vel}
+    for name in ("rho", "prs", "tmp"):
+        out[name] = np.zeros(full, order="F")
+    out["rho"][sl] = rho
+    out["prs"][sl] = p
+    out["tmp"][sl] = T
+    vel[sl + (0,)] = u
+    vel[sl + (1,)] = v
+    vel[sl + (2,)] = w
+    q[sl + (0,)] = rho
+    q[sl + (1,)] = rho * u
+    q[sl + (2,)] = rho * v
+    q[sl + (3,)] = rho * w
+    q[sl + (4,)] = q5
+    return out

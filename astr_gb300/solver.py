@@ -1,0 +1,185 @@
+"""Host-side mirror of the ASTR module interface for the RHS hot path.
+
+ASTR's time loop calls argument-less module routines on module arrays
+(``filterq``, ``qswap``, ``gradcal``, ``rhscal``, ``updatefvar``; the stage
+loop ``time_integration_rk``, src/mainloop.F90:301-601).  ``GpuSolver`` keeps
+the same routine names, with the module state resident in HBM behind the C
+ABI of ``include/astr_gpu.h``.  Host arrays use the reference's Fortran
+layout: halo arrays ``(im+11, jm+11, km+11[, n])`` in Fortran order.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import capi
+
+HM = 5
+
+
+def halo_shape(im, jm, km, n=None):
+    s = (im + 2 * HM + 1, jm + 2 * HM + 1, km + 2 * HM + 1)
+    return s + (n,) if n else s
+
+
+def interior_shape(im, jm, km, n=None):
+    s = (im + 1, jm + 1, km + 1)
+    return s + (n,) if n else s
+
+
+def _f(a, shape):
+    a = np.asarray(a, dtype=np.float64)
+    if a.shape != shape and a.size == int(np.prod(shape)) and a.shape[:3] == shape[:3]:
+        # trailing component axes given flattened, e.g. dxi(...,9) for dxi(...,3,3)
+        a = np.asfortranarray(a).reshape(shape, order="F")
+    if a.shape != shape:
+        raise ValueError(f"array shape {a.shape}, expected {shape}")
+    return np.asfortranarray(a)
+
+
+class GpuSolver:
+    """One single-rank block of the ASTR solver resident on one GPU."""
+
+    def __init__(self, im, jm, km, *, order=capi.ORDER_MAIN, precision=capi.FP64,
+                 npdc=(3, 3, 3), lfilter=True, diffterm=True, alfa_filter=0.49,
+                 beter_halo=1.11, beter_bound=0.98, mach=0.1, reynolds=1600.0, prandtl=0.72,
+                 ref_tem=273.15, suth_const=None, deltat=1e-3, ia=None, ja=None, ka=None):
+        L = capi.load()
+        if suth_const is None:
+            suth_const = 110.4 if order == capi.ORDER_MINIAPP else 110.3
+        self.im, self.jm, self.km = im, jm, km
+        self.dims = capi.AstrDims(im, jm, km, im if ia is None else ia, jm if ja is None else ja,
+                                  km if ka is None else ka, *npdc)
+        self.params = capi.AstrParams(order, precision, int(lfilter), int(diffterm), alfa_filter,
+                                      beter_halo, beter_bound, mach, reynolds, prandtl, ref_tem,
+                                      suth_const, deltat)
+        h = ctypes.c_void_p()
+        rc = L.astr_gpu_create(ctypes.byref(self.dims), ctypes.byref(self.params), ctypes.byref(h))
+        if rc != capi.ASTR_OK:
+            raise capi.AstrError(rc, capi.last_error(None))
+        self.h = h
+        self.L = L
+
+    # -- lifecycle --------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.astr_gpu_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _c(self, rc):
+        return capi.check(self.h, rc)
+
+    # -- data movement ----------------------------------------------------
+    def set_metrics(self, dxi, jacob):
+        im, jm, km = self.im, self.jm, self.km
+        dxi = _f(dxi, halo_shape(im, jm, km) + (3, 3))
+        jacob = _f(jacob, halo_shape(im, jm, km))
+        self._c(self.L.astr_gpu_set_metrics(self.h, capi.dptr(dxi), capi.dptr(jacob)))
+
+    def set_metrics_diag(self, dxi11, dxi22, dxi33, jacob):
+        shp = halo_shape(self.im, self.jm, self.km)
+        arrs = [_f(a, shp) for a in (dxi11, dxi22, dxi33, jacob)]
+        self._c(self.L.astr_gpu_set_metrics_diag(self.h, *(capi.dptr(a) for a in arrs)))
+
+    def upload_state(self, q, rho, vel, prs, tmp):
+        im, jm, km = self.im, self.jm, self.km
+        q = _f(q, halo_shape(im, jm, km, 5))
+        rho = _f(rho, halo_shape(im, jm, km))
+        vel = _f(vel, halo_shape(im, jm, km, 3))
+        prs = _f(prs, halo_shape(im, jm, km))
+        tmp = _f(tmp, halo_shape(im, jm, km))
+        self._c(self.L.astr_gpu_upload_state(self.h, capi.dptr(q), capi.dptr(rho), capi.dptr(vel),
+                                             capi.dptr(prs), capi.dptr(tmp)))
+
+    def download_state(self):
+        im, jm, km = self.im, self.jm, self.km
+        out = {
+            "q": np.zeros(halo_shape(im, jm, km, 5), order="F"),
+            "rho": np.zeros(halo_shape(im, jm, km), order="F"),
+            "vel": np.zeros(halo_shape(im, jm, km, 3), order="F"),
+            "prs": np.zeros(halo_shape(im, jm, km), order="F"),
+            "tmp": np.zeros(halo_shape(im, jm, km), order="F"),
+        }
+        self._c(self.L.astr_gpu_download_state(self.h, *(capi.dptr(out[k]) for k in
+                                                          ("q", "rho", "vel", "prs", "tmp"))))
+        return out
+
+    def download_rhs(self):
+        im, jm, km = self.im, self.jm, self.km
+        out = {
+            "qrhs": np.zeros(interior_shape(im, jm, km, 5), order="F"),
+            "dvel": np.zeros(interior_shape(im, jm, km) + (3, 3), order="F"),
+            "dtmp": np.zeros(interior_shape(im, jm, km, 3), order="F"),
+        }
+        self._c(self.L.astr_gpu_download_rhs(self.h, capi.dptr(out["qrhs"]), capi.dptr(out["dvel"]),
+                                             capi.dptr(out["dtmp"])))
+        return out
+
+    # -- reference routines -------------------------------------------------
+    def time_integration_rk(self, nsteps: int = 1, stats: bool = True):
+        """nsteps RK3 steps; returns the (nsteps, 2) kinetic-energy /
+        enstrophy history sampled at stage 1 of each step."""
+        hist = np.zeros(2 * max(nsteps, 1))
+        st = capi.AstrStatus()
+        self._c(self.L.astr_gpu_rk3_step(self.h, int(nsteps), capi.dptr(hist) if stats else None,
+                                         ctypes.byref(st)))
+        return hist[: 2 * nsteps].reshape(nsteps, 2)
+
+    def filterq(self):
+        self._c(self.L.astr_gpu_filterq(self.h))
+
+    def qswap(self):
+        self._c(self.L.astr_gpu_qswap(self.h))
+
+    def gradcal(self):
+        self._c(self.L.astr_gpu_gradcal(self.h))
+
+    def rhscal(self):
+        self._c(self.L.astr_gpu_rhscal(self.h))
+
+    def updatefvar(self):
+        self._c(self.L.astr_gpu_updatefvar(self.h))
+
+    def reduce_stats(self):
+        ke, en = ctypes.c_double(), ctypes.c_double()
+        self._c(self.L.astr_gpu_reduce_stats(self.h, ctypes.byref(ke), ctypes.byref(en)))
+        return ke.value, en.value
+
+    def timed_steps(self, nsteps: int) -> float:
+        """Device milliseconds of nsteps RK3 steps (CUDA events on the
+        context's stream, no statistics)."""
+        ms = ctypes.c_double()
+        self._c(self.L.astr_gpu_timed_steps(self.h, int(nsteps), ctypes.byref(ms)))
+        return ms.value
+
+    def set_profiling(self, on: bool):
+        self._c(self.L.astr_gpu_set_profiling(self.h, int(on)))
+
+    def kernel_times(self):
+        n = len(capi.KERNEL_CLASSES)
+        ms = np.zeros(n)
+        cnt = (ctypes.c_longlong * n)()
+        rc = self.L.astr_gpu_kernel_times(self.h, capi.dptr(ms), cnt, n)
+        if rc < 0:
+            capi.check(self.h, rc)
+        return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(capi.KERNEL_CLASSES)}
+
+    def synchronize(self):
+        self._c(self.L.astr_gpu_synchronize(self.h))
+
+    @property
+    def launches(self) -> int:
+        return int(self.L.astr_gpu_launch_count(self.h))

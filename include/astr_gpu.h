@@ -1,0 +1,159 @@
+/*
+ * astr_gpu.h — C ABI of the GB300 (sm_103a) right-hand-side hot path for
+ * the ASTR compressible Navier-Stokes solver.
+ *
+ * The Fortran main loop of ASTR calls argument-less module routines that
+ * act on module arrays (src/mainloop.F90:396-486).  This library replaces
+ * their bodies.  A context holds every field resident in HBM on one GPU,
+ * for one single-rank block; host arrays cross the boundary only on upload
+ * and download, in the reference's own Fortran layout:
+ *   halo arrays      var(-hm:im+hm,-hm:jm+hm,-hm:km+hm[,n]), hm = 5
+ *   interior arrays  var(0:im,0:jm,0:km[,n])
+ * (src/commarray.F90:14-27, 56-108).  All entry points are extern "C",
+ * take plain pointers and sizes, never throw, and return ASTR_OK (0) or a
+ * negative status; astr_gpu_last_error() gives the message.
+ *
+ * Threading: one context per host thread at a time; each context owns its
+ * own CUDA stream.
+ */
+#ifndef ASTR_GPU_H
+#define ASTR_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define ASTR_OK 0
+#define ASTR_ERR_ARG -1        /* bad dimensions or parameters            */
+#define ASTR_ERR_OOM -2        /* device allocation failed                */
+#define ASTR_ERR_CUDA -3       /* CUDA runtime error                      */
+#define ASTR_ERR_UNSUPPORTED -4 /* configuration outside what is built   */
+#define ASTR_ERR_NONFINITE -5  /* crash check: non-finite or rho <= 0     */
+#define ASTR_ERR_STATE -6      /* call out of order (e.g. no metrics)     */
+
+/* Stage ordering. */
+#define ASTR_ORDER_MAIN 0     /* src/mainloop.F90:396-486                 */
+#define ASTR_ORDER_MINIAPP 1  /* miniapps/tgv_solver_3d/tgvsolver.F90:994-1082 */
+
+/* Precision forms. */
+#define ASTR_FP64 0           /* plain FP64: the drop-in                  */
+#define ASTR_FP32_STORAGE 1   /* FP32 streams, FP64 RK accumulation       */
+
+/* Block dimensions and boundary types (src/commvar.F90:17-18;
+ * npdc* as set by src/parallel.F90:1042-1228: 3 = periodic/inner block,
+ * 4 = physical boundary at both ends). */
+typedef struct {
+  int im, jm, km;          /* intervals; km == 0 for a 2-D case            */
+  int ia, ja, ka;          /* global intervals (statistics normalisation)  */
+  int npdci, npdcj, npdck;
+} astr_dims;
+
+/* Scheme and flow constants (src/commvar.F90; refcal src/solver.F90:28-173). */
+typedef struct {
+  int order;               /* ASTR_ORDER_*                                  */
+  int precision;           /* ASTR_FP64 or ASTR_FP32_STORAGE                */
+  int lfilter;             /* compact filter at each stage                 */
+  int diffterm;            /* viscous terms                                 */
+  double alfa_filter;      /* filter alpha (0.49)                           */
+  double beter_halo;       /* filter end-row alpha at block interfaces (1.11) */
+  double beter_bound;      /* filter boundary-row parameter (0.98; mini-app 1.09) */
+  double mach, reynolds, prandtl;
+  double ref_tem;          /* reference temperature (Sutherland)           */
+  double suth_const;       /* Sutherland constant (110.3 main, 110.4 mini-app) */
+  double deltat;
+} astr_params;
+
+typedef struct {
+  double kenergy;          /* kenergycal, src/statistic.F90:938-992         */
+  double enstrophy;        /* enstophycal, src/statistic.F90:871-936        */
+  int crash;               /* 1 when a non-finite value or rho <= 0 was seen */
+} astr_status;
+
+typedef struct astr_ctx astr_ctx;
+
+/* Create a context and allocate every field in HBM.  Replaces the set-up of
+ * solvrinit (src/comsolver.F90:47-146) and allocommarray
+ * (src/commarray.F90:56-108).  Returns ASTR_OK and *out on success. */
+int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx** out);
+void astr_gpu_destroy(astr_ctx* ctx);
+
+/* Copy the grid metrics: dxi(-hm:..,1:3,1:3) and jacob(-hm:..) in Fortran
+ * layout, as produced by gridgeom (src/geom.F90:99-930).  Host pointers. */
+int astr_gpu_set_metrics(astr_ctx* ctx, const double* dxi, const double* jacob);
+
+/* Upload the conserved variables q(-hm:..,1:5) (halo layout) and the
+ * primitive arrays rho, vel(..,1:3), prs, tmp (halo layout).  The
+ * primitives are part of the solver state: interior primitives are the
+ * ones updatefvar left at the end of the previous stage. */
+int astr_gpu_upload_state(astr_ctx* ctx, const double* q, const double* rho,
+                          const double* vel, const double* prs, const double* tmp);
+/* Download the same arrays (any pointer may be NULL to skip it). */
+int astr_gpu_download_state(astr_ctx* ctx, double* q, double* rho, double* vel,
+                            double* prs, double* tmp);
+/* Download qrhs(0:im,..,1:5), dvel(0:im,..,1:3,1:3), dtmp(0:im,..,1:3). */
+int astr_gpu_download_rhs(astr_ctx* ctx, double* qrhs, double* dvel, double* dtmp);
+
+/* nsteps full RK3 steps (time_integration_rk, src/mainloop.F90:301-601).
+ * If hist != NULL it receives {kenergy, enstrophy} per step, sampled at
+ * stage 1 (where rkfirst/statcal sample them).  status may be NULL. */
+int astr_gpu_rk3_step(astr_ctx* ctx, int nsteps, double* hist, astr_status* status);
+
+/* Finer drop-in entry points, one per reference routine. */
+int astr_gpu_filterq(astr_ctx* ctx);     /* src/comsolver.F90:514-632   */
+int astr_gpu_qswap(astr_ctx* ctx);       /* src/parallel.F90:4848-5318  */
+int astr_gpu_gradcal(astr_ctx* ctx);     /* src/comsolver.F90:244-497   */
+int astr_gpu_rhscal(astr_ctx* ctx);      /* src/solver.F90:185-282      */
+int astr_gpu_updatefvar(astr_ctx* ctx);  /* src/fludyna.F90:191-242     */
+
+/* Device-side statistics of the current state (uses the last gradients). */
+int astr_gpu_reduce_stats(astr_ctx* ctx, double* kenergy, double* enstrophy);
+
+/* Wait for all work of the context; returns the first asynchronous error. */
+int astr_gpu_synchronize(astr_ctx* ctx);
+
+/* Message of the last failed call on this context (or of the last failed
+ * astr_gpu_create when ctx is NULL). Returns its length. */
+int astr_gpu_last_error(astr_ctx* ctx, char* buf, int len);
+
+/* Bytes of HBM held by a context with these dimensions and parameters. */
+size_t astr_gpu_footprint(const astr_dims* dims, const astr_params* params);
+
+/* Number of kernel launches issued by this context since creation. */
+long long astr_gpu_launch_count(astr_ctx* ctx);
+
+/* Diagonal-metric upload: dxi(:,:,:,1,1), dxi(:,:,:,2,2), dxi(:,:,:,3,3)
+ * and jacob, each one halo-layout array.  Equivalent to
+ * astr_gpu_set_metrics with every off-diagonal dxi equal to zero, without
+ * the host holding the six zero arrays (no counterpart in the reference,
+ * whose gridgeom always stores all nine). */
+int astr_gpu_set_metrics_diag(astr_ctx* ctx, const double* dxi11, const double* dxi22,
+                              const double* dxi33, const double* jacob);
+
+/* Page-locked host memory for uploads and downloads (cudaMallocHost);
+ * a Fortran host can c_f_pointer onto it.  NULL on failure. */
+void* astr_gpu_host_alloc(size_t bytes);
+void astr_gpu_host_free(void* p);
+
+/* nsteps RK3 steps without statistics, bracketed by CUDA events on the
+ * context's stream; *elapsed_ms receives the device time. */
+int astr_gpu_timed_steps(astr_ctx* ctx, int nsteps, double* elapsed_ms);
+
+/* Per-kernel-class device times.  With profiling on, every launch is
+ * bracketed by CUDA events; astr_gpu_kernel_times synchronises and returns,
+ * per class, the summed milliseconds and the launch counts.  Classes:
+ * 0 filter, 1 halo (qswap/bchomo), 2 convective+gradient, 3 viscous(+RK),
+ * 4 pointwise, 5 statistics.  Returns the number of classes. */
+int astr_gpu_set_profiling(astr_ctx* ctx, int on);
+int astr_gpu_kernel_times(astr_ctx* ctx, double* ms, long long* launches, int nclass);
+
+/* Measurement helper: FP64 FMA throughput of this device in TFLOP/s (each
+ * FMA counts two flops), from a register-resident FMA loop. */
+int astr_gpu_measure_fp64_peak(double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,167 @@
+"""GPU parity: the sm_103a path through the C ABI against the oracle.
+
+Bar: max-norm relative difference <= 1e-12 per state field (FP64 form), the
+spec tolerance for the plain FP64 form.  The line solves run as
+chunked Thomas recurrences joined by an exact carry scan, so results agree
+with the sequential reference recurrences to rounding, not bit for bit.
+
+Derivative arrays (dvel, dtmp, qrhs) are measured against the scale of the
+operation that produced them, max|f| * max|d(xi)/dx| for a gradient of f and
+max over components for the residual: the temperature of a Mach-0.1 vortex
+is uniform to 1e-3, so the rounding of T ~ 1 (which the reference carries
+too) is large next to max|grad T| itself.
+"""
+import numpy as np
+import pytest
+
+from conftest import relerr
+from oracle import pyoracle as po
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+
+
+def gpu_from_oracle(o, **kw):
+    from astr_gb300 import capi
+    from astr_gb300.solver import GpuSolver
+    c = o.cfg
+    g = GpuSolver(o.im, o.jm, o.km, order=o.mode, npdc=(c.npdci, c.npdcj, c.npdck),
+                  lfilter=bool(c.lfilter), diffterm=bool(c.diffterm), alfa_filter=c.alfa_filter,
+                  beter_halo=c.beter_halo, beter_bound=c.beter_bound, mach=c.mach,
+                  reynolds=c.reynolds, prandtl=c.prandtl, ref_tem=c.ref_tem,
+                  suth_const=c.suth_const, deltat=c.deltat, ia=c.ia, ja=c.ja, ka=c.ka, **kw)
+    if o.mode == capi.ORDER_MAIN:
+        g.set_metrics(o.field("dxi"), o.field("jacob"))
+    g.upload_state(o.field("q"), o.field("rho"), o.field("vel"), o.field("prs"), o.field("tmp"))
+    return g
+
+
+def interior(a, o):
+    h = po.HM
+    return a[h:h + o.im + 1, h:h + o.jm + 1, h:h + o.km + 1, ...]
+
+
+def compare_state(o, st, full=True, tol=TOL):
+    errs = {}
+    for name in ("q", "rho", "vel", "prs", "tmp"):
+        ref = o.field(name)
+        got = st[name]
+        if full:
+            errs[name] = relerr(got, ref)
+        else:
+            errs[name] = relerr(interior(got, o), interior(ref, o))
+    print("state parity:", " ".join(f"{k} {v:.2e}" for k, v in errs.items()))
+    bad = {k: v for k, v in errs.items() if not v <= tol}
+    assert not bad, f"parity violated: {errs}"
+    return errs
+
+
+@pytest.mark.parametrize("n", [32, 24])
+def test_tgv_main_steps(gpu_lib, n):
+    o = po.tgv_main(n)
+    g = gpu_from_oracle(o)
+    hist_g = g.time_integration_rk(4)
+    hist_o = o.rk3_steps(4)
+    compare_state(o, g.download_state(), full=True)
+    assert relerr(hist_g, hist_o) <= TOL
+
+
+def test_tgv_main_anisotropic(gpu_lib):
+    o = po.Oracle(24, 20, 28, mode=po.MODE_MAIN)
+    L = 2 * np.pi
+    o.gridcube(L, L, L)
+    o.call("gridgeom")
+    o.call("init_tgv")
+    g = gpu_from_oracle(o)
+    g.time_integration_rk(3)
+    o.rk3_steps(3)
+    compare_state(o, g.download_state(), full=True)
+
+
+def test_tgv_miniapp_steps(gpu_lib):
+    o = po.tgv_miniapp(32)
+    g = gpu_from_oracle(o)
+    hist_g = g.time_integration_rk(4)
+    hist_o = o.rk3_steps(4)
+    compare_state(o, g.download_state(), full=False)
+    assert relerr(hist_g, hist_o) <= TOL
+
+
+def test_tgv128_golden_history_on_gpu(gpu_lib):
+    """The mini-app ordering on the GPU reproduces the reference's own
+    100-step history miniapps/tgv_solver_3d/state.ref_128."""
+    import os
+    ref = np.loadtxt(os.path.join(os.path.dirname(__file__), "golden", "tgv128_state_ref.txt"))
+    o = po.tgv_miniapp(128)  # initial state only
+    g = gpu_from_oracle(o)
+    hist = g.time_integration_rk(100)
+    assert relerr(hist[:, 0], ref[:, 2]) <= TOL
+    assert relerr(hist[:, 1], ref[:, 3]) <= TOL
+
+
+# -- one reference routine at a time -------------------------------------
+@pytest.fixture
+def evolved_pair(gpu_lib):
+    o = po.tgv_main(24)
+    o.rk3_steps(2)
+    g = gpu_from_oracle(o)
+    return o, g
+
+
+def test_filterq(evolved_pair):
+    o, g = evolved_pair
+    o.call("filterq")
+    g.filterq()
+    st = g.download_state()
+    assert relerr(interior(st["q"], o), interior(o.field("q"), o)) <= TOL
+
+
+def test_qswap(evolved_pair):
+    o, g = evolved_pair
+    o.call("filterq")
+    g.filterq()
+    o.call("qswap")
+    g.qswap()
+    compare_state(o, g.download_state(), full=True)
+
+
+def test_gradcal_rhscal(evolved_pair):
+    o, g = evolved_pair
+    for x in (o,):
+        x.call("filterq")
+        x.call("qswap")
+        x.call("gradcal")
+    g.filterq()
+    g.qswap()
+    g.gradcal()
+    r = g.download_rhs()
+    dxi_max = float(np.max(np.abs(o.field("dxi"))))
+    vel = interior(o.field("vel"), o)
+    tmp = interior(o.field("tmp"), o)
+    dvel_ref = o.field("dvel")
+    dvel = r["dvel"].reshape(dvel_ref.shape, order="F")
+    e_dvel = np.max(np.abs(dvel - dvel_ref)) / (np.max(np.abs(vel)) * dxi_max)
+    e_dtmp = np.max(np.abs(r["dtmp"] - o.field("dtmp"))) / (np.max(np.abs(tmp)) * dxi_max)
+    print(f"gradcal: dvel {e_dvel:.2e} (per-field {relerr(dvel, dvel_ref):.2e}), "
+          f"dtmp {e_dtmp:.2e} (per-field {relerr(r['dtmp'], o.field('dtmp')):.2e})")
+    assert e_dvel <= TOL and e_dtmp <= TOL
+    o.field("qrhs")[...] = 0.0
+    o.call("rhscal")
+    g.rhscal()
+    r = g.download_rhs()
+    e_q = relerr(r["qrhs"], o.field("qrhs"))
+    print(f"rhscal: qrhs {e_q:.2e}; per component "
+          + " ".join(f"{relerr(r['qrhs'][..., n], o.field('qrhs')[..., n]):.1e}" for n in range(5)))
+    assert e_q <= TOL
+
+
+def test_updatefvar(evolved_pair):
+    o, g = evolved_pair
+    o.call("filterq")
+    g.filterq()
+    o.call("updatefvar")
+    g.updatefvar()
+    st = g.download_state()
+    for name in ("rho", "vel", "prs", "tmp"):
+        assert relerr(interior(st[name], o), interior(o.field(name), o)) <= TOL
