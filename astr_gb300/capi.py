@@ -37,7 +37,9 @@ EXPORTS = [
     "astr_gpu_footprint", "astr_gpu_launch_count", "astr_gpu_set_metrics_diag",
     "astr_gpu_host_alloc", "astr_gpu_host_free", "astr_gpu_timed_steps",
     "astr_gpu_set_profiling", "astr_gpu_kernel_times", "astr_gpu_measure_fp64_peak",
+    "astr_gpu_stats_noalloc",
 ]
+NOALLOC_STATS_MAX_BLOCKS = 65536
 KERNEL_CLASSES = ["filter", "halo", "convgrad", "visc", "pointwise", "stats"]
 
 
@@ -115,6 +117,9 @@ def load(path: str = LIB_PATH):
     L.astr_gpu_kernel_times.restype = ip
     L.astr_gpu_measure_fp64_peak.argtypes = [dp]
     L.astr_gpu_measure_fp64_peak.restype = ip
+    L.astr_gpu_stats_noalloc.argtypes = [vp, vp, vp, ctypes.POINTER(AstrDims), ctypes.c_double,
+                                         vp, dp, dp]
+    L.astr_gpu_stats_noalloc.restype = ip
     for n in ("astr_gpu_set_metrics", "astr_gpu_upload_state", "astr_gpu_download_state",
               "astr_gpu_download_rhs", "astr_gpu_rk3_step", "astr_gpu_reduce_stats"):
         getattr(L, n).restype = ip

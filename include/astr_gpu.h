@@ -153,6 +153,28 @@ int astr_gpu_kernel_times(astr_ctx* ctx, double* ms, long long* launches, int nc
  * FMA counts two flops), from a register-resident FMA loop. */
 int astr_gpu_measure_fp64_peak(double* tflops);
 
+/* Kinetic energy and enstrophy without allocating anything (no counterpart
+ * in the reference: it exists for callers that cannot call cudaMalloc, such
+ * as a host whose HBM is all handed to its own pool, or a time loop that must
+ * not synchronise the device through an allocation between steps).
+ * Computes what astr_gpu_reduce_stats computes, from device arrays the
+ * caller owns: rho and vel(:,:,:,1:3) in the halo layout, dvel(:,:,:,1:3,1:3)
+ * in the interior layout, for the block `dims` (l0: enstrophy length scale,
+ * 0 means 1).  Runs on `stream` (a cudaStream_t, NULL for the default
+ * stream) and waits for it before returning.
+ * Scratch: a fixed device array of 2*ASTR_NOALLOC_STATS_MAX_BLOCKS doubles
+ * (1 MiB, held by every GPU that loads the library until exit), one pair of
+ * partial sums per 4096 interior nodes; blocks with more than
+ * 4096 * (ASTR_NOALLOC_STATS_MAX_BLOCKS - 1) = 268,431,360 interior nodes
+ * are rejected with ASTR_ERR_UNSUPPORTED.  All calls share that array, so
+ * calls whose work overlaps on the GPU race; serialise them.  The first call
+ * on a device looks up the array's device address; make it before any
+ * stream capture. */
+#define ASTR_NOALLOC_STATS_MAX_BLOCKS 65536
+int astr_gpu_stats_noalloc(const double* rho, const double* vel, const double* dvel,
+                           const astr_dims* dims, double l0, void* stream,
+                           double* kenergy, double* enstrophy);
+
 #ifdef __cplusplus
 }
 #endif
