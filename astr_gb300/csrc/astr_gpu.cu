@@ -14,6 +14,9 @@
 //                          primitives
 // The mini-app ordering (miniapps/tgv_solver_3d/tgvsolver.F90:994-1082) runs
 // the same kernels with its own halo fill, scalings and filter placement.
+//
+// Two precision forms share the kernels: plain FP64 (T = double), and FP32
+// storage (T = float) with the RK3 base and a master copy of q in FP64.
 #include "launch.cuh"
 #include "../../include/astr_gpu.h"
 
@@ -22,6 +25,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 using namespace astr;
@@ -47,19 +51,19 @@ __device__ __forceinline__ bool face_line(const Geo& g, int& dim, long long& bas
 
 // qswap single-rank periodic branch of one direction (src/parallel.F90:
 // 4876-4920, 5018-5065, 5159-5206).
-template <int DIR>
-__global__ void k_qswap(Geo g, Dev d, Phys ph) {
+template <typename T, int DIR>
+__global__ void k_qswap(Geo g, DevT<T> d, Phys ph) {
   int dim;
   long long base, hs;
   if (!face_line<DIR>(g, dim, base, hs)) return;
   for (int n = 0; n < 5; ++n) {
-    double* v = d.q + n * g.nh + base;
+    T* v = d.q + n * g.nh + base;
     if (dim == 0) {
       for (int l = -HMD; l <= HMD; ++l) v[hs * l] = v[0];
     } else {
       for (int h = 1; h <= HMD; ++h) v[-hs * h] = v[hs * (dim - h)];
       for (int h = 1; h <= HMD; ++h) v[hs * (dim + h)] = v[hs * h];
-      const double avg = 0.5 * (v[0] + v[hs * dim]);
+      const T avg = T(0.5) * (v[0] + v[hs * dim]);
       v[0] = avg;
       v[hs * dim] = avg;
     }
@@ -69,21 +73,22 @@ __global__ void k_qswap(Geo g, Dev d, Phys ph) {
 }
 
 // bchomo of the mini-app, one direction (tgvsolver.F90:271-369).
-template <int DIR>
-__global__ void k_bchomo(Geo g, Dev d, Phys ph) {
+template <typename T, int DIR>
+__global__ void k_bchomo(Geo g, DevT<T> d, Phys ph) {
   int dim;
   long long base, hs;
   if (!face_line<DIR>(g, dim, base, hs)) return;
   const long long nh = g.nh;
+  const T c6 = T(1) / pc<T>(ph.rconst6, ph.f_rconst6);
   auto copy = [&](long long dst, long long src) {
     for (int m = 0; m < 6; ++m) d.pr[dst + m * nh] = d.pr[src + m * nh];
-    const double ro = d.pr[dst], u = d.pr[dst + nh], v = d.pr[dst + 2 * nh], w = d.pr[dst + 3 * nh];
+    const T ro = d.pr[dst], u = d.pr[dst + nh], v = d.pr[dst + 2 * nh], w = d.pr[dst + 3 * nh];
     d.q[dst] = ro;
     d.q[dst + nh] = ro * u;
     d.q[dst + 2 * nh] = ro * v;
     d.q[dst + 3 * nh] = ro * w;
-    const double var1 = 0.5 * (u * u + v * v + w * w);
-    d.q[dst + 4 * nh] = d.pr[dst + 4 * nh] * ph.const6 + ro * var1;
+    const T var1 = T(0.5) * (u * u + v * v + w * w);
+    d.q[dst + 4 * nh] = d.pr[dst + 4 * nh] * c6 + ro * var1;
   };
   for (int h = 1; h <= HMD; ++h) copy(base - hs * h, base + hs * (dim - h));
   for (int h = 1; h <= HMD; ++h) copy(base + hs * (dim + h), base + hs * h);
@@ -101,44 +106,30 @@ __device__ __forceinline__ bool point_of(const Geo& g, long long idx, int& i, in
   return true;
 }
 
-__global__ void k_updatefvar(Geo g, Dev d, Phys ph) {
+template <typename T>
+__global__ void k_updatefvar(Geo g, DevT<T> d, Phys ph) {
   int i, j, k;
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (!point_of(g, idx, i, j, k)) return;
   q2fvar_store(g, d, ph, hidx(g, i, j, k));
 }
 
-__global__ void k_sigma(Geo g, Dev d, Phys ph) {
+template <typename T>
+__global__ void k_sigma(Geo g, DevT<T> d, Phys ph) {
   int i, j, k;
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (!point_of(g, idx, i, j, k)) return;
   sigma_point(g, d, ph, idx, hidx(g, i, j, k));
 }
 
-__global__ void k_qsave(Geo g, Dev d, Phys ph) {
+template <typename T>
+__global__ void k_rkupdate(Geo g, DevT<T> d, Phys ph, int q2f) {
   int i, j, k;
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (!point_of(g, idx, i, j, k)) return;
   const long long p = hidx(g, i, j, k);
-  for (int m = 0; m < 5; ++m)
-    d.qsave[m * g.n0 + idx] = ph.mini ? d.q[p + m * g.nh] : d.q[p + m * g.nh] * d.jac[p];
-}
-
-__global__ void k_rkupdate(Geo g, Dev d, Phys ph, int q2f) {
-  int i, j, k;
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (!point_of(g, idx, i, j, k)) return;
-  const long long p = hidx(g, i, j, k);
-  for (int m = 0; m < 5; ++m) {
-    double* qp = d.q + m * g.nh + p;
-    *qp = rk_combine(ph, d.qsave[m * g.n0 + idx], *qp, d.jac[p], d.qrhs[m * g.n0 + idx]);
-  }
+  for (int m = 0; m < 5; ++m) rk_update(g, d, ph, p, idx, m, (double)d.qrhs[m * g.n0 + idx]);
   if (q2f) q2fvar_store(g, d, ph, p);
-}
-
-__global__ void k_negate(double* a, long long n) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx < n) a[idx] = -a[idx];
 }
 
 // Fixed-order reduction of the per-warp statistics partials.
@@ -165,6 +156,38 @@ __global__ void k_stats_final(const double* part, long long nw, double* out) {
   }
 }
 
+// Precision conversions of whole arrays (upload / download of the FP32 form).
+__global__ void k_to_float(const double* a, float* b, long long n) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = __double2float_rn(a[i]);
+}
+__global__ void k_to_double(const float* a, double* b, long long n) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (double)a[i];
+}
+__global__ void k_reciprocal(const double* a, double* b, long long n) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = a[i] != 0.0 ? 1.0 / a[i] : 0.0;
+}
+// interior of a halo-layout array <-> interior-layout array
+__global__ void k_halo_to_interior(Geo g, const double* h, double* z) {
+  int i, j, k;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (!point_of(g, idx, i, j, k)) return;
+  z[idx] = h[hidx(g, i, j, k)];
+}
+// h holds the FP32 copy widened to FP64; interior points take the FP64
+// master plus the change the FP32 copy received since the last RK3 update.
+__global__ void k_master_to_halo(Geo g, const double* z, double* h) {
+  int i, j, k;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (!point_of(g, idx, i, j, k)) return;
+  const long long p = hidx(g, i, j, k);
+  const double master = z[idx];
+  const float inc = (float)h[p] - __double2float_rn(master);
+  h[p] = master + (double)inc;
+}
+
 // FP64 FMA throughput probe: eight independent register-resident chains.
 __global__ void k_fp64_probe(double* out, int iters, double a, double b) {
   double x0 = threadIdx.x * 1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
@@ -181,12 +204,22 @@ __global__ void k_fp64_probe(double* out, int iters, double a, double b) {
 // Host-side scheme set-up (restates fd_scheme_initiate,
 // src/derivative.F90:63-158; compact_filter_initiate, src/filter.F90:31-100;
 // filter_coefficient_cal, src/filter.F90:299-432; tridiagonal_thomas_
-// proprocess, src/commfunc.F90:752-774) plus the chunk carry weights.
+// proprocess, src/commfunc.F90:752-774) plus the chunk carry weights and the
+// ac2-folded interior coefficients.
 // ---------------------------------------------------------------------------
+const double H_NUM1D3 = 1.0 / 3.0;
+const double H_NUM7D9 = 7.0 / 9.0;
+const double H_NUM1D36 = 1.0 / 36.0;
+
+struct HostFTab {
+  double c10[6], c8[5], c6[4], cb[3][7], ch[3][11];
+};
+
 struct HostScheme {
   int first = 0, n = 0, ntype = 3, dim = 0;
-  std::vector<double> a, c, ac1, ac2, ac3, G, H;
-  void finish(int CH) {
+  bool filter = false;
+  std::vector<double> a, c, ac1, ac2, ac3, G, H, K, KD;
+  void finish(int CH, const HostFTab& t) {
     ac1.assign(n, 0.0); ac2.assign(n, 0.0); ac3.assign(n, 0.0);
     ac1[0] = c[0];
     for (int i = 1; i < n; ++i) {
@@ -202,14 +235,32 @@ struct HostScheme {
       p = 1.0;
       for (int r = e; r >= s; --r) { p *= -ac1[r]; H[r] = p; }
     }
+    // ac2-folded interior coefficients (row 0 is never an interior row)
+    if (filter) {
+      K.assign(6 * (size_t)n, 0.0);
+      KD.assign(5 * (size_t)n, 0.0);
+      for (int r = 0; r < n; ++r) {
+        K[r] = 2.0 * t.c10[0] * ac2[r];
+        for (int m = 1; m < 6; ++m) K[m * (size_t)n + r] = t.c10[m] * ac2[r];
+        // second-difference weights of (B - A) f on interior rows
+        KD[r] = (t.c10[1] - a[r]) * ac2[r];
+        for (int m = 2; m < 6; ++m) KD[(m - 1) * (size_t)n + r] = t.c10[m] * ac2[r];
+      }
+    } else {
+      K.assign(2 * (size_t)n, 0.0);
+      for (int r = 0; r < n; ++r) {
+        K[r] = H_NUM7D9 * ac2[r];
+        K[n + r] = H_NUM1D36 * ac2[r];
+      }
+    }
   }
 };
 
-HostScheme make_deriv(int ntype, int dim, int CH) {
+HostScheme make_deriv(int ntype, int dim, int CH, const HostFTab& t) {
   HostScheme s;
   int i0 = ntype == 4 ? 0 : -1, im = ntype == 4 ? dim : dim + 1;
   s.first = i0; s.n = im - i0 + 1; s.ntype = ntype; s.dim = dim;
-  s.a.assign(s.n, NUM1D3); s.c.assign(s.n, NUM1D3);
+  s.a.assign(s.n, H_NUM1D3); s.c.assign(s.n, H_NUM1D3);
   s.a[0] = s.c[0] = 0.0;
   s.a[s.n - 1] = s.c[s.n - 1] = 0.0;
   if (ntype == 4) {
@@ -218,24 +269,24 @@ HostScheme make_deriv(int ntype, int dim, int CH) {
     s.a[s.n - 1] = s.c[s.n - 1] = 2.0;
     s.a[s.n - 2] = s.c[s.n - 2] = 0.25;
   }
-  s.finish(CH);
+  s.finish(CH, t);
   return s;
 }
 
-HostScheme make_filter(int ntype, int dim, double alfa, int CH) {
+HostScheme make_filter(int ntype, int dim, double alfa, int CH, const HostFTab& t) {
   HostScheme s;
   int i0 = ntype == 4 ? 0 : -3, im = ntype == 4 ? dim : dim + 3;
   double b = ntype == 4 ? 0.98 : 1.11;
-  s.first = i0; s.n = im - i0 + 1; s.ntype = ntype; s.dim = dim;
+  s.first = i0; s.n = im - i0 + 1; s.ntype = ntype; s.dim = dim; s.filter = true;
   s.a.assign(s.n, alfa); s.c.assign(s.n, alfa);
   s.a[0] = s.c[0] = b;
   s.a[s.n - 1] = s.c[s.n - 1] = b;
-  s.finish(CH);
+  s.finish(CH, t);
   return s;
 }
 
-FTab make_ftab(double alfa, double bh, double bb) {
-  FTab t;
+HostFTab make_ftab(double alfa, double bh, double bb) {
+  HostFTab t;
   std::memset(&t, 0, sizeof(t));
   t.c6[0] = (11.0 + 10.0 * alfa) / 32.0;
   t.c6[1] = (15.0 + 34.0 * alfa) / 64.0;
@@ -287,6 +338,19 @@ FTab make_ftab(double alfa, double bh, double bb) {
   return t;
 }
 
+template <typename T>
+FTab<T> cast_ftab(const HostFTab& h) {
+  FTab<T> t;
+  for (int m = 0; m < 6; ++m) t.c10[m] = (T)h.c10[m];
+  for (int m = 0; m < 5; ++m) t.c8[m] = (T)h.c8[m];
+  for (int m = 0; m < 4; ++m) t.c6[m] = (T)h.c6[m];
+  for (int r = 0; r < 3; ++r) {
+    for (int m = 0; m < 7; ++m) t.cb[r][m] = (T)h.cb[r][m];
+    for (int m = 0; m < 11; ++m) t.ch[r][m] = (T)h.ch[r][m];
+  }
+  return t;
+}
+
 const int kCH[] = {3, 5, 9, 17, 33};
 
 int pick_ch(int nmax) {
@@ -306,14 +370,19 @@ struct astr_ctx {
   astr_dims dm;
   astr_params pm;
   Geo g;
-  Dev d;
   Phys ph;
-  FTab ft;
-  DScheme fd[3], fl[3];
+  int prec = ASTR_FP64;
+  DevT<double> d64;
+  DevT<float> d32;
+  FTab<double> ft64;
+  FTab<float> ft32;
+  DScheme<double> fd64[3], fl64[3];
+  DScheme<float> fd32[3], fl32[3];
   int CH[3] = {0, 0, 0};
-  double* coef = nullptr;
   double* stats_dev = nullptr;
-  long long part_cap = 0;
+  double* staging = nullptr;  // nh doubles (FP32 form: host <-> device conversions)
+  double* jac64 = nullptr;
+  double* rjac64 = nullptr;
   cudaStream_t st = nullptr;
   std::string err;
   long long launches = 0;
@@ -328,6 +397,19 @@ struct astr_ctx {
 };
 
 namespace {
+
+template <typename T> DevT<T>& dev(astr_ctx* c);
+template <> DevT<double>& dev<double>(astr_ctx* c) { return c->d64; }
+template <> DevT<float>& dev<float>(astr_ctx* c) { return c->d32; }
+template <typename T> const FTab<T>& ftab(astr_ctx* c);
+template <> const FTab<double>& ftab<double>(astr_ctx* c) { return c->ft64; }
+template <> const FTab<float>& ftab<float>(astr_ctx* c) { return c->ft32; }
+template <typename T> const DScheme<T>& sch_d(astr_ctx* c, int dir);
+template <> const DScheme<double>& sch_d<double>(astr_ctx* c, int dir) { return c->fd64[dir]; }
+template <> const DScheme<float>& sch_d<float>(astr_ctx* c, int dir) { return c->fd32[dir]; }
+template <typename T> const DScheme<T>& sch_f(astr_ctx* c, int dir);
+template <> const DScheme<double>& sch_f<double>(astr_ctx* c, int dir) { return c->fl64[dir]; }
+template <> const DScheme<float>& sch_f<float>(astr_ctx* c, int dir) { return c->fl32[dir]; }
 
 int fail(astr_ctx* c, int code, const std::string& msg) {
   if (c) c->err = msg;
@@ -345,6 +427,12 @@ int cuda_check(astr_ctx* c, cudaError_t e, const char* what) {
   do {                                                           \
     int _rc = cuda_check(c, (call), #call);                      \
     if (_rc != ASTR_OK) return _rc;                              \
+  } while (0)
+
+#define RC(x)                      \
+  do {                             \
+    int _r = (x);                  \
+    if (_r != ASTR_OK) return _r;  \
   } while (0)
 
 int after_launch(astr_ctx* c, const char* what) {
@@ -383,7 +471,10 @@ long long sweep_warps(const Geo& g) {
   return (long long)gr.x * gr.y * (bl.x * bl.y / 32);
 }
 
-SweepCtx sctx(const astr_ctx* c) { return SweepCtx{c->g, c->d, c->ph, c->st}; }
+template <typename T>
+SweepCtx<T> sctx(astr_ctx* c) {
+  return SweepCtx<T>{c->g, dev<T>(c), c->ph, c->st};
+}
 
 int launch_result(astr_ctx* c, cudaError_t e, const char* what) {
   ++c->launches;
@@ -393,73 +484,72 @@ int launch_result(astr_ctx* c, cudaError_t e, const char* what) {
   return ASTR_OK;
 }
 
-template <int DIR>
+template <typename T, int DIR>
 int launch_filter(astr_ctx* c, int do_q2f) {
   prof_begin(c, KC_FILTER);
-  const cudaError_t e = astr::launch_filter<DIR>(sctx(c), c->fl[DIR], c->ft, c->CH[DIR], do_q2f);
+  const cudaError_t e = astr::launch_filter<T, DIR>(sctx<T>(c), sch_f<T>(c, DIR), ftab<T>(c),
+                                                    c->CH[DIR], do_q2f);
   prof_end(c);
   return launch_result(c, e, "k_filter");
 }
 
-template <int DIR>
+template <typename T, int DIR>
 int launch_convgrad(astr_ctx* c, CGFlags f) {
   prof_begin(c, (f.conv || f.grad) ? KC_CONVGRAD : KC_STATS);
-  const cudaError_t e = astr::launch_convgrad<DIR>(sctx(c), c->fd[DIR], c->CH[DIR], f);
+  const cudaError_t e = astr::launch_convgrad<T, DIR>(sctx<T>(c), sch_d<T>(c, DIR), c->CH[DIR], f);
   prof_end(c);
   return launch_result(c, e, "k_convgrad");
 }
 
-template <int DIR>
+template <typename T, int DIR>
 int launch_visc(astr_ctx* c, VFlags f) {
   prof_begin(c, KC_VISC);
-  const cudaError_t e = astr::launch_visc<DIR>(sctx(c), c->fd[DIR], c->CH[DIR], f);
+  const cudaError_t e = astr::launch_visc<T, DIR>(sctx<T>(c), sch_d<T>(c, DIR), c->CH[DIR], f);
   prof_end(c);
   return launch_result(c, e, "k_visc");
 }
 
-template <int DIR>
+template <typename T, int DIR>
 int launch_face(astr_ctx* c, bool mini) {
   const Geo& g = c->g;
   const int na = DIR == 0 ? g.jm : g.im;
   const int nb = DIR == 2 ? g.jm : g.km;
   dim3 bl(128), gr((na + 128) / 128, nb + 1);
   prof_begin(c, KC_HALO);
-  if (mini) k_bchomo<DIR><<<gr, bl, 0, c->st>>>(c->g, c->d, c->ph);
-  else k_qswap<DIR><<<gr, bl, 0, c->st>>>(c->g, c->d, c->ph);
+  if (mini) k_bchomo<T, DIR><<<gr, bl, 0, c->st>>>(c->g, dev<T>(c), c->ph);
+  else k_qswap<T, DIR><<<gr, bl, 0, c->st>>>(c->g, dev<T>(c), c->ph);
   prof_end(c);
   return after_launch(c, mini ? "k_bchomo" : "k_qswap");
 }
 
-dim3 point_grid(const Geo& g) { return dim3((unsigned)((g.n0 + 255) / 256)); }
+dim3 point_grid(long long n) { return dim3((unsigned)((n + 255) / 256)); }
 
-#define RC(x)                      \
-  do {                             \
-    int _r = (x);                  \
-    if (_r != ASTR_OK) return _r;  \
-  } while (0)
-
+template <typename T>
 int run_filter(astr_ctx* c, bool q2f_last) {
   const int nd = c->g.ndims;
-  RC(launch_filter<0>(c, 0));
-  RC(launch_filter<1>(c, (q2f_last && nd == 2) ? 1 : 0));
-  if (nd == 3) RC(launch_filter<2>(c, q2f_last ? 1 : 0));
+  RC((launch_filter<T, 0>(c, 0)));
+  RC((launch_filter<T, 1>(c, (q2f_last && nd == 2) ? 1 : 0)));
+  if (nd == 3) RC((launch_filter<T, 2>(c, q2f_last ? 1 : 0)));
   return ASTR_OK;
 }
 
+template <typename T>
 int run_qswap(astr_ctx* c) {
-  if (c->g.per[0]) RC(launch_face<0>(c, false));
-  if (c->g.per[1]) RC(launch_face<1>(c, false));
-  if (c->g.per[2]) RC(launch_face<2>(c, false));
+  if (c->g.per[0]) RC((launch_face<T, 0>(c, false)));
+  if (c->g.per[1]) RC((launch_face<T, 1>(c, false)));
+  if (c->g.per[2]) RC((launch_face<T, 2>(c, false)));
   return ASTR_OK;
 }
 
+template <typename T>
 int run_bchomo(astr_ctx* c) {
-  RC(launch_face<0>(c, true));
-  RC(launch_face<1>(c, true));
-  if (c->g.ndims == 3) RC(launch_face<2>(c, true));
+  RC((launch_face<T, 0>(c, true)));
+  RC((launch_face<T, 1>(c, true)));
+  if (c->g.ndims == 3) RC((launch_face<T, 2>(c, true)));
   return ASTR_OK;
 }
 
+template <typename T>
 int run_convgrad(astr_ctx* c, bool conv, bool grad, bool sigma, bool stats, bool qsave) {
   const int nd = c->g.ndims;
   for (int dir = 0; dir < nd; ++dir) {
@@ -470,19 +560,22 @@ int run_convgrad(astr_ctx* c, bool conv, bool grad, bool sigma, bool stats, bool
     f.sigma = sigma && f.last;
     f.stats = stats && f.last;
     f.qsave = qsave && dir == 0;
-    int r = dir == 0 ? launch_convgrad<0>(c, f) : (dir == 1 ? launch_convgrad<1>(c, f) : launch_convgrad<2>(c, f));
+    int r = dir == 0 ? launch_convgrad<T, 0>(c, f)
+                     : (dir == 1 ? launch_convgrad<T, 1>(c, f) : launch_convgrad<T, 2>(c, f));
     RC(r);
   }
   return ASTR_OK;
 }
 
+template <typename T>
 int run_visc(astr_ctx* c, bool fuse_rk, bool q2f) {
   const int nd = c->g.ndims;
   for (int dir = 0; dir < nd; ++dir) {
     VFlags f;
     f.last = fuse_rk && dir == nd - 1;
     f.q2f = q2f;
-    int r = dir == 0 ? launch_visc<0>(c, f) : (dir == 1 ? launch_visc<1>(c, f) : launch_visc<2>(c, f));
+    int r = dir == 0 ? launch_visc<T, 0>(c, f)
+                     : (dir == 1 ? launch_visc<T, 1>(c, f) : launch_visc<T, 2>(c, f));
     RC(r);
   }
   return ASTR_OK;
@@ -492,7 +585,7 @@ int stats_finish(astr_ctx* c, double* out2) {
   const int last = c->g.ndims - 1;
   const long long nw = last == 2 ? sweep_warps<2>(c->g) : (last == 1 ? sweep_warps<1>(c->g) : sweep_warps<0>(c->g));
   prof_begin(c, KC_STATS);
-  k_stats_final<<<1, 1024, 0, c->st>>>(c->d.part, nw, c->stats_dev);
+  k_stats_final<<<1, 1024, 0, c->st>>>(c->d64.part, nw, c->stats_dev);
   prof_end(c);
   RC(after_launch(c, "k_stats_final"));
   double h[2];
@@ -518,35 +611,76 @@ void set_stage(astr_ctx* c, int s) {
   c->ph.rk3 = rk[s][2];
 }
 
+template <typename T>
+int rk_pointwise(astr_ctx* c, int q2f) {
+  prof_begin(c, KC_POINT);
+  k_rkupdate<T><<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, dev<T>(c), c->ph, q2f);
+  prof_end(c);
+  return after_launch(c, "k_rkupdate");
+}
+
+template <typename T>
 int one_step(astr_ctx* c, double* stats) {
   const bool mini = c->pm.order == ASTR_ORDER_MINIAPP;
   for (int s = 0; s < 3; ++s) {
     set_stage(c, s);
     const bool st1 = s == 0;
     if (mini) {
-      RC(run_bchomo(c));
-      RC(run_convgrad(c, true, true, c->pm.diffterm != 0, st1 && stats, st1));
-      if (c->pm.diffterm) RC(run_visc(c, true, false));
-      else {
-        prof_begin(c, KC_POINT);
-        k_rkupdate<<<point_grid(c->g), 256, 0, c->st>>>(c->g, c->d, c->ph, 0);
-        prof_end(c);
-        RC(after_launch(c, "k_rkupdate"));
-      }
-      RC(run_filter(c, true));
+      RC(run_bchomo<T>(c));
+      RC(run_convgrad<T>(c, true, true, c->pm.diffterm != 0, st1 && stats, st1));
+      if (c->pm.diffterm) RC(run_visc<T>(c, true, false));
+      else RC(rk_pointwise<T>(c, 0));
+      RC(run_filter<T>(c, true));
     } else {
-      if (c->pm.lfilter) RC(run_filter(c, false));
-      RC(run_qswap(c));
-      RC(run_convgrad(c, true, true, c->pm.diffterm != 0, st1 && stats, st1));
-      if (c->pm.diffterm) RC(run_visc(c, true, true));
-      else {
-        prof_begin(c, KC_POINT);
-        k_rkupdate<<<point_grid(c->g), 256, 0, c->st>>>(c->g, c->d, c->ph, 1);
-        prof_end(c);
-        RC(after_launch(c, "k_rkupdate"));
-      }
+      if (c->pm.lfilter) RC(run_filter<T>(c, false));
+      RC(run_qswap<T>(c));
+      RC(run_convgrad<T>(c, true, true, c->pm.diffterm != 0, st1 && stats, st1));
+      if (c->pm.diffterm) RC(run_visc<T>(c, true, true));
+      else RC(rk_pointwise<T>(c, 1));
     }
     if (st1 && stats) RC(stats_finish(c, stats));
+  }
+  return ASTR_OK;
+}
+
+int step(astr_ctx* c, double* stats) {
+  return c->prec == ASTR_FP64 ? one_step<double>(c, stats) : one_step<float>(c, stats);
+}
+
+// --- host <-> device in the storage precision ---------------------------
+size_t wsize(const astr_ctx* c) { return c->prec == ASTR_FP64 ? 8 : 4; }
+
+int upload_array(astr_ctx* c, void* dst, const double* src, size_t n) {
+  if (c->prec == ASTR_FP64) {
+    CK(cudaMemcpyAsync(dst, src, n * 8, cudaMemcpyHostToDevice, c->st));
+    return ASTR_OK;
+  }
+  CK(cudaMemcpyAsync(c->staging, src, n * 8, cudaMemcpyHostToDevice, c->st));
+  k_to_float<<<point_grid((long long)n), 256, 0, c->st>>>(c->staging, (float*)dst, (long long)n);
+  return after_launch(c, "k_to_float");
+}
+
+int download_array(astr_ctx* c, double* dst, const void* src, size_t n) {
+  if (c->prec == ASTR_FP64) {
+    CK(cudaMemcpyAsync(dst, src, n * 8, cudaMemcpyDeviceToHost, c->st));
+    return ASTR_OK;
+  }
+  k_to_double<<<point_grid((long long)n), 256, 0, c->st>>>((const float*)src, c->staging, (long long)n);
+  RC(after_launch(c, "k_to_double"));
+  CK(cudaMemcpyAsync(dst, c->staging, n * 8, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));  // the staging buffer is reused by the next call
+  return ASTR_OK;
+}
+
+template <typename T>
+int rhscal_t(astr_ctx* c) {
+  RC(run_convgrad<T>(c, true, false, false, false, false));
+  if (c->pm.diffterm) {
+    prof_begin(c, KC_POINT);
+    k_sigma<T><<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, dev<T>(c), c->ph);
+    prof_end(c);
+    RC(after_launch(c, "k_sigma"));
+    RC(run_visc<T>(c, false, false));
   }
   return ASTR_OK;
 }
@@ -559,11 +693,17 @@ int one_step(astr_ctx* c, double* stats) {
 extern "C" {
 
 size_t astr_gpu_footprint(const astr_dims* dims, const astr_params* params) {
-  (void)params;
   if (!dims) return 0;
   const size_t nh = (size_t)(dims->im + 2 * HMD + 1) * (dims->jm + 2 * HMD + 1) * (dims->km + 2 * HMD + 1);
   const size_t n0 = (size_t)(dims->im + 1) * (dims->jm + 1) * (dims->km + 1);
-  return 8 * (15 * nh + 31 * n0);
+  const bool f32 = params && params->precision == ASTR_FP32_STORAGE;
+  const size_t w = f32 ? 4 : 8;
+  // q 5, primitives 6, metrics 4 (halo arrays, storage type); 1/J (FP64);
+  // qrhs 5, gradients 12, sigma 6, heat flux 3 (interior, storage type);
+  // qsave 5 (FP64); FP32 form: J, master q 5 and a staging array in FP64
+  size_t b = w * (15 * nh + 26 * n0) + 8 * (nh + 5 * n0);
+  if (f32) b += 8 * (2 * nh + 5 * n0);
+  return b;
 }
 
 int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx** out) {
@@ -576,8 +716,8 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
   const int npdc[3] = {dims->npdci, dims->npdcj, dims->npdck};
   for (int i = 0; i < 3; ++i)
     if (npdc[i] != 3 && npdc[i] != 4) return fail(nullptr, ASTR_ERR_UNSUPPORTED, "npdc must be 3 or 4 on one rank");
-  if (params->precision != ASTR_FP64)
-    return fail(nullptr, ASTR_ERR_UNSUPPORTED, "only the FP64 form is built in this library version");
+  if (params->precision != ASTR_FP64 && params->precision != ASTR_FP32_STORAGE)
+    return fail(nullptr, ASTR_ERR_ARG, "precision must be ASTR_FP64 or ASTR_FP32_STORAGE");
   if (params->order == ASTR_ORDER_MINIAPP && (npdc[0] != 3 || npdc[1] != 3 || (ndims == 3 && npdc[2] != 3)))
     return fail(nullptr, ASTR_ERR_ARG, "mini-app ordering is periodic only");
   if (ndims == 2 && npdc[2] != 3) return fail(nullptr, ASTR_ERR_ARG, "2-D cases need npdck = 3");
@@ -585,6 +725,7 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
   c = new astr_ctx();
   c->dm = *dims;
   c->pm = *params;
+  c->prec = params->precision;
   const int dimv[3] = {dims->im, dims->jm, dims->km};
   for (int d = 0; d < ndims; ++d) {
     const int nmax = npdc[d] == 4 ? dimv[d] + 1 : dimv[d] + 7;
@@ -608,18 +749,27 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
   // refcal (src/solver.F90:102-128)
   const double gamma = 1.4, mach = params->mach;
   Phys& ph = c->ph;
-  ph.const2 = gamma * (mach * mach);
-  ph.const5 = (gamma - 1.0) * (mach * mach);
-  ph.const6 = 1.0 / (gamma - 1.0);
+  std::memset(&ph, 0, sizeof(ph));
+  const double const2 = gamma * (mach * mach);
+  const double const5 = (gamma - 1.0) * (mach * mach);
+  const double const6 = 1.0 / (gamma - 1.0);
+  ph.const2 = const2;
+  ph.rconst6 = 1.0 / const6;
+  ph.hcc_scale = 1.0 / (params->prandtl * const5);
   ph.tempconst = params->suth_const / params->ref_tem;
   ph.tempconst1 = 1.0 + ph.tempconst;
-  ph.reynolds = params->reynolds;
-  ph.prandtl = params->prandtl;
+  ph.rreynolds = 1.0 / params->reynolds;
   ph.dt = params->deltat;
   ph.mini = params->order == ASTR_ORDER_MINIAPP;
   const double PI = 4.0 * std::atan(1.0);
-  for (int d = 0; d < 3; ++d) ph.dx[d] = dimv[d] > 0 ? 2.0 * PI / (double)dimv[d] : 1.0;
-  c->ft = make_ftab(params->alfa_filter, params->beter_halo, params->beter_bound);
+  for (int d = 0; d < 3; ++d) ph.rdx[d] = dimv[d] > 0 ? 1.0 / (2.0 * PI / (double)dimv[d]) : 1.0;
+  ph.f_const2 = (float)ph.const2; ph.f_rconst6 = (float)ph.rconst6;
+  ph.f_hcc_scale = (float)ph.hcc_scale; ph.f_tempconst = (float)ph.tempconst;
+  ph.f_tempconst1 = (float)ph.tempconst1; ph.f_rreynolds = (float)ph.rreynolds;
+  for (int d = 0; d < 3; ++d) ph.f_rdx[d] = (float)ph.rdx[d];
+  const HostFTab hft = make_ftab(params->alfa_filter, params->beter_halo, params->beter_bound);
+  c->ft64 = cast_ftab<double>(hft);
+  c->ft32 = cast_ftab<float>(hft);
 
   cudaError_t e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
@@ -627,74 +777,94 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
     delete c;
     return fail(nullptr, ASTR_ERR_CUDA, m);
   }
+  bool ok = true;
   auto alloc = [&](size_t bytes) -> void* {
     void* p = nullptr;
-    if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
+    if (cudaMalloc(&p, bytes) != cudaSuccess) { ok = false; return nullptr; }
     c->allocs.push_back(p);
     return p;
   };
-  const size_t nh = (size_t)g.nh, n0 = (size_t)g.n0;
-  Dev& d = c->d;
-  d.q = (double*)alloc(5 * nh * 8);
-  d.pr = (double*)alloc(6 * nh * 8);
-  double* xd = (double*)alloc(3 * nh * 8);
-  double* jac = (double*)alloc(nh * 8);
-  d.xd = xd; d.jac = jac;
-  d.qrhs = (double*)alloc(5 * n0 * 8);
-  d.qsave = (double*)alloc(5 * n0 * 8);
-  d.grad = (double*)alloc(12 * n0 * 8);
-  d.sig = (double*)alloc(6 * n0 * 8);
-  d.qf = (double*)alloc(3 * n0 * 8);
+  const bool f32 = c->prec == ASTR_FP32_STORAGE;
+  const size_t nh = (size_t)g.nh, n0 = (size_t)g.n0, w = wsize(c);
+  void* q = alloc(5 * nh * w);
+  void* pr = alloc(6 * nh * w);
+  void* xd = alloc(3 * nh * w);
+  void* jac = alloc(nh * w);
+  void* qrhs = alloc(5 * n0 * w);
+  void* grad = alloc(12 * n0 * w);
+  void* sig = alloc(6 * n0 * w);
+  void* qf = alloc(3 * n0 * w);
+  double* qsave = (double*)alloc(5 * n0 * 8);
+  double* qm = f32 ? (double*)alloc(5 * n0 * 8) : nullptr;
+  c->staging = f32 ? (double*)alloc(nh * 8) : nullptr;
+  c->jac64 = f32 ? (double*)alloc(nh * 8) : (double*)jac;
+  c->rjac64 = (double*)alloc(nh * 8);
   long long nw = std::max(sweep_warps<0>(g), std::max(sweep_warps<1>(g), sweep_warps<2>(g)));
-  c->part_cap = nw;
-  d.part = (double*)alloc(2 * nw * 8);
-  d.flag = (int*)alloc(64);
+  double* part = (double*)alloc(2 * nw * 8);
+  int* flag = (int*)alloc(64);
   c->stats_dev = (double*)alloc(64);
-  // schemes
+  // schemes: per direction derivative + filter, in both precisions
   std::vector<HostScheme> hs;
   for (int dd = 0; dd < 3; ++dd) {
     const int CH = dd < ndims ? c->CH[dd] : 3;
-    hs.push_back(make_deriv(npdc[dd], std::max(dimv[dd], 1), CH));
-    hs.push_back(make_filter(npdc[dd], std::max(dimv[dd], 1), params->alfa_filter, CH));
+    hs.push_back(make_deriv(npdc[dd], std::max(dimv[dd], 1), CH, hft));
+    hs.push_back(make_filter(npdc[dd], std::max(dimv[dd], 1), params->alfa_filter, CH, hft));
   }
   size_t tot = 0;
-  for (auto& s : hs) tot += 5 * (size_t)s.n;
-  c->coef = (double*)alloc(tot * 8);
-  bool ok = d.q && d.pr && xd && jac && d.qrhs && d.qsave && d.grad && d.sig && d.qf && d.part &&
-            d.flag && c->stats_dev && c->coef;
+  for (auto& s : hs) tot += 6 * (size_t)s.n + s.K.size() + s.KD.size();
+  double* coef64 = (double*)alloc(tot * 8);
+  float* coef32 = (float*)alloc(tot * 4);
   if (!ok) {
     astr_gpu_destroy(c);
     return fail(nullptr, ASTR_ERR_OOM, "device allocation failed");
   }
   std::vector<double> hbuf(tot);
+  std::vector<float> fbuf(tot);
   size_t off = 0;
   for (int idx = 0; idx < 6; ++idx) {
     HostScheme& s = hs[idx];
-    const size_t n = s.n;
-    double* dst = c->coef + off;
-    std::memcpy(&hbuf[off], s.ac1.data(), n * 8);
-    std::memcpy(&hbuf[off + n], s.ac2.data(), n * 8);
-    std::memcpy(&hbuf[off + 2 * n], s.ac3.data(), n * 8);
-    std::memcpy(&hbuf[off + 3 * n], s.G.data(), n * 8);
-    std::memcpy(&hbuf[off + 4 * n], s.H.data(), n * 8);
-    DScheme ds;
-    ds.ac1 = dst; ds.ac2 = dst + n; ds.ac3 = dst + 2 * n; ds.G = dst + 3 * n; ds.H = dst + 4 * n;
-    ds.n = s.n; ds.first = s.first; ds.ntype = s.ntype; ds.dim = s.dim;
-    if (idx % 2 == 0) c->fd[idx / 2] = ds;
-    else c->fl[idx / 2] = ds;
-    off += 5 * n;
+    const size_t n = s.n, nk = s.K.size(), nkd = s.KD.size();
+    const std::vector<double>* arr[6] = {&s.ac1, &s.ac3, &s.G, &s.H, &s.ac2, &s.a};
+    for (int a = 0; a < 6; ++a) std::memcpy(&hbuf[off + a * n], arr[a]->data(), n * 8);
+    std::memcpy(&hbuf[off + 6 * n], s.K.data(), nk * 8);
+    if (nkd) std::memcpy(&hbuf[off + 6 * n + nk], s.KD.data(), nkd * 8);
+    const size_t len = 6 * n + nk + nkd;
+    for (size_t i = 0; i < len; ++i) fbuf[off + i] = (float)hbuf[off + i];
+    DScheme<double> d8;
+    DScheme<float> d4;
+    d8.ac1 = coef64 + off; d8.ac3 = coef64 + off + n; d8.G = coef64 + off + 2 * n;
+    d8.H = coef64 + off + 3 * n; d8.ac2 = coef64 + off + 4 * n; d8.A = coef64 + off + 5 * n;
+    d8.K = coef64 + off + 6 * n; d8.KD = nkd ? coef64 + off + 6 * n + nk : nullptr;
+    d4.ac1 = coef32 + off; d4.ac3 = coef32 + off + n; d4.G = coef32 + off + 2 * n;
+    d4.H = coef32 + off + 3 * n; d4.ac2 = coef32 + off + 4 * n; d4.A = coef32 + off + 5 * n;
+    d4.K = coef32 + off + 6 * n; d4.KD = nkd ? coef32 + off + 6 * n + nk : nullptr;
+    d8.n = d4.n = s.n; d8.first = d4.first = s.first; d8.ntype = d4.ntype = s.ntype;
+    d8.dim = d4.dim = s.dim;
+    if (idx % 2 == 0) { c->fd64[idx / 2] = d8; c->fd32[idx / 2] = d4; }
+    else { c->fl64[idx / 2] = d8; c->fl32[idx / 2] = d4; }
+    off += len;
   }
-  e = cudaMemcpy(c->coef, hbuf.data(), tot * 8, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemset(d.q, 0, 5 * nh * 8);
-  if (e == cudaSuccess) e = cudaMemset(d.pr, 0, 6 * nh * 8);
-  if (e == cudaSuccess) e = cudaMemset(d.qrhs, 0, 5 * n0 * 8);
-  if (e == cudaSuccess) e = cudaMemset(d.grad, 0, 12 * n0 * 8);
-  if (e == cudaSuccess) e = cudaMemset(d.flag, 0, 64);
+  e = cudaMemcpy(coef64, hbuf.data(), tot * 8, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(coef32, fbuf.data(), tot * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(q, 0, 5 * nh * w);
+  if (e == cudaSuccess) e = cudaMemset(pr, 0, 6 * nh * w);
+  if (e == cudaSuccess) e = cudaMemset(qrhs, 0, 5 * n0 * w);
+  if (e == cudaSuccess) e = cudaMemset(grad, 0, 12 * n0 * w);
+  if (e == cudaSuccess) e = cudaMemset(flag, 0, 64);
   if (e != cudaSuccess) {
     std::string m = std::string("initialisation: ") + cudaGetErrorString(e);
     astr_gpu_destroy(c);
     return fail(nullptr, ASTR_ERR_CUDA, m);
   }
+  auto fill = [&](auto& D, auto* tag) {
+    using TT = std::remove_pointer_t<decltype(tag)>;
+    D.q = (TT*)q; D.pr = (TT*)pr; D.xd = (const TT*)xd; D.jac = (const TT*)jac;
+    D.jac64 = c->jac64; D.rjac64 = c->rjac64;
+    D.qrhs = (TT*)qrhs; D.qsave = qsave; D.qm = qm; D.grad = (TT*)grad; D.sig = (TT*)sig;
+    D.qf = (TT*)qf; D.part = part; D.flag = flag;
+  };
+  fill(c->d64, (double*)nullptr);
+  fill(c->d32, (float*)nullptr);
   *out = c;
   return ASTR_OK;
 }
@@ -706,6 +876,20 @@ void astr_gpu_destroy(astr_ctx* c) {
   for (void* p : c->allocs) cudaFree(p);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
+}
+
+static int metrics_common(astr_ctx* c, const double* const src[3], const double* jacob) {
+  const size_t nh = (size_t)c->g.nh, w = wsize(c);
+  char* xd = (char*)c->d64.xd;
+  for (int dd = 0; dd < 3; ++dd) RC(upload_array(c, xd + dd * nh * w, src[dd], nh));
+  RC(upload_array(c, (void*)c->d64.jac, jacob, nh));
+  if (c->prec == ASTR_FP32_STORAGE)
+    CK(cudaMemcpyAsync(c->jac64, jacob, nh * 8, cudaMemcpyHostToDevice, c->st));
+  k_reciprocal<<<point_grid((long long)nh), 256, 0, c->st>>>(c->jac64, c->rjac64, (long long)nh);
+  RC(after_launch(c, "k_reciprocal"));
+  CK(cudaStreamSynchronize(c->st));
+  c->metrics_set = true;
+  return ASTR_OK;
 }
 
 int astr_gpu_set_metrics(astr_ctx* c, const double* dxi, const double* jacob) {
@@ -720,24 +904,36 @@ int astr_gpu_set_metrics(astr_ctx* c, const double* dxi, const double* jacob) {
         if (p[i] != 0.0)
           return fail(c, ASTR_ERR_UNSUPPORTED, "non-diagonal grid metrics are not supported");
     }
-  for (int dd = 0; dd < 3; ++dd)
-    CK(cudaMemcpyAsync((double*)c->d.xd + dd * nh, dxi + (size_t)(dd + 3 * dd) * nh, nh * 8,
-                       cudaMemcpyHostToDevice, c->st));
-  CK(cudaMemcpyAsync((double*)c->d.jac, jacob, nh * 8, cudaMemcpyHostToDevice, c->st));
-  CK(cudaStreamSynchronize(c->st));
-  c->metrics_set = true;
-  return ASTR_OK;
+  const double* const src[3] = {dxi, dxi + 4 * nh, dxi + 8 * nh};
+  return metrics_common(c, src, jacob);
+}
+
+int astr_gpu_set_metrics_diag(astr_ctx* c, const double* x11, const double* x22, const double* x33,
+                              const double* jacob) {
+  if (!c || !x11 || !x22 || !x33 || !jacob) return fail(c, ASTR_ERR_ARG, "null argument");
+  const double* const src[3] = {x11, x22, x33};
+  return metrics_common(c, src, jacob);
 }
 
 int astr_gpu_upload_state(astr_ctx* c, const double* q, const double* rho, const double* vel,
                           const double* prs, const double* tmp) {
   if (!c || !q || !rho || !vel || !prs || !tmp) return fail(c, ASTR_ERR_ARG, "null argument");
-  const size_t nh = (size_t)c->g.nh;
-  CK(cudaMemcpyAsync(c->d.q, q, 5 * nh * 8, cudaMemcpyHostToDevice, c->st));
-  CK(cudaMemcpyAsync(c->d.pr, rho, nh * 8, cudaMemcpyHostToDevice, c->st));
-  CK(cudaMemcpyAsync(c->d.pr + nh, vel, 3 * nh * 8, cudaMemcpyHostToDevice, c->st));
-  CK(cudaMemcpyAsync(c->d.pr + 4 * nh, prs, nh * 8, cudaMemcpyHostToDevice, c->st));
-  CK(cudaMemcpyAsync(c->d.pr + 5 * nh, tmp, nh * 8, cudaMemcpyHostToDevice, c->st));
+  const size_t nh = (size_t)c->g.nh, w = wsize(c);
+  char* dq = (char*)c->d64.q;
+  char* dp = (char*)c->d64.pr;
+  for (int m = 0; m < 5; ++m) {
+    RC(upload_array(c, dq + m * nh * w, q + m * nh, nh));
+    if (c->prec == ASTR_FP32_STORAGE) {
+      // the FP64 master takes the uploaded interior values directly
+      k_halo_to_interior<<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, c->staging,
+                                                                 c->d32.qm + m * c->g.n0);
+      RC(after_launch(c, "k_halo_to_interior"));
+    }
+  }
+  RC(upload_array(c, dp, rho, nh));
+  for (int m = 0; m < 3; ++m) RC(upload_array(c, dp + (1 + m) * nh * w, vel + m * nh, nh));
+  RC(upload_array(c, dp + 4 * nh * w, prs, nh));
+  RC(upload_array(c, dp + 5 * nh * w, tmp, nh));
   CK(cudaStreamSynchronize(c->st));
   c->state_set = true;
   return ASTR_OK;
@@ -745,22 +941,45 @@ int astr_gpu_upload_state(astr_ctx* c, const double* q, const double* rho, const
 
 int astr_gpu_download_state(astr_ctx* c, double* q, double* rho, double* vel, double* prs, double* tmp) {
   if (!c) return fail(c, ASTR_ERR_ARG, "null context");
-  const size_t nh = (size_t)c->g.nh;
-  if (q) CK(cudaMemcpyAsync(q, c->d.q, 5 * nh * 8, cudaMemcpyDeviceToHost, c->st));
-  if (rho) CK(cudaMemcpyAsync(rho, c->d.pr, nh * 8, cudaMemcpyDeviceToHost, c->st));
-  if (vel) CK(cudaMemcpyAsync(vel, c->d.pr + nh, 3 * nh * 8, cudaMemcpyDeviceToHost, c->st));
-  if (prs) CK(cudaMemcpyAsync(prs, c->d.pr + 4 * nh, nh * 8, cudaMemcpyDeviceToHost, c->st));
-  if (tmp) CK(cudaMemcpyAsync(tmp, c->d.pr + 5 * nh, nh * 8, cudaMemcpyDeviceToHost, c->st));
+  const size_t nh = (size_t)c->g.nh, w = wsize(c);
+  const char* dq = (const char*)c->d64.q;
+  const char* dp = (const char*)c->d64.pr;
+  if (q) {
+    for (int m = 0; m < 5; ++m) {
+      if (c->prec == ASTR_FP64) {
+        CK(cudaMemcpyAsync(q + m * nh, dq + m * nh * w, nh * 8, cudaMemcpyDeviceToHost, c->st));
+      } else {
+        // halos from the FP32 copy, interior from the FP64 master
+        k_to_double<<<point_grid((long long)nh), 256, 0, c->st>>>((const float*)(dq + m * nh * w),
+                                                                   c->staging, (long long)nh);
+        RC(after_launch(c, "k_to_double"));
+        k_master_to_halo<<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, c->d32.qm + m * c->g.n0,
+                                                                 c->staging);
+        RC(after_launch(c, "k_master_to_halo"));
+        CK(cudaMemcpyAsync(q + m * nh, c->staging, nh * 8, cudaMemcpyDeviceToHost, c->st));
+        CK(cudaStreamSynchronize(c->st));
+      }
+    }
+  }
+  if (rho) RC(download_array(c, rho, dp, nh));
+  if (vel)
+    for (int m = 0; m < 3; ++m) RC(download_array(c, vel + m * nh, dp + (1 + m) * nh * w, nh));
+  if (prs) RC(download_array(c, prs, dp + 4 * nh * w, nh));
+  if (tmp) RC(download_array(c, tmp, dp + 5 * nh * w, nh));
   CK(cudaStreamSynchronize(c->st));
   return ASTR_OK;
 }
 
 int astr_gpu_download_rhs(astr_ctx* c, double* qrhs, double* dvel, double* dtmp) {
   if (!c) return fail(c, ASTR_ERR_ARG, "null context");
-  const size_t n0 = (size_t)c->g.n0;
-  if (qrhs) CK(cudaMemcpyAsync(qrhs, c->d.qrhs, 5 * n0 * 8, cudaMemcpyDeviceToHost, c->st));
-  if (dvel) CK(cudaMemcpyAsync(dvel, c->d.grad, 9 * n0 * 8, cudaMemcpyDeviceToHost, c->st));
-  if (dtmp) CK(cudaMemcpyAsync(dtmp, c->d.grad + 9 * n0, 3 * n0 * 8, cudaMemcpyDeviceToHost, c->st));
+  const size_t n0 = (size_t)c->g.n0, w = wsize(c);
+  if (qrhs)
+    for (int m = 0; m < 5; ++m) RC(download_array(c, qrhs + m * n0, (char*)c->d64.qrhs + m * n0 * w, n0));
+  if (dvel)
+    for (int m = 0; m < 9; ++m) RC(download_array(c, dvel + m * n0, (char*)c->d64.grad + m * n0 * w, n0));
+  if (dtmp)
+    for (int m = 0; m < 3; ++m)
+      RC(download_array(c, dtmp + m * n0, (char*)c->d64.grad + (9 + m) * n0 * w, n0));
   CK(cudaStreamSynchronize(c->st));
   return ASTR_OK;
 }
@@ -776,10 +995,10 @@ static int ready(astr_ctx* c) {
 int astr_gpu_rk3_step(astr_ctx* c, int nsteps, double* hist, astr_status* status) {
   RC(ready(c));
   if (nsteps < 0) return fail(c, ASTR_ERR_ARG, "nsteps < 0");
-  for (int s = 0; s < nsteps; ++s) RC(one_step(c, hist ? hist + 2 * s : nullptr));
+  for (int s = 0; s < nsteps; ++s) RC(step(c, hist ? hist + 2 * s : nullptr));
   if (status) {
     int flag = 0;
-    CK(cudaMemcpyAsync(&flag, c->d.flag, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaMemcpyAsync(&flag, c->d64.flag, sizeof(int), cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
     status->crash = flag;
     status->kenergy = hist && nsteps > 0 ? hist[2 * (nsteps - 1)] : 0.0;
@@ -791,43 +1010,46 @@ int astr_gpu_rk3_step(astr_ctx* c, int nsteps, double* hist, astr_status* status
 
 int astr_gpu_filterq(astr_ctx* c) {
   RC(ready(c));
-  return run_filter(c, false);
+  return c->prec == ASTR_FP64 ? run_filter<double>(c, false) : run_filter<float>(c, false);
 }
 
 int astr_gpu_qswap(astr_ctx* c) {
   RC(ready(c));
-  return c->pm.order == ASTR_ORDER_MINIAPP ? run_bchomo(c) : run_qswap(c);
+  const bool mini = c->pm.order == ASTR_ORDER_MINIAPP;
+  if (c->prec == ASTR_FP64) return mini ? run_bchomo<double>(c) : run_qswap<double>(c);
+  return mini ? run_bchomo<float>(c) : run_qswap<float>(c);
 }
 
 int astr_gpu_gradcal(astr_ctx* c) {
   RC(ready(c));
-  return run_convgrad(c, false, true, false, false, false);
+  return c->prec == ASTR_FP64 ? run_convgrad<double>(c, false, true, false, false, false)
+                              : run_convgrad<float>(c, false, true, false, false, false);
 }
 
 int astr_gpu_rhscal(astr_ctx* c) {
   RC(ready(c));
-  RC(run_convgrad(c, true, false, false, false, false));
-  if (c->pm.diffterm) {
-    k_sigma<<<point_grid(c->g), 256, 0, c->st>>>(c->g, c->d, c->ph);
-    RC(after_launch(c, "k_sigma"));
-    RC(run_visc(c, false, false));
-  }
-  return ASTR_OK;
+  return c->prec == ASTR_FP64 ? rhscal_t<double>(c) : rhscal_t<float>(c);
 }
 
 int astr_gpu_updatefvar(astr_ctx* c) {
   RC(ready(c));
-  k_updatefvar<<<point_grid(c->g), 256, 0, c->st>>>(c->g, c->d, c->ph);
+  if (c->prec == ASTR_FP64)
+    k_updatefvar<double><<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, c->d64, c->ph);
+  else
+    k_updatefvar<float><<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, c->d32, c->ph);
   return after_launch(c, "k_updatefvar");
 }
 
 int astr_gpu_reduce_stats(astr_ctx* c, double* ke, double* en) {
   RC(ready(c));
-  // statistics pass over the current gradients: recompute through the last
+  // statistics over the current primitives and gradients: the last
   // conv/grad direction with only the statistics enabled
   CGFlags f{0, 0, 0, 0, 0, 1, 0};
   const int last = c->g.ndims - 1;
-  RC(last == 2 ? launch_convgrad<2>(c, f) : launch_convgrad<1>(c, f));
+  int r;
+  if (c->prec == ASTR_FP64) r = last == 2 ? launch_convgrad<double, 2>(c, f) : launch_convgrad<double, 1>(c, f);
+  else r = last == 2 ? launch_convgrad<float, 2>(c, f) : launch_convgrad<float, 1>(c, f);
+  RC(r);
   double o[2];
   RC(stats_finish(c, o));
   if (ke) *ke = o[0];
@@ -852,19 +1074,6 @@ int astr_gpu_last_error(astr_ctx* c, char* buf, int len) {
 
 long long astr_gpu_launch_count(astr_ctx* c) { return c ? c->launches : 0; }
 
-int astr_gpu_set_metrics_diag(astr_ctx* c, const double* x11, const double* x22, const double* x33,
-                              const double* jacob) {
-  if (!c || !x11 || !x22 || !x33 || !jacob) return fail(c, ASTR_ERR_ARG, "null argument");
-  const size_t nh = (size_t)c->g.nh;
-  const double* src[3] = {x11, x22, x33};
-  for (int dd = 0; dd < 3; ++dd)
-    CK(cudaMemcpyAsync((double*)c->d.xd + dd * nh, src[dd], nh * 8, cudaMemcpyHostToDevice, c->st));
-  CK(cudaMemcpyAsync((double*)c->d.jac, jacob, nh * 8, cudaMemcpyHostToDevice, c->st));
-  CK(cudaStreamSynchronize(c->st));
-  c->metrics_set = true;
-  return ASTR_OK;
-}
-
 void* astr_gpu_host_alloc(size_t bytes) {
   void* p = nullptr;
   if (cudaMallocHost(&p, bytes) != cudaSuccess) return nullptr;
@@ -883,7 +1092,7 @@ int astr_gpu_timed_steps(astr_ctx* c, int nsteps, double* elapsed_ms) {
   CK(cudaEventCreate(&e1));
   CK(cudaEventRecord(e0, c->st));
   int rc = ASTR_OK;
-  for (int s = 0; s < nsteps && rc == ASTR_OK; ++s) rc = one_step(c, nullptr);
+  for (int s = 0; s < nsteps && rc == ASTR_OK; ++s) rc = step(c, nullptr);
   CK(cudaEventRecord(e1, c->st));
   CK(cudaEventSynchronize(e1));
   float ms = 0.0f;

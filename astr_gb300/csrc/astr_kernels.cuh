@@ -10,12 +10,20 @@
 //   forward   y_r = ytilde_r + G_r * y_{s-1},  G_r = prod_{m=s..r} (-ac3_m)
 //   backward  x_r = xtilde_r + H_r * x_{e+1},  H_r = prod_{m=r..e} (-ac1_m)
 // where s..e are the rows of the chunk.  The matrix factors ac1..ac3 are the
-// reference's tridiagonal_thomas_proprocess (src/commfunc.F90:752-774).
+// reference's tridiagonal_thomas_proprocess (src/commfunc.F90:752-774).  The
+// forward factor ac2 is folded into per-row right-hand-side coefficients
+// (K7 = 7/9 ac2, K36 = 1/36 ac2 for the derivative; FK[m] = c10i(m) ac2 for
+// the filter), so the forward step is one fused multiply-add.
+//
+// Precision: every kernel is a template on T, the type the sweeps store and
+// compute in (double: the plain FP64 form; float: the FP32-storage form).
+// The FP32-storage form keeps the conserved variables' RK3 base and master
+// copy in FP64 (DevT::qsave, DevT::qm).
 //
 // Line orientation:
 //   x-lines (DIR 0): a warp per line, lane = chunk; lines are contiguous.
 //   y/z-lines (DIR 1,2): a block of 16 lines x 32 chunks; threadIdx.x walks
-//   16 consecutive i so every row access is a coalesced 128-byte segment.
+//   16 consecutive i so every row access is a coalesced segment.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -28,30 +36,30 @@ constexpr int NCH = 32;      // chunks per line
 constexpr int YZ_LINES = 16; // lines per block for y/z sweeps
 constexpr int X_LINES = 8;   // lines (warps) per block for x sweeps
 
-constexpr double NUM1D3 = 1.0 / 3.0;
-constexpr double NUM7D9 = 7.0 / 9.0;
-constexpr double NUM1D36 = 1.0 / 36.0;
-constexpr double NUM1D60 = 1.0 / 60.0;
-
 // One compact scheme (derivative or filter) of one direction, with the
 // chunk carry weights for the chunk length used on that direction.
+template <typename T>
 struct DScheme {
-  const double* ac1;
-  const double* ac2;
-  const double* ac3;
-  const double* G;
-  const double* H;
-  int n;      // rows of the system
-  int first;  // grid node of row 0
-  int ntype;  // 3: periodic / inner block, 4: physical boundary at both ends
-  int dim;    // im, jm or km
+  const T* ac1;
+  const T* ac3;
+  const T* G;
+  const T* H;
+  const T* ac2;  // forward factor (special rows)
+  const T* K;    // folded interior coefficients: deriv 2 x n, filter 6 x n
+  const T* KD;   // filter, correction form: 5 x n folded second-difference weights
+  const T* A;    // off-diagonal coefficient of each row (a = c)
+  int n;         // rows of the system
+  int first;     // grid node of row 0
+  int ntype;     // 3: periodic / inner block, 4: physical boundary at both ends
+  int dim;       // im, jm or km
 };
 
 // Filter right-hand-side tables (src/filter.F90:299-432).
+template <typename T>
 struct FTab {
-  double c10[6], c8[5], c6[4];
-  double cb[3][7];
-  double ch[3][11];
+  T c10[6], c8[5], c6[4];
+  T cb[3][7];
+  T ch[3][11];
 };
 
 struct Geo {
@@ -63,33 +71,49 @@ struct Geo {
   int ndims;
 };
 
-struct Dev {
-  double* q;        // 5 halo arrays
-  double* pr;       // 6 halo arrays: rho, u, v, w, p, T
-  const double* xd; // 3 halo arrays: dxi(1,1), dxi(2,2), dxi(3,3)
-  const double* jac;// halo array
-  double* qrhs;     // 5 interior arrays
-  double* qsave;    // 5 interior arrays
-  double* grad;     // 12 interior arrays: dvel(n,m) at n+3m, dtmp(m) at 9+m
-  double* sig;      // 6 interior arrays
-  double* qf;       // 3 interior arrays
-  double* part;     // statistics partial sums, 2 per block
+template <typename T>
+struct DevT {
+  T* q;             // 5 halo arrays
+  T* pr;            // 6 halo arrays: rho, u, v, w, p, T
+  const T* xd;      // 3 halo arrays: dxi(1,1), dxi(2,2), dxi(3,3)
+  const T* jac;     // halo array
+  const double* jac64;   // halo array: J in FP64 (the RK3 base and update)
+  const double* rjac64;  // halo array: 1/J in FP64
+  T* qrhs;          // 5 interior arrays
+  double* qsave;    // 5 interior arrays (RK3 base, FP64 in both forms)
+  double* qm;       // 5 interior arrays: FP64 master of q (FP32 form only)
+  T* grad;          // 12 interior arrays: dvel(n,m) at n+3m, dtmp(m) at 9+m
+  T* sig;           // 6 interior arrays
+  T* qf;            // 3 interior arrays
+  double* part;     // statistics partial sums, 2 per warp
   int* flag;        // crash flag
 };
 
 struct Phys {
-  double const2, const5, const6;
-  double tempconst, tempconst1, reynolds, prandtl;
+  double const2, rconst6, hcc_scale;  // p/rho*const2 ; 1/const6 ; 1/(Pr*const5)
+  double tempconst, tempconst1, rreynolds;
   double dt;
   double rk1, rk2, rk3;
-  double dx[3];  // mini-app uniform spacings
-  int mini;      // 1: mini-app ordering and scalings
+  double rdx[3];  // mini-app reciprocal spacings
+  // the same constants rounded to FP32 once, for the FP32 sweeps
+  float f_const2, f_rconst6, f_hcc_scale, f_tempconst, f_tempconst1, f_rreynolds;
+  float f_rdx[3];
+  int mini;       // 1: mini-app ordering and scalings
 };
 
+// A physical constant in the sweep precision T.
+template <typename T>
+__device__ __forceinline__ T pc(double dv, float fv);
+template <>
+__device__ __forceinline__ double pc<double>(double dv, float) { return dv; }
+template <>
+__device__ __forceinline__ float pc<float>(double, float fv) { return fv; }
+
 // Everything a sweep launch needs besides its scheme.
+template <typename T>
 struct SweepCtx {
   Geo g;
-  Dev d;
+  DevT<T> d;
   Phys ph;
   cudaStream_t st;
 };
@@ -115,8 +139,8 @@ __device__ __forceinline__ void line_ijk(int a, int b, int l, int& i, int& j, in
   else { i = a; j = b; k = l; }
 }
 
-// Thread -> (line, chunk) mapping.  Returns false for threads past the last
-// line; those threads still take part in block-wide synchronisation.
+// Thread -> (line, chunk) mapping.  Threads past the last line still take
+// part in block-wide synchronisation (y/z); x-line warps past the end exit.
 template <int DIR>
 struct LineMap {
   int a, b, c;
@@ -143,43 +167,45 @@ struct LineMap {
 // ---------------------------------------------------------------------------
 // Carry scans across the 32 chunks of a line.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double scan_fwd_warp(double M, double L, int lane) {
+template <typename T>
+__device__ __forceinline__ T scan_fwd_warp(T M, T L, int lane) {
 #pragma unroll
   for (int off = 1; off < 32; off <<= 1) {
-    const double Mo = __shfl_up_sync(0xffffffffu, M, off);
-    const double Lo = __shfl_up_sync(0xffffffffu, L, off);
+    const T Mo = __shfl_up_sync(0xffffffffu, M, off);
+    const T Lo = __shfl_up_sync(0xffffffffu, L, off);
     if (lane >= off) {
       L = L + M * Lo;
       M = M * Mo;
     }
   }
-  const double prev = __shfl_up_sync(0xffffffffu, L, 1);
-  return lane == 0 ? 0.0 : prev;
+  const T prev = __shfl_up_sync(0xffffffffu, L, 1);
+  return lane == 0 ? T(0) : prev;
 }
 
-__device__ __forceinline__ double scan_bwd_warp(double M, double L, int lane) {
+template <typename T>
+__device__ __forceinline__ T scan_bwd_warp(T M, T L, int lane) {
 #pragma unroll
   for (int off = 1; off < 32; off <<= 1) {
-    const double Mo = __shfl_down_sync(0xffffffffu, M, off);
-    const double Lo = __shfl_down_sync(0xffffffffu, L, off);
+    const T Mo = __shfl_down_sync(0xffffffffu, M, off);
+    const T Lo = __shfl_down_sync(0xffffffffu, L, off);
     if (lane + off < 32) {
       L = L + M * Lo;
       M = M * Mo;
     }
   }
-  const double next = __shfl_down_sync(0xffffffffu, L, 1);
-  return lane == 31 ? 0.0 : next;
+  const T next = __shfl_down_sync(0xffffffffu, L, 1);
+  return lane == 31 ? T(0) : next;
 }
 
 constexpr int SM_PITCH = YZ_LINES + 1;
-constexpr int SCAN_SMEM_DOUBLES = 2 * NCH * SM_PITCH;
+constexpr int SCAN_SMEM_WORDS = 2 * NCH * SM_PITCH;
 
 // y/z sweeps: (M,L) of chunk c = threadIdx.y for line threadIdx.x.
 // Warp w scans line w with lane = chunk.
-template <bool FWD>
-__device__ __forceinline__ double scan_block(double M, double L, double* sm) {
-  double* sM = sm;
-  double* sL = sm + NCH * SM_PITCH;
+template <bool FWD, typename T>
+__device__ __forceinline__ T scan_block(T M, T L, T* sm) {
+  T* sM = sm;
+  T* sL = sm + NCH * SM_PITCH;
   const int tx = threadIdx.x, ty = threadIdx.y;
   sM[ty * SM_PITCH + tx] = M;
   sL[ty * SM_PITCH + tx] = L;
@@ -187,12 +213,12 @@ __device__ __forceinline__ double scan_block(double M, double L, double* sm) {
   const int tid = tx + YZ_LINES * ty;
   const int w = tid >> 5, lane = tid & 31;
   if (w < YZ_LINES) {
-    double m = sM[lane * SM_PITCH + w];
-    double l = sL[lane * SM_PITCH + w];
+    T m = sM[lane * SM_PITCH + w];
+    T l = sL[lane * SM_PITCH + w];
 #pragma unroll
     for (int off = 1; off < 32; off <<= 1) {
-      const double Mo = FWD ? __shfl_up_sync(0xffffffffu, m, off) : __shfl_down_sync(0xffffffffu, m, off);
-      const double Lo = FWD ? __shfl_up_sync(0xffffffffu, l, off) : __shfl_down_sync(0xffffffffu, l, off);
+      const T Mo = FWD ? __shfl_up_sync(0xffffffffu, m, off) : __shfl_down_sync(0xffffffffu, m, off);
+      const T Lo = FWD ? __shfl_up_sync(0xffffffffu, l, off) : __shfl_down_sync(0xffffffffu, l, off);
       const bool ok = FWD ? (lane >= off) : (lane + off < 32);
       if (ok) {
         l = l + m * Lo;
@@ -202,48 +228,47 @@ __device__ __forceinline__ double scan_block(double M, double L, double* sm) {
     sL[lane * SM_PITCH + w] = l;
   }
   __syncthreads();
-  double r;
-  if (FWD) r = ty == 0 ? 0.0 : sL[(ty - 1) * SM_PITCH + tx];
-  else r = ty == NCH - 1 ? 0.0 : sL[(ty + 1) * SM_PITCH + tx];
+  T r;
+  if (FWD) r = ty == 0 ? T(0) : sL[(ty - 1) * SM_PITCH + tx];
+  else r = ty == NCH - 1 ? T(0) : sL[(ty + 1) * SM_PITCH + tx];
   __syncthreads();
   return r;
 }
 
-// In: y[t] = right-hand side of row c*CH+t.  Out: y[t] = solution.
-template <int CH, int DIR>
-__device__ __forceinline__ void chunk_solve(double (&y)[CH], const DScheme& S, int c, double* sm) {
+// In: y[t] = ac2-scaled right-hand side of row c*CH+t (row 0 unscaled).
+// Out: y[t] = solution.
+template <int CH, int DIR, typename T>
+__device__ __forceinline__ void chunk_solve(T (&y)[CH], const DScheme<T>& S, int c, T* sm) {
   const int s = c * CH;
-  double L = 0.0, M = 1.0;
+  T L = T(0), M = T(1);
 #pragma unroll
   for (int t = 0; t < CH; ++t) {
     const int r = s + t;
     if (r < S.n) {
-      if (t == 0) {
-        if (r != 0) y[0] = y[0] * __ldg(S.ac2 + r);
-      } else {
-        y[t] = y[t] * __ldg(S.ac2 + r) - y[t - 1] * __ldg(S.ac3 + r);
-      }
+      if (t > 0) y[t] = y[t] - y[t - 1] * __ldg(S.ac3 + r);
       L = y[t];
       M = __ldg(S.G + r);
     }
   }
-  const double Yp = (DIR == 0) ? scan_fwd_warp(M, L, c) : scan_block<true>(M, L, sm);
+  const T Yp = (DIR == 0) ? scan_fwd_warp(M, L, c) : scan_block<true>(M, L, sm);
+  if (c > 0) {
 #pragma unroll
-  for (int t = 0; t < CH; ++t) {
-    const int r = s + t;
-    if (r < S.n) y[t] = y[t] + __ldg(S.G + r) * Yp;
+    for (int t = 0; t < CH; ++t) {
+      const int r = s + t;
+      if (r < S.n) y[t] = y[t] + __ldg(S.G + r) * Yp;
+    }
   }
 #pragma unroll
   for (int t = CH - 2; t >= 0; --t) {
     const int r = s + t;
     if (r < S.n - 1) y[t] = y[t] - __ldg(S.ac1 + r) * y[t + 1];
   }
-  double Lb = 0.0, Mb = 1.0;
+  T Lb = T(0), Mb = T(1);
   if (s < S.n) {
     Lb = y[0];
     Mb = __ldg(S.H + s);
   }
-  const double Xn = (DIR == 0) ? scan_bwd_warp(Mb, Lb, c) : scan_block<false>(Mb, Lb, sm);
+  const T Xn = (DIR == 0) ? scan_bwd_warp(Mb, Lb, c) : scan_block<false>(Mb, Lb, sm);
 #pragma unroll
   for (int t = 0; t < CH; ++t) {
     const int r = s + t;
@@ -252,188 +277,300 @@ __device__ __forceinline__ void chunk_solve(double (&y)[CH], const DScheme& S, i
 }
 
 // Right-hand side of the compact first derivative (compact_fd_rhs,
-// src/derivative.F90:210-306) for the rows of chunk c.  f(node) is
-// evaluated once per node into a window of radius 3.
-template <int CH, class Fetch>
-__device__ __forceinline__ void deriv_rhs(double (&y)[CH], const DScheme& S, int c, const Fetch& f) {
+// src/derivative.F90:210-306) for the rows of chunk c, scaled by ac2.
+// f(node) is evaluated once per node into a window of radius 3.
+template <int CH, typename T, class Fetch>
+__device__ __forceinline__ void deriv_rhs(T (&y)[CH], const DScheme<T>& S, int c, const Fetch& f) {
   const int s = c * CH;
   const int nb = S.first + s - 3;
   const int last = S.first + S.n - 1;
-  double w[CH + 6];
+  T w[CH + 6];
 #pragma unroll
   for (int t = 0; t < CH + 6; ++t) {
     const int nd = nb + t;
-    w[t] = (nd >= S.first - 3 && nd <= last + 3) ? f(nd) : 0.0;
+    w[t] = (nd >= S.first - 3 && nd <= last + 3) ? f(nd) : T(0);
   }
+  const T* K7 = S.K;
+  const T* K36 = S.K + S.n;
 #pragma unroll
   for (int t = 0; t < CH; ++t) {
     const int r = s + t;
-    const double* W = w + t + 3;
-    double d;
-    if (S.ntype == 4) {
-      if (r == 0) d = -2.5 * W[0] + 2.0 * W[1] + 0.5 * W[2];
-      else if (r == 1 || r == S.n - 2) d = 0.75 * (W[1] - W[-1]);
-      else if (r == S.n - 1) d = 2.5 * W[0] - 2.0 * W[-1] - 0.5 * W[-2];
-      else d = NUM7D9 * (W[1] - W[-1]) + NUM1D36 * (W[2] - W[-2]);
-    } else {
-      if (r == 0 || r == S.n - 1)
-        d = 0.75 * (W[1] - W[-1]) - 0.15 * (W[2] - W[-2]) + NUM1D60 * (W[3] - W[-3]);
-      else
-        d = NUM7D9 * (W[1] - W[-1]) + NUM1D36 * (W[2] - W[-2]);
+    const T* W = w + t + 3;
+    T d = T(0);
+    if (r < S.n) {
+      const bool special = S.ntype == 4 ? (r <= 1 || r >= S.n - 2) : (r == 0 || r == S.n - 1);
+      if (!special) {
+        d = __ldg(K7 + r) * (W[1] - W[-1]) + __ldg(K36 + r) * (W[2] - W[-2]);
+      } else {
+        if (S.ntype == 4) {
+          if (r == 0) d = T(-2.5) * W[0] + T(2.0) * W[1] + T(0.5) * W[2];
+          else if (r == S.n - 1) d = T(2.5) * W[0] - T(2.0) * W[-1] - T(0.5) * W[-2];
+          else d = T(0.75) * (W[1] - W[-1]);
+        } else {
+          d = T(0.75) * (W[1] - W[-1]) - T(0.15) * (W[2] - W[-2]) + T(1.0 / 60.0) * (W[3] - W[-3]);
+        }
+        if (r > 0) d = d * __ldg(S.ac2 + r);
+      }
     }
-    y[t] = (r < S.n) ? d : 0.0;
+    y[t] = d;
   }
 }
 
-template <class Fetch>
-__device__ __forceinline__ double filt_c10(const FTab& T, const Fetch& f, int j) {
-  const double v0 = f(j) + f(j), v1 = f(j + 1) + f(j - 1), v2 = f(j + 2) + f(j - 2);
-  const double v3 = f(j + 3) + f(j - 3), v4 = f(j + 4) + f(j - 4), v5 = f(j + 5) + f(j - 5);
-  return T.c10[0] * v0 + T.c10[1] * v1 + T.c10[2] * v2 + T.c10[3] * v3 + T.c10[4] * v4 +
-         T.c10[5] * v5;
+template <typename T, class Fetch>
+__device__ __forceinline__ T filt_c8(const FTab<T>& Tb, const Fetch& f, int j) {
+  const T v0 = f(j) + f(j), v1 = f(j + 1) + f(j - 1), v2 = f(j + 2) + f(j - 2);
+  const T v3 = f(j + 3) + f(j - 3), v4 = f(j + 4) + f(j - 4);
+  return Tb.c8[0] * v0 + Tb.c8[1] * v1 + Tb.c8[2] * v2 + Tb.c8[3] * v3 + Tb.c8[4] * v4;
 }
-template <class Fetch>
-__device__ __forceinline__ double filt_c8(const FTab& T, const Fetch& f, int j) {
-  const double v0 = f(j) + f(j), v1 = f(j + 1) + f(j - 1), v2 = f(j + 2) + f(j - 2);
-  const double v3 = f(j + 3) + f(j - 3), v4 = f(j + 4) + f(j - 4);
-  return T.c8[0] * v0 + T.c8[1] * v1 + T.c8[2] * v2 + T.c8[3] * v3 + T.c8[4] * v4;
-}
-template <class Fetch>
-__device__ __forceinline__ double filt_c6(const FTab& T, const Fetch& f, int j) {
-  const double v0 = f(j) + f(j), v1 = f(j + 1) + f(j - 1), v2 = f(j + 2) + f(j - 2);
-  const double v3 = f(j + 3) + f(j - 3);
-  return T.c6[0] * v0 + T.c6[1] * v1 + T.c6[2] * v2 + T.c6[3] * v3;
+template <typename T, class Fetch>
+__device__ __forceinline__ T filt_c6(const FTab<T>& Tb, const Fetch& f, int j) {
+  const T v0 = f(j) + f(j), v1 = f(j + 1) + f(j - 1), v2 = f(j + 2) + f(j - 2);
+  const T v3 = f(j + 3) + f(j - 3);
+  return Tb.c6[0] * v0 + Tb.c6[1] * v1 + Tb.c6[2] * v2 + Tb.c6[3] * v3;
 }
 
 // Boundary and end rows of the compact filter (compact_filter_rhs,
-// src/filter.F90:176-269).  Out of line: only the first and last chunk of a
-// line reach it.  v + base is node 0 of the line, hs the node stride.
-static __device__ __noinline__ double filter_special_row(const DScheme& S, const FTab& T, int r,
-                                                  const double* v, long long base, long long hs,
-                                                  int per) {
+// src/filter.F90:176-269), scaled by ac2.  Out of line: only the first and
+// last chunk of a line reach it.  v + base is node 0, hs the node stride.
+// The row is evaluated on f - shift (shift = 0 is the reference's row).
+template <typename T>
+__device__ __noinline__ T filter_special_row(const DScheme<T>& S, const FTab<T>& Tb, int r,
+                                             const T* v, long long base, long long hs, int per,
+                                             T shift = T(0)) {
   const int dim = S.dim;
-  auto f = [&](int node) -> double {
+  auto f = [&](int node) -> T {
     int nd = node;
     if (per) nd = nd < 0 ? nd + dim : (nd > dim ? nd - dim : nd);
-    return v[base + hs * nd];
+    return v[base + hs * nd] - shift;
   };
   const int last = S.first + S.n - 1;
   const int j = S.first + r;
-  double d = 0.0;
+  T d = T(0);
   if (S.ntype == 4) {
     if (r <= 2) {
-      for (int m = 0; m <= 6; ++m) d = d + T.cb[r][m] * f(m);
+      for (int m = 0; m <= 6; ++m) d = d + Tb.cb[r][m] * f(m);
     } else if (r >= S.n - 3) {
       const int kk = S.n - 1 - r;
-      for (int m = 0; m <= 6; ++m) d = d + T.cb[kk][m] * f(last - m);
+      for (int m = 0; m <= 6; ++m) d = d + Tb.cb[kk][m] * f(last - m);
     } else if (r == 3 || r == S.n - 4) {
-      d = filt_c6(T, f, j);
+      d = filt_c6(Tb, f, j);
     } else {
-      d = filt_c8(T, f, j);
+      d = filt_c8(Tb, f, j);
     }
   } else {
     if (r <= 2) {
-      for (int m = 0; m <= 10; ++m) d = d + T.ch[r][m] * f(S.first - 2 + m);
+      for (int m = 0; m <= 10; ++m) d = d + Tb.ch[r][m] * f(S.first - 2 + m);
     } else {
       const int kk = S.n - 1 - r;
-      for (int m = 0; m <= 10; ++m) d = d + T.ch[kk][m] * f(last + 2 - m);
+      for (int m = 0; m <= 10; ++m) d = d + Tb.ch[kk][m] * f(last + 2 - m);
     }
   }
-  return d;
+  return r > 0 ? d * S.ac2[r] : d;
 }
 
 // Right-hand side of the compact filter (compact_filter_rhs,
-// src/filter.F90:156-285) for the rows of chunk c.
-template <int CH>
-__device__ __forceinline__ void filter_rhs(double (&y)[CH], const DScheme& S, const FTab& T, int c,
-                                           const double* v, long long base, long long hs, int per) {
+// src/filter.F90:156-285) for the rows of chunk c, scaled by ac2.  The
+// interior stencil uses FK[m] = c10i(m) * ac2 with the centre weight doubled
+// (the reference's f+f, exact).
+template <int CH, typename T>
+__device__ __forceinline__ void filter_rhs(T (&y)[CH], const DScheme<T>& S, const FTab<T>& Tb,
+                                           int c, const T* v, long long base, long long hs,
+                                           int per) {
   const int s = c * CH;
   const int dim = S.dim;
-  auto f = [&](int node) -> double {
+  auto f = [&](int node) -> T {
     int nd = node;
     if (per) nd = nd < 0 ? nd + dim : (nd > dim ? nd - dim : nd);
     return v[base + hs * nd];
   };
+  const T* FK = S.K;
+  const int n = S.n;
 #pragma unroll
   for (int t = 0; t < CH; ++t) {
     const int r = s + t;
-    double d = 0.0;
-    if (r < S.n) {
-      const bool special = S.ntype == 4 ? (r <= 4 || r >= S.n - 5) : (r <= 2 || r >= S.n - 3);
-      if (special) d = filter_special_row(S, T, r, v, base, hs, per);
-      else d = filt_c10(T, f, S.first + r);
+    T d = T(0);
+    if (r < n) {
+      const bool special = S.ntype == 4 ? (r <= 4 || r >= n - 5) : (r <= 2 || r >= n - 3);
+      if (special) {
+        d = filter_special_row(S, Tb, r, v, base, hs, per);
+      } else {
+        const int j = S.first + r;
+        d = __ldg(FK + r) * f(j) + __ldg(FK + n + r) * (f(j + 1) + f(j - 1)) +
+            __ldg(FK + 2 * n + r) * (f(j + 2) + f(j - 2)) +
+            __ldg(FK + 3 * n + r) * (f(j + 3) + f(j - 3)) +
+            __ldg(FK + 4 * n + r) * (f(j + 4) + f(j - 4)) +
+            __ldg(FK + 5 * n + r) * (f(j + 5) + f(j - 5));
+      }
+    }
+    y[t] = d;
+  }
+}
+
+// Correction form of the compact filter for the FP32 sweeps: the increment
+// delta = A^{-1} (B - A) f.  B - A annihilates constants, so on interior rows
+// (B - A) f is a sum of second differences f(j+k) + f(j-k) - 2 f(j), k = 1..5,
+// with weights c10i(1) - alpha, c10i(2..5) (folded with ac2 in KD).  Their
+// rounding scales with the variation of f, not its mean, which is what keeps
+// the FP32 error of the filter small next to the field.  Every boundary and
+// end row preserves constants as well (each B row sums to its A row: 1 + 2
+// alpha, or 1 + beta on an end row), so those rows are evaluated on f - f(j)
+// and the diagonal term drops out.
+template <typename T>
+__device__ __noinline__ T filter_special_delta(const DScheme<T>& S, const FTab<T>& Tb, int r,
+                                               const T* v, long long base, long long hs,
+                                               int per) {
+  const int dim = S.dim;
+  auto f = [&](int node) -> T {
+    int nd = node;
+    if (per) nd = nd < 0 ? nd + dim : (nd > dim ? nd - dim : nd);
+    return v[base + hs * nd];
+  };
+  const int j = S.first + r;
+  const T f0 = f(j);
+  const T sc = r > 0 ? S.ac2[r] : T(1);
+  const T d = filter_special_row(S, Tb, r, v, base, hs, per, f0);  // already * ac2
+  const T a = S.A[r];
+  T af = T(0);
+  if (r > 0) af = af + a * (f(j - 1) - f0);
+  if (r < S.n - 1) af = af + a * (f(j + 1) - f0);
+  return d - af * sc;
+}
+
+template <int CH, typename T>
+__device__ __forceinline__ void filter_rhs_delta(T (&y)[CH], const DScheme<T>& S,
+                                                 const FTab<T>& Tb, int c, const T* v,
+                                                 long long base, long long hs, int per) {
+  const int s = c * CH;
+  const int dim = S.dim;
+  auto f = [&](int node) -> T {
+    int nd = node;
+    if (per) nd = nd < 0 ? nd + dim : (nd > dim ? nd - dim : nd);
+    return v[base + hs * nd];
+  };
+  const T* KD = S.KD;
+  const int n = S.n;
+#pragma unroll
+  for (int t = 0; t < CH; ++t) {
+    const int r = s + t;
+    T d = T(0);
+    if (r < n) {
+      const bool special = S.ntype == 4 ? (r <= 4 || r >= n - 5) : (r <= 2 || r >= n - 3);
+      if (special) {
+        d = filter_special_delta(S, Tb, r, v, base, hs, per);
+      } else {
+        const int j = S.first + r;
+        const T f0 = f(j);
+        d = __ldg(KD + r) * ((f(j + 1) - f0) + (f(j - 1) - f0)) +
+            __ldg(KD + n + r) * ((f(j + 2) - f0) + (f(j - 2) - f0)) +
+            __ldg(KD + 2 * n + r) * ((f(j + 3) - f0) + (f(j - 3) - f0)) +
+            __ldg(KD + 3 * n + r) * ((f(j + 4) - f0) + (f(j - 4) - f0)) +
+            __ldg(KD + 4 * n + r) * ((f(j + 5) - f0) + (f(j - 5) - f0));
+      }
     }
     y[t] = d;
   }
 }
 
 // q2fvar (src/fludyna.F90:545-634): conserved -> primitives at one point.
-__device__ __forceinline__ void q2fvar_pt(const Phys& ph, double q1, double q2, double q3, double q4,
-                                          double q5, double& ro, double& u, double& v, double& w,
-                                          double& p, double& T) {
+// The divisions by rho and const6 are multiplications by reciprocals.
+template <typename T>
+__device__ __forceinline__ void q2fvar_pt(const Phys& ph, T q1, T q2, T q3, T q4, T q5, T& ro,
+                                          T& u, T& v, T& w, T& p, T& tt) {
   ro = q1;
-  u = q2 / ro;
-  v = q3 / ro;
-  w = q4 / ro;
-  p = (q5 - 0.5 * ro * (u * u + v * v + w * w)) / ph.const6;
-  T = p / ro * ph.const2;
+  const T rr = T(1) / ro;
+  u = q2 * rr;
+  v = q3 * rr;
+  w = q4 * rr;
+  p = (q5 - T(0.5) * ro * (u * u + v * v + w * w)) * pc<T>(ph.rconst6, ph.f_rconst6);
+  tt = p * rr * pc<T>(ph.const2, ph.f_const2);
 }
 
-__device__ __forceinline__ void q2fvar_store(const Geo& g, const Dev& d, const Phys& ph, long long p) {
+template <typename T>
+__device__ __forceinline__ void q2fvar_store(const Geo& g, const DevT<T>& d, const Phys& ph,
+                                             long long p) {
   const long long nh = g.nh;
-  double ro, u, v, w, pp, T;
-  q2fvar_pt(ph, d.q[p], d.q[p + nh], d.q[p + 2 * nh], d.q[p + 3 * nh], d.q[p + 4 * nh], ro, u, v, w,
-            pp, T);
+  T ro, u, v, w, pp, tt;
+  q2fvar_pt<T>(ph, d.q[p], d.q[p + nh], d.q[p + 2 * nh], d.q[p + 3 * nh], d.q[p + 4 * nh], ro, u,
+               v, w, pp, tt);
   d.pr[p] = ro;
   d.pr[p + nh] = u;
   d.pr[p + 2 * nh] = v;
   d.pr[p + 3 * nh] = w;
   d.pr[p + 4 * nh] = pp;
-  d.pr[p + 5 * nh] = T;
-  if (!(ro > 0.0)) atomicOr(d.flag, 1);
+  d.pr[p + 5 * nh] = tt;
+  if (!(ro > T(0))) atomicOr(d.flag, 1);
 }
 
 struct CGFlags {
   int conv, grad, first, last, sigma, stats, qsave;
 };
 
-__device__ __forceinline__ void sigma_point(const Geo& g, const Dev& d, const Phys& ph, long long z,
-                                            long long h) {
-  const long long n0 = g.n0, nh = g.nh;
-  const double* G = d.grad + z;
-  const double T = d.pr[h + 5 * nh];
-  // miucal (src/fludyna.F90:791-820) / reynolds
-  const double miu = T * sqrt(T) * ph.tempconst1 / (T + ph.tempconst) / ph.reynolds;
-  const double s11 = G[0];
-  const double s12 = 0.5 * (G[3 * n0] + G[1 * n0]);
-  const double s13 = 0.5 * (G[6 * n0] + G[2 * n0]);
-  const double s22 = G[4 * n0];
-  const double s23 = 0.5 * (G[7 * n0] + G[5 * n0]);
-  const double s33 = G[8 * n0];
-  const double skk = NUM1D3 * (s11 + s22 + s33);
-  const double miu2 = 2.0 * miu;
-  const double hcc = (miu / ph.prandtl) / ph.const5;
-  const double S1 = miu2 * (s11 - skk), S2 = miu2 * s12, S3 = miu2 * s13;
-  const double S4 = miu2 * (s22 - skk), S5 = miu2 * s23, S6 = miu2 * (s33 - skk);
-  const double u = d.pr[h + nh], v = d.pr[h + 2 * nh], w = d.pr[h + 3 * nh];
-  double* Sg = d.sig + z;
-  Sg[0] = S1; Sg[n0] = S2; Sg[2 * n0] = S3; Sg[3 * n0] = S4; Sg[4 * n0] = S5; Sg[5 * n0] = S6;
-  double* Q = d.qf + z;
-  Q[0] = hcc * G[9 * n0] + S1 * u + S2 * v + S3 * w;
-  Q[n0] = hcc * G[10 * n0] + S2 * u + S4 * v + S5 * w;
-  Q[2 * n0] = hcc * G[11 * n0] + S3 * u + S5 * v + S6 * w;
-}
-
 struct VFlags {
   int last;  // fuse the RK3 update of all five variables
   int q2f;   // and recover the primitives (main ordering)
 };
 
-__device__ __forceinline__ double rk_combine(const Phys& ph, double qs, double qv, double J,
-                                             double rhs) {
-  if (ph.mini) return ph.rk1 * qs + ph.rk2 * qv + ph.rk3 * rhs * ph.dt;
-  const double v = ph.rk1 * qs + ph.rk2 * qv * J + ph.rk3 * rhs * ph.dt;
-  return v / J;
+// Viscous stress and heat flux at one interior point (diffrsdcal6,
+// src/solver.F90:2433-2545), miucal (src/fludyna.F90:791-820).
+template <typename T>
+__device__ __forceinline__ void sigma_point(const Geo& g, const DevT<T>& d, const Phys& ph,
+                                            long long z, long long h) {
+  const long long n0 = g.n0, nh = g.nh;
+  const T* G = d.grad + z;
+  const T tt = d.pr[h + 5 * nh];
+  const T miu = tt * sqrt(tt) * pc<T>(ph.tempconst1, ph.f_tempconst1) /
+                (tt + pc<T>(ph.tempconst, ph.f_tempconst)) * pc<T>(ph.rreynolds, ph.f_rreynolds);
+  const T s11 = G[0];
+  const T s12 = T(0.5) * (G[3 * n0] + G[1 * n0]);
+  const T s13 = T(0.5) * (G[6 * n0] + G[2 * n0]);
+  const T s22 = G[4 * n0];
+  const T s23 = T(0.5) * (G[7 * n0] + G[5 * n0]);
+  const T s33 = G[8 * n0];
+  const T skk = T(1.0 / 3.0) * (s11 + s22 + s33);
+  const T miu2 = T(2) * miu;
+  const T hcc = miu * pc<T>(ph.hcc_scale, ph.f_hcc_scale);
+  const T S1 = miu2 * (s11 - skk), S2 = miu2 * s12, S3 = miu2 * s13;
+  const T S4 = miu2 * (s22 - skk), S5 = miu2 * s23, S6 = miu2 * (s33 - skk);
+  const T u = d.pr[h + nh], v = d.pr[h + 2 * nh], w = d.pr[h + 3 * nh];
+  T* Sg = d.sig + z;
+  Sg[0] = S1; Sg[n0] = S2; Sg[2 * n0] = S3; Sg[3 * n0] = S4; Sg[4 * n0] = S5; Sg[5 * n0] = S6;
+  T* Q = d.qf + z;
+  Q[0] = hcc * G[9 * n0] + S1 * u + S2 * v + S3 * w;
+  Q[n0] = hcc * G[10 * n0] + S2 * u + S4 * v + S5 * w;
+  Q[2 * n0] = hcc * G[11 * n0] + S3 * u + S5 * v + S6 * w;
+}
+
+// The conserved value q at an interior point with FP64 accuracy: the FP64
+// form reads it; the FP32-storage form adds to the FP64 master every change
+// the FP32 copy received since the last RK3 update (filter, interface
+// averaging).
+__device__ __forceinline__ double q64(const DevT<double>& d, long long p, long long z, int m,
+                                      long long nh, long long n0) {
+  (void)z; (void)n0;
+  return d.q[m * nh + p];
+}
+__device__ __forceinline__ double q64(const DevT<float>& d, long long p, long long z, int m,
+                                      long long nh, long long n0) {
+  const double master = d.qm[m * n0 + z];
+  const float inc = d.q[m * nh + p] - __double2float_rn(master);
+  return master + (double)inc;
+}
+
+// RK3 stage update (src/mainloop.F90:441-451) of variable m at one point.
+// Main ordering: q = (rk1*qsave + rk2*q*J + rk3*dt*rhs)/J, the division a
+// multiplication by the stored 1/J; mini-app ordering: no Jacobian.
+template <typename T>
+__device__ __forceinline__ void rk_update(const Geo& g, const DevT<T>& d, const Phys& ph,
+                                          long long p, long long z, int m, double rhs) {
+  const long long nh = g.nh, n0 = g.n0;
+  const double J = d.jac64[p], rj = d.rjac64[p];
+  const double qv = q64(d, p, z, m, nh, n0);
+  const double qs = d.qsave[m * n0 + z];
+  double v;
+  if (ph.mini) v = ph.rk1 * qs + ph.rk2 * qv + ph.rk3 * rhs * ph.dt;
+  else v = (ph.rk1 * qs + ph.rk2 * qv * J + ph.rk3 * rhs * ph.dt) * rj;
+  d.q[m * nh + p] = (T)v;
+  if (d.qm) d.qm[m * n0 + z] = v;
 }
 
 }  // namespace astr

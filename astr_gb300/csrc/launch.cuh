@@ -1,5 +1,5 @@
 // Host-side view of the line-sweep launchers (definitions in sweeps.cuh,
-// instantiated per direction in sweep_x.cu, sweep_y.cu, sweep_z.cu).
+// instantiated per direction and precision in the sweep_*.cu units).
 #pragma once
 
 #include "astr_kernels.cuh"
@@ -19,21 +19,26 @@ inline dim3 sweep_grid(const Geo& g) {
   return dim3(gx, DIR == 1 ? g.km + 1 : g.jm + 1);
 }
 
-template <int DIR>
-cudaError_t launch_filter(const SweepCtx& c, const DScheme& S, const FTab& T, int CH, int do_q2f);
-template <int DIR>
-cudaError_t launch_convgrad(const SweepCtx& c, const DScheme& S, int CH, CGFlags f);
-template <int DIR>
-cudaError_t launch_visc(const SweepCtx& c, const DScheme& S, int CH, VFlags f);
+template <typename T, int DIR>
+cudaError_t launch_filter(const SweepCtx<T>& c, const DScheme<T>& S, const FTab<T>& Tb, int CH,
+                          int do_q2f);
+template <typename T, int DIR>
+cudaError_t launch_convgrad(const SweepCtx<T>& c, const DScheme<T>& S, int CH, CGFlags f);
+template <typename T, int DIR>
+cudaError_t launch_visc(const SweepCtx<T>& c, const DScheme<T>& S, int CH, VFlags f);
 
-extern template cudaError_t launch_filter<0>(const SweepCtx&, const DScheme&, const FTab&, int, int);
-extern template cudaError_t launch_filter<1>(const SweepCtx&, const DScheme&, const FTab&, int, int);
-extern template cudaError_t launch_filter<2>(const SweepCtx&, const DScheme&, const FTab&, int, int);
-extern template cudaError_t launch_convgrad<0>(const SweepCtx&, const DScheme&, int, CGFlags);
-extern template cudaError_t launch_convgrad<1>(const SweepCtx&, const DScheme&, int, CGFlags);
-extern template cudaError_t launch_convgrad<2>(const SweepCtx&, const DScheme&, int, CGFlags);
-extern template cudaError_t launch_visc<0>(const SweepCtx&, const DScheme&, int, VFlags);
-extern template cudaError_t launch_visc<1>(const SweepCtx&, const DScheme&, int, VFlags);
-extern template cudaError_t launch_visc<2>(const SweepCtx&, const DScheme&, int, VFlags);
+#define ASTR_DECLARE_SWEEPS(T, DIR)                                                                \
+  extern template cudaError_t launch_filter<T, DIR>(const SweepCtx<T>&, const DScheme<T>&,         \
+                                                    const FTab<T>&, int, int);                    \
+  extern template cudaError_t launch_convgrad<T, DIR>(const SweepCtx<T>&, const DScheme<T>&, int,  \
+                                                      CGFlags);                                   \
+  extern template cudaError_t launch_visc<T, DIR>(const SweepCtx<T>&, const DScheme<T>&, int, VFlags);
+
+ASTR_DECLARE_SWEEPS(double, 0)
+ASTR_DECLARE_SWEEPS(double, 1)
+ASTR_DECLARE_SWEEPS(double, 2)
+ASTR_DECLARE_SWEEPS(float, 0)
+ASTR_DECLARE_SWEEPS(float, 1)
+ASTR_DECLARE_SWEEPS(float, 2)
 
 }  // namespace astr

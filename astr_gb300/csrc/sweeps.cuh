@@ -1,36 +1,50 @@
 // Line-sweep kernels (filter, convective + gradient, viscous) and their
-// launchers.  Included once per sweep direction by sweep_x.cu, sweep_y.cu and
-// sweep_z.cu so the three directions compile in parallel.
+// launchers.  Included once per sweep direction and precision by the
+// sweep_*.cu translation units so they compile in parallel.
 #pragma once
 
 #include "launch.cuh"
 
 namespace astr {
 
-// ---------------------------------------------------------------------------
-// Sweep kernels
-// ---------------------------------------------------------------------------
 template <int DIR>
 constexpr int block_threads() { return DIR == 0 ? NCH * X_LINES : NCH * YZ_LINES; }
 
-// filterq (src/comsolver.F90:514-632): one direction, all five variables.
-template <int DIR, int CH>
+// filterq (src/comsolver.F90:514-632): one direction, all five variables,
+// in place.  do_q2f (mini-app ordering, last direction): recover the
+// primitives of the filtered state.
+template <typename T, int DIR, int CH>
 __global__ void __launch_bounds__(block_threads<DIR>())
-k_filter(Geo g, Dev d, DScheme S, FTab T, Phys ph, int do_q2f) {
-  __shared__ double sm[SCAN_SMEM_DOUBLES];
+k_filter(Geo g, DevT<T> d, DScheme<T> S, FTab<T> Tb, Phys ph, int do_q2f) {
+  __shared__ T sm[SCAN_SMEM_WORDS];
   LineMap<DIR> lm(g);
   if (DIR == 0 && !lm.active) return;  // whole warp: x-lines own a warp
   const long long hs = hstride<DIR>(g);
   int i0, j0, k0;
   line_ijk<DIR>(lm.a, lm.b, 0, i0, j0, k0);
   const long long base = hidx(g, i0, j0, k0);
+  const long long bz = zidx(g, i0, j0, k0), zs = zstride<DIR>(g);
   const int dim = S.dim;
-  const bool per = g.per[DIR] != 0;
+  const int per = g.per[DIR] ? 1 : 0;
 #pragma unroll 1
   for (int n = 0; n < 5; ++n) {
-    double* v = d.q + n * g.nh;
-    double y[CH];
-    filter_rhs<CH>(y, S, T, lm.c, v, base, hs, per ? 1 : 0);
+    T* v = d.q + n * g.nh;
+    // FP64: the reference's form, x = A^{-1} B f.  FP32: the increment
+    // form, x = f + A^{-1} (B - A) f (see filter_rhs_delta), with the
+    // increment added to the FP64 master so that none of it is lost below
+    // the FP32 spacing of f.
+    constexpr bool delta = sizeof(T) == 4;
+    T y[CH];
+    if (delta) filter_rhs_delta<CH>(y, S, Tb, lm.c, v, base, hs, per);
+    else filter_rhs<CH>(y, S, Tb, lm.c, v, base, hs, per);
+    T fv[CH];
+    if (delta) {
+#pragma unroll
+      for (int t = 0; t < CH; ++t) {
+        const int node = S.first + lm.c * CH + t;
+        fv[t] = (node >= 0 && node <= dim) ? v[base + hs * node] : T(0);
+      }
+    }
     chunk_solve<CH, DIR>(y, S, lm.c, sm);
     if (DIR == 0) __syncwarp();
     if (lm.active) {
@@ -39,7 +53,16 @@ k_filter(Geo g, Dev d, DScheme S, FTab T, Phys ph, int do_q2f) {
         const int r = lm.c * CH + t;
         const int node = S.first + r;
         const bool keep_end = S.ntype == 4 && (node == 0 || node == dim);
-        if (r < S.n && node >= 0 && node <= dim && !keep_end) v[base + hs * node] = y[t];
+        if (r < S.n && node >= 0 && node <= dim && !keep_end) {
+          if (delta && d.qm) {
+            double* M = d.qm + n * g.n0 + bz + zs * node;
+            const double nv = *M + (double)y[t];
+            *M = nv;
+            v[base + hs * node] = (T)nv;
+          } else {
+            v[base + hs * node] = delta ? fv[t] + y[t] : y[t];
+          }
+        }
       }
     }
   }
@@ -53,11 +76,11 @@ k_filter(Geo g, Dev d, DScheme S, FTab T, Phys ph, int do_q2f) {
 }
 
 // convrsdcal6 (src/solver.F90:2173-2341) and gradcal
-// (src/comsolver.F90:244-497), one direction.
-template <int DIR, int CH>
+// (src/comsolver.F90:244-497), one direction, diagonal metrics.
+template <typename T, int DIR, int CH>
 __global__ void __launch_bounds__(block_threads<DIR>())
-k_convgrad(Geo g, Dev d, DScheme S, Phys ph, CGFlags fl) {
-  __shared__ double sm[SCAN_SMEM_DOUBLES];
+k_convgrad(Geo g, DevT<T> d, DScheme<T> S, Phys ph, CGFlags fl) {
+  __shared__ T sm[SCAN_SMEM_WORDS];
   LineMap<DIR> lm(g);
   if (DIR == 0 && !lm.active) {  // whole warp: x-lines own a warp
     if (fl.stats && threadIdx.x == 0) {
@@ -78,32 +101,32 @@ k_convgrad(Geo g, Dev d, DScheme S, Phys ph, CGFlags fl) {
   // transverse ranges of convrsdcal6 (js..je, ks..ke etc.)
   const int ta = DIR == 0 ? 1 : 0, tb = DIR == 2 ? 1 : 2;
   const bool cline = lm.a >= g.lo[ta] && lm.a <= g.hi[ta] && lm.b >= g.lo[tb] && lm.b <= g.hi[tb];
-  const double rdx = ph.dx[DIR];
-  const double* xd = d.xd + DIR * nh;
+  const T rdx = pc<T>(ph.rdx[DIR], ph.f_rdx[DIR]);
+  const T* xd = d.xd + DIR * nh;
 
   if (fl.conv) {
 #pragma unroll 1
     for (int n = 0; n < 5; ++n) {
-      auto f = [&](int node) -> double {
+      auto f = [&](int node) -> T {
         const long long p = bh + hs * node;
-        const double pp = d.pr[p + 4 * nh];
-        const double ud = d.pr[p + (1 + DIR) * nh];
-        const double qn = d.q[p + n * nh];
+        const T pp = d.pr[p + 4 * nh];
+        const T ud = d.pr[p + (1 + DIR) * nh];
+        const T qn = d.q[p + n * nh];
         if (ph.mini) {
-          const double uu = ud;
+          const T uu = ud;
           if (n == 4) return (qn + pp) * uu;
           if (n == 1 + DIR) return qn * uu + pp;
           return qn * uu;
         }
-        const double x = xd[p];
-        const double J = d.jac[p];
-        const double uu = x * ud;
+        const T x = xd[p];
+        const T J = d.jac[p];
+        const T uu = x * ud;
         if (n == 0) return J * qn * uu;
         if (n == 4) return J * (qn + pp) * uu;
         if (n == 1 + DIR) return J * (qn * uu + x * pp);
         return J * (qn * uu);
       };
-      double y[CH];
+      T y[CH];
       deriv_rhs<CH>(y, S, lm.c, f);
       chunk_solve<CH, DIR>(y, S, lm.c, sm);
       if (lm.active) {
@@ -111,10 +134,10 @@ k_convgrad(Geo g, Dev d, DScheme S, Phys ph, CGFlags fl) {
         for (int t = 0; t < CH; ++t) {
           const int node = S.first + lm.c * CH + t;
           if (node >= 0 && node <= dim) {
-            double* R = d.qrhs + n * n0 + bz + zs * node;
+            T* R = d.qrhs + n * n0 + bz + zs * node;
             const bool in = cline && node >= lo && node <= hi;
-            const double add = in ? (ph.mini ? y[t] / rdx : y[t]) : 0.0;
-            double val = fl.first ? add : (*R + add);
+            const T add = in ? (ph.mini ? y[t] * rdx : y[t]) : T(0);
+            T val = fl.first ? add : (*R + add);
             if (fl.last) val = -val;
             *R = val;
           }
@@ -125,9 +148,9 @@ k_convgrad(Geo g, Dev d, DScheme S, Phys ph, CGFlags fl) {
   if (fl.grad) {
 #pragma unroll 1
     for (int n = 0; n < 4; ++n) {
-      const double* src = d.pr + (n < 3 ? 1 + n : 5) * nh;
-      auto f = [&](int node) -> double { return src[bh + hs * node]; };
-      double y[CH];
+      const T* src = d.pr + (n < 3 ? 1 + n : 5) * nh;
+      auto f = [&](int node) -> T { return src[bh + hs * node]; };
+      T y[CH];
       deriv_rhs<CH>(y, S, lm.c, f);
       chunk_solve<CH, DIR>(y, S, lm.c, sm);
       const int comp = n < 3 ? n + 3 * DIR : 9 + DIR;
@@ -136,7 +159,7 @@ k_convgrad(Geo g, Dev d, DScheme S, Phys ph, CGFlags fl) {
         for (int t = 0; t < CH; ++t) {
           const int node = S.first + lm.c * CH + t;
           if (node >= 0 && node <= dim) {
-            const double gv = ph.mini ? y[t] / rdx : y[t] * xd[bh + hs * node];
+            const T gv = ph.mini ? y[t] * rdx : y[t] * xd[bh + hs * node];
             d.grad[comp * n0 + bz + zs * node] = gv;
           }
         }
@@ -144,14 +167,17 @@ k_convgrad(Geo g, Dev d, DScheme S, Phys ph, CGFlags fl) {
     }
   }
   if (fl.qsave && lm.active) {
+    // RK3 base at stage 1 (src/mainloop.F90:427-433): q*J (mini-app: q)
 #pragma unroll
     for (int t = 0; t < CH; ++t) {
       const int node = S.first + lm.c * CH + t;
       if (node >= 0 && node <= dim) {
         const long long p = bh + hs * node, z = bz + zs * node;
-        const double J = d.jac[p];
-        for (int m = 0; m < 5; ++m)
-          d.qsave[m * n0 + z] = ph.mini ? d.q[p + m * nh] : d.q[p + m * nh] * J;
+        const double J = d.jac64[p];
+        for (int m = 0; m < 5; ++m) {
+          const double qv = q64(d, p, z, m, nh, n0);
+          d.qsave[m * n0 + z] = ph.mini ? qv : qv * J;
+        }
       }
     }
   }
@@ -175,12 +201,12 @@ k_convgrad(Geo g, Dev d, DScheme S, Phys ph, CGFlags fl) {
           const long long p = bh + hs * node, z = bz + zs * node;
           const double ro = d.pr[p], u = d.pr[p + nh], v = d.pr[p + 2 * nh], w = d.pr[p + 3 * nh];
           ke += ro * (u * u + v * v + w * w);
-          const double* G = d.grad + z;
-          const double o3 = G[1 * n0] - G[3 * n0];
+          const T* G = d.grad + z;
+          const double o3 = (double)G[1 * n0] - (double)G[3 * n0];
           double om = o3 * o3;
           if (g.ndims == 3) {
-            const double o1 = G[5 * n0] - G[7 * n0];
-            const double o2 = G[6 * n0] - G[2 * n0];
+            const double o1 = (double)G[5 * n0] - (double)G[7 * n0];
+            const double o2 = (double)G[6 * n0] - (double)G[2 * n0];
             om = o1 * o1 + o2 * o2 + o3 * o3;
           }
           en += ro * om;
@@ -202,11 +228,12 @@ k_convgrad(Geo g, Dev d, DScheme S, Phys ph, CGFlags fl) {
   }
 }
 
-// diffrsdcal6 sweeps (src/solver.F90:2619-2852), one direction.
-template <int DIR, int CH>
+// diffrsdcal6 sweeps (src/solver.F90:2619-2852), one direction.  The last
+// direction applies the RK3 update (and, main ordering, q2fvar).
+template <typename T, int DIR, int CH>
 __global__ void __launch_bounds__(block_threads<DIR>())
-k_visc(Geo g, Dev d, DScheme S, Phys ph, VFlags fl) {
-  __shared__ double sm[SCAN_SMEM_DOUBLES];
+k_visc(Geo g, DevT<T> d, DScheme<T> S, Phys ph, VFlags fl) {
+  __shared__ T sm[SCAN_SMEM_WORDS];
   LineMap<DIR> lm(g);
   if (DIR == 0 && !lm.active) return;  // whole warp: x-lines own a warp
   const long long hs = hstride<DIR>(g), zs = zstride<DIR>(g);
@@ -218,25 +245,25 @@ k_visc(Geo g, Dev d, DScheme S, Phys ph, VFlags fl) {
   const long long nh = g.nh, n0 = g.n0;
   const int lo = g.lo[DIR], hi = g.hi[DIR];
   const bool per = g.per[DIR] != 0;
-  const double rdx = ph.dx[DIR];
-  const double* xd = d.xd + DIR * nh;
+  const T rdx = pc<T>(ph.rdx[DIR], ph.f_rdx[DIR]);
+  const T* xd = d.xd + DIR * nh;
   constexpr int s0 = DIR == 0 ? 0 : (DIR == 1 ? 1 : 2);
   constexpr int s1 = DIR == 0 ? 1 : (DIR == 1 ? 3 : 4);
   constexpr int s2 = DIR == 0 ? 2 : (DIR == 1 ? 4 : 5);
 #pragma unroll 1
   for (int n = 0; n < 4; ++n) {
     const int sc = n == 0 ? s0 : (n == 1 ? s1 : s2);
-    const double* src = n < 3 ? d.sig + sc * n0 : d.qf + DIR * n0;
-    auto f = [&](int node) -> double {
+    const T* src = n < 3 ? d.sig + sc * n0 : d.qf + DIR * n0;
+    auto f = [&](int node) -> T {
       int nd = node;
       if (per) nd = nd < 0 ? nd + dim : (nd > dim ? nd - dim : nd);
-      else if (nd < 0 || nd > dim) return 0.0;
-      const double sv = src[bz + zs * nd];
+      else if (nd < 0 || nd > dim) return T(0);
+      const T sv = src[bz + zs * nd];
       if (ph.mini) return sv;
       const long long p = bh + hs * node;
       return (sv * xd[p]) * d.jac[p];
     };
-    double y[CH];
+    T y[CH];
     deriv_rhs<CH>(y, S, lm.c, f);
     chunk_solve<CH, DIR>(y, S, lm.c, sm);
     if (lm.active) {
@@ -245,16 +272,11 @@ k_visc(Geo g, Dev d, DScheme S, Phys ph, VFlags fl) {
         const int node = S.first + lm.c * CH + t;
         if (node >= 0 && node <= dim) {
           const long long z = bz + zs * node;
-          double* R = d.qrhs + (n + 1) * n0 + z;
+          T* R = d.qrhs + (n + 1) * n0 + z;
           const bool in = node >= lo && node <= hi;
-          const double val = *R + (in ? (ph.mini ? y[t] / rdx : y[t]) : 0.0);
-          if (!fl.last) {
-            *R = val;
-          } else {
-            const long long p = bh + hs * node;
-            double* qp = d.q + (n + 1) * nh + p;
-            *qp = rk_combine(ph, d.qsave[(n + 1) * n0 + z], *qp, d.jac[p], val);
-          }
+          const T val = *R + (in ? (ph.mini ? y[t] * rdx : y[t]) : T(0));
+          if (!fl.last) *R = val;
+          else rk_update(g, d, ph, bh + hs * node, z, n + 1, (double)val);
         }
       }
     }
@@ -265,13 +287,12 @@ k_visc(Geo g, Dev d, DScheme S, Phys ph, VFlags fl) {
       const int node = S.first + lm.c * CH + t;
       if (node >= 0 && node <= dim) {
         const long long z = bz + zs * node, p = bh + hs * node;
-        d.q[p] = rk_combine(ph, d.qsave[z], d.q[p], d.jac[p], d.qrhs[z]);
+        rk_update(g, d, ph, p, z, 0, (double)d.qrhs[z]);
         if (fl.q2f) q2fvar_store(g, d, ph, p);
       }
     }
   }
 }
-
 
 #define ASTR_CH_SWITCH(CHV, EXPR)                           \
   switch (CHV) {                                            \
@@ -283,30 +304,32 @@ k_visc(Geo g, Dev d, DScheme S, Phys ph, VFlags fl) {
     default: return cudaErrorInvalidValue;                  \
   }
 
-template <int DIR>
-cudaError_t launch_filter(const SweepCtx& c, const DScheme& S, const FTab& T, int CH, int do_q2f) {
+template <typename T, int DIR>
+cudaError_t launch_filter(const SweepCtx<T>& c, const DScheme<T>& S, const FTab<T>& Tb, int CH,
+                          int do_q2f) {
   const dim3 gr = sweep_grid<DIR>(c.g), bl = sweep_block<DIR>();
-  ASTR_CH_SWITCH(CH, (k_filter<DIR, CHC><<<gr, bl, 0, c.st>>>(c.g, c.d, S, T, c.ph, do_q2f)));
+  ASTR_CH_SWITCH(CH, (k_filter<T, DIR, CHC><<<gr, bl, 0, c.st>>>(c.g, c.d, S, Tb, c.ph, do_q2f)));
   return cudaGetLastError();
 }
 
-template <int DIR>
-cudaError_t launch_convgrad(const SweepCtx& c, const DScheme& S, int CH, CGFlags f) {
+template <typename T, int DIR>
+cudaError_t launch_convgrad(const SweepCtx<T>& c, const DScheme<T>& S, int CH, CGFlags f) {
   const dim3 gr = sweep_grid<DIR>(c.g), bl = sweep_block<DIR>();
-  ASTR_CH_SWITCH(CH, (k_convgrad<DIR, CHC><<<gr, bl, 0, c.st>>>(c.g, c.d, S, c.ph, f)));
+  ASTR_CH_SWITCH(CH, (k_convgrad<T, DIR, CHC><<<gr, bl, 0, c.st>>>(c.g, c.d, S, c.ph, f)));
   return cudaGetLastError();
 }
 
-template <int DIR>
-cudaError_t launch_visc(const SweepCtx& c, const DScheme& S, int CH, VFlags f) {
+template <typename T, int DIR>
+cudaError_t launch_visc(const SweepCtx<T>& c, const DScheme<T>& S, int CH, VFlags f) {
   const dim3 gr = sweep_grid<DIR>(c.g), bl = sweep_block<DIR>();
-  ASTR_CH_SWITCH(CH, (k_visc<DIR, CHC><<<gr, bl, 0, c.st>>>(c.g, c.d, S, c.ph, f)));
+  ASTR_CH_SWITCH(CH, (k_visc<T, DIR, CHC><<<gr, bl, 0, c.st>>>(c.g, c.d, S, c.ph, f)));
   return cudaGetLastError();
 }
 
-#define ASTR_INSTANTIATE_SWEEPS(DIR)                                                            \
-  template cudaError_t launch_filter<DIR>(const SweepCtx&, const DScheme&, const FTab&, int, int); \
-  template cudaError_t launch_convgrad<DIR>(const SweepCtx&, const DScheme&, int, CGFlags);       \
-  template cudaError_t launch_visc<DIR>(const SweepCtx&, const DScheme&, int, VFlags);
+#define ASTR_INSTANTIATE_SWEEPS(T, DIR)                                                          \
+  template cudaError_t launch_filter<T, DIR>(const SweepCtx<T>&, const DScheme<T>&, const FTab<T>&, \
+                                             int, int);                                         \
+  template cudaError_t launch_convgrad<T, DIR>(const SweepCtx<T>&, const DScheme<T>&, int, CGFlags); \
+  template cudaError_t launch_visc<T, DIR>(const SweepCtx<T>&, const DScheme<T>&, int, VFlags);
 
 }  // namespace astr
