@@ -245,6 +245,27 @@ def refcal(mach, reynolds, prandtl=0.72, gamma=1.4):
     return c
 
 
+def cfl_deltat(st, dxi_diag, mach, cfl=0.5, im=None, jm=None, km=None):
+    """Time step at a given CFL number, as cflcal (src/commcal.F90:27-87)
+    measures it: CFL = dt * (Di + Dj + Dk), D the largest contravariant
+    velocity plus sound speed along each computational direction over the
+    interior nodes, sos = sqrt(T)/mach (nondimensional, src/fludyna.F90:
+    832-859).  Diagonal metrics: dxi_diag = (dxi11, dxi22, dxi33)."""
+    q = st["q"]
+    im = q.shape[0] - 2 * HM - 1 if im is None else im
+    jm = q.shape[1] - 2 * HM - 1 if jm is None else jm
+    km = q.shape[2] - 2 * HM - 1 if km is None else km
+    sl = (slice(HM, HM + im + 1), slice(HM, HM + jm + 1), slice(HM, HM + km + 1))
+    css = np.sqrt(st["tmp"][sl]) / mach
+    total = 0.0
+    for d in range(3 if km > 0 else 2):
+        x = np.asarray(dxi_diag[d])[sl]
+        ubar = x * st["vel"][sl + (d,)]
+        cs = css * np.abs(x)
+        total += max(0.0, float(np.max(ubar + cs)))
+    return cfl / total
+
+
 def tgv_state(im, jm, km, mach=0.1, x=None, y=None, z=None):
     """tgvini + updateq (src/initialisation.F90:621-691, src/fludyna.F90:
     254-300): halo-layout q, rho, vel, prs, tmp with interior nodes set."""

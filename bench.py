@@ -1,18 +1,27 @@
 """Benchmark of the RHS hot path: Mpts*RKstages/s on the 512^3 Taylor-Green
 vortex (ASTR main-solver ordering: compact 6th-order derivatives, 10th-order
-compact filter, RK3, FP64).
+compact filter, RK3), FP32-storage form against the plain FP64 form, at the
+measured error of the FP32-storage form.
 
 One JSON line on rank 0.  A "step" is one RK3 time step (three stages) over
 the whole 512^3 periodic box; value = unique points (512^3) * 3 stages *
-steps / device time.  Inputs are resident in HBM (about 50 GB, far larger
-than the 129 MB L2, so no flush is needed between steps).  e2e is the same
-metric through the C ABI with host buffers: every step uploads the full
-state from page-locked host memory, runs one RK3 step, and downloads q and
-the statistics.
+steps / device time of the FP32-storage form (fields stored and swept in
+FP32, RK3 base and master conserved state in FP64).  The plain FP64 form
+runs the same steps from the same initial state; "forms" carries both
+throughputs and "error_vs_fp64" the relative L2 / Linf difference of the
+two final states.  Inputs are resident in HBM (about 37 GB / 50 GB, far
+larger than the 129 MB L2, so no flush is needed between steps).  e2e is
+the headline form through the C ABI with host buffers: every step uploads
+the full FP64 state from page-locked host memory, runs one RK3 step, and
+downloads q and the statistics.
 
 --impl reference times the CPU restatement of the reference (oracle/, a
 C++ port of the Fortran routines; the Fortran itself cannot be built on
 this image) on all host cores, on bounded 128^3 samples of the same case.
+
+--history N instead runs both forms N steps with the kinetic-energy and
+enstrophy history sampled every step and prints their largest relative
+difference and the final-state error (the 200-step scale comparison).
 
 Multi-GPU: the path does not shard (single-rank numerics), so N GPUs run N
 independent replicas ("scaling": "weak").
@@ -33,7 +42,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-METRIC = "Mpts*RKstages/s (TGV 512^3, FP64)"
+METRIC = "Mpts*RKstages/s (TGV 512^3, FP32 storage / FP64 accumulate, at stated error vs FP64)"
 UNIT = "Mpts*stages/s"
 
 # Algorithmic work of the FP64 form per interior point per launch, from the
@@ -47,14 +56,52 @@ UNIT = "Mpts*stages/s"
 #         adds the RK3 update (40) and primitive recovery (14)
 FLOPS_PER_PT = {"filter": 110.0, "convgrad": 113.0, "convgrad_last": 161.0,
                 "visc": 52.0, "visc_last": 106.0}
-# Algorithmic DRAM bytes per interior point per launch (FP64 words * 8):
-#   filter: q 5 in, 5 out; convgrad x: q, u, v, w, p, T, dxi, J in; qrhs 5 +
-#   4 gradients out; y adds qrhs in; z adds 8 gradients in and sigma 6 +
-#   heat flux 3 out; visc x/y: 3 sigma + 1 heat flux + dxi + J + 4 qrhs in,
-#   4 out; visc z: 4 + dxi + J + qrhs 5 + qsave 5 + q 5 in, q 5 + 6
-#   primitives out.
-BYTES_PER_PT = {"filter": 80.0, "convgrad": (168.0 + 208.0 + 344.0) / 3.0,
-                "visc": (112.0 + 112.0 + 256.0) / 3.0}
+
+
+def bytes_per_pt(kind, d, stage1, f32):
+    """Algorithmic DRAM bytes per interior point of one launch: every array
+    element the kernel must read or write once.  w = storage word (8 or 4);
+    m = FP64 word of the RK3 base, the FP32 form's master state and 1/J.
+      filter: q 5 in, 5 out (FP32 form: + master 5 in, 5 out)
+      convgrad x: q 5, u v w p T, dxi, J in; qrhs 5 + 4 gradients out;
+        stage 1 adds the RK3 base: qsave 5 out (FP32 form: + master 5 and
+        an FP64 J in); y adds qrhs 5 in; z adds 8 gradients in, stress 6 +
+        heat flux 3 out, stage 1 adds rho for the statistics
+      visc x, y: stress 3 + heat flux 1, dxi, J, qrhs 4 in; qrhs 4 out
+      visc z: stress/heat 4, dxi, J, qrhs 5, q 5 in, qsave 5 and 1/J (FP64)
+        in; q 5 + primitives 6 out (FP32 form: + FP64 J, master 5 in, 5 out)
+    """
+    w = 4.0 if f32 else 8.0
+    m = 8.0
+    if kind == "filter":
+        return 10 * w + (10 * m if f32 else 0.0)
+    if kind == "convgrad":
+        b = [21 * w, 26 * w, 43 * w][d]
+        if stage1 and d == 0:
+            b += 5 * m + (6 * m if f32 else 0.0)
+        if stage1 and d == 2:
+            b += w
+        return b
+    if kind == "visc":
+        if d < 2:
+            return 14 * w
+        # the FP64 form's J is the array the fluxes read; the FP32 form reads
+        # an FP64 copy of J beside its FP32 one
+        return (4 + 1 + 1 + 5 + 5 + 5 + 6) * w + 6 * m + (11 * m if f32 else 0.0)
+    raise ValueError(kind)
+
+
+def class_work(kind, f32, launches, pts):
+    """Algorithmic bytes and flops of `launches` launches of one kernel class
+    over whole RK3 steps (3 directions x 3 stages per step)."""
+    per_step_b = sum(bytes_per_pt(kind, d, s == 0, f32) for s in range(3) for d in range(3))
+    if kind == "filter":
+        per_step_f = 9 * FLOPS_PER_PT["filter"]
+    elif kind == "convgrad":
+        per_step_f = 3 * (2 * FLOPS_PER_PT["convgrad"] + FLOPS_PER_PT["convgrad_last"])
+    else:
+        per_step_f = 3 * (2 * FLOPS_PER_PT["visc"] + FLOPS_PER_PT["visc_last"])
+    return per_step_b / 9.0 * pts * launches, per_step_f / 9.0 * pts * launches
 
 
 def env_int(name, default):
@@ -188,27 +235,98 @@ def run_reference(args, rank, world, dist):
     return 0
 
 
-def run_gpu(args, rank, world, dist):
-    from astr_gb300 import capi, cases
-    from astr_gb300.solver import GpuSolver
+CFL = 0.5
 
-    n = args.n
+
+def tgv_inputs(n):
+    """Grid metrics and initial state of the n^3 TGV, and the time step at
+    CFL 0.5 (cflcal's measure) on that grid."""
+    from astr_gb300 import cases
     L = 2.0 * np.pi
-    t0 = time.perf_counter()
     x, y, z = cases.gridcube(n, n, n, L, L, L)
     (d11, d22, d33), J = cases.rect_metrics(x, y, z, diag_only=True)
     st = cases.tgv_state(n, n, n, mach=0.1, x=x, y=y, z=z)
-    t_setup = time.perf_counter() - t0
+    st["deltat"] = cases.cfl_deltat(st, (d11, d22, d33), 0.1, CFL)
+    return (d11, d22, d33, J), st
 
-    g = GpuSolver(n, n, n, order=capi.ORDER_MAIN, precision=capi.FP64, mach=0.1,
-                  reynolds=1600.0, deltat=1e-3)
-    g.set_metrics_diag(d11, d22, d33, J)
-    del d11, d22, d33
+
+def make_solver(n, precision, metrics, st):
+    from astr_gb300 import capi
+    from astr_gb300.solver import GpuSolver
+    g = GpuSolver(n, n, n, order=capi.ORDER_MAIN, precision=precision, mach=0.1,
+                  reynolds=1600.0, deltat=st["deltat"])
+    g.set_metrics_diag(*metrics)
     g.upload_state(st["q"], st["rho"], st["vel"], st["prs"], st["tmp"])
+    return g
+
+
+def interior_q(g, n):
+    """Interior conserved variables (n+1)^3 x 5 from the device."""
+    s = g.download_state()
+    h = 5
+    return np.ascontiguousarray(s["q"][h:h + n + 1, h:h + n + 1, h:h + n + 1, :])
+
+
+def state_error(q, ref):
+    """Relative L2 and Linf of q against ref: density and energy field by
+    field, momentum as one vector field (the TGV's w starts at zero), and the
+    whole state with each variable scaled by its reference RMS."""
+    def l2(a, b):
+        return float(np.linalg.norm((a - b).ravel()) / np.linalg.norm(b.ravel()))
+
+    def linf(a, b):
+        return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+    groups = {"rho": slice(0, 1), "momentum": slice(1, 4), "energy": slice(4, 5)}
+    out = {"rel_l2": {}, "rel_linf": {}}
+    for k, sl in groups.items():
+        out["rel_l2"][k] = l2(q[..., sl], ref[..., sl])
+        out["rel_linf"][k] = linf(q[..., sl], ref[..., sl])
+    return out
+
+
+def form_roofline(kt, f32, pts_int, fp64_peak, hbm_peak):
+    classes = {}
+    for k in ("filter", "convgrad", "visc"):
+        tms, cnt = kt[k]
+        if cnt == 0:
+            continue
+        nbytes, flops = class_work(k, f32, cnt, pts_int)
+        classes[k] = {"ms": tms, "launches": cnt, "avg_ms": tms / cnt,
+                      "gbs": nbytes / (tms / 1e3) / 1e9, "tflops": flops / (tms / 1e3) / 1e12,
+                      "bytes_per_launch": nbytes / cnt, "flops_per_launch": flops / cnt}
+    dom = max(classes, key=lambda k: classes[k]["ms"])
+    dc = classes[dom]
+    traffic = None
+    try:
+        prof = json.load(open(os.path.join(ROOT, "profiles", "ncu_traffic.json")))
+        bpt = prof.get("fp32" if f32 else "fp64", {}).get(dom, {}).get("bytes_per_pt")
+        traffic = None if bpt is None else round(bpt * pts_int)
+    except Exception:
+        pass
+    rnd = lambda v: round(v, 4) if isinstance(v, float) else v  # noqa: E731
+    if f32:
+        roof = {"bound": "hbm", "kernel": dom, "achieved": round(dc["gbs"], 1),
+                "peak": hbm_peak, "unit": "GB/s", "frac": round(dc["gbs"] / hbm_peak, 4),
+                "peak_source": "hbm_gbs of measured (MEASURED_PEAKS.json, burst copy)"}
+    else:
+        roof = {"bound": "fp64", "kernel": dom, "achieved": round(dc["tflops"], 4),
+                "peak": round(fp64_peak, 4), "unit": "TFLOP/s",
+                "frac": round(dc["tflops"] / fp64_peak, 4),
+                "peak_source": "FP64 FMA loop measured live in this run",
+                "hbm_achieved_gbs": round(dc["gbs"], 1),
+                "hbm_frac_of_measured": round(dc["gbs"] / hbm_peak, 4)}
+    roof["traffic"] = traffic
+    roof["classes"] = {k: {kk: rnd(vv) for kk, vv in v.items()} for k, v in classes.items()}
+    return roof
+
+
+def time_form(g, args, dist):
+    """Warm-up, then K timed steps with per-class kernel times; returns
+    (device ms for K steps, kernel times, clock record, first-step stats)."""
     hist0 = g.time_integration_rk(1)  # includes kernel warm-up
     if args.warmup > 1:
         g.timed_steps(args.warmup - 1)
-
     clocks = ClockSampler(env_int("LOCAL_RANK", 0))
     clocks.start()
     barrier(dist)
@@ -218,61 +336,60 @@ def run_gpu(args, rank, world, dist):
     g.set_profiling(False)
     barrier(dist)
     clk = clocks.stop()
-    ms = max_over_ranks(dist, ms)
-    pts = float(n) ** 3
-    value = world * pts * 3 * args.steps / (ms / 1e3) / 1e6
+    return max_over_ranks(dist, ms), kt, clk, hist0
 
-    # roofline of the dominant kernel class
-    I = n + 1
-    pts_int = float(I) ** 3
-    tf_peak = ctypes_peak()
-    classes = {}
-    for k in ("filter", "convgrad", "visc"):
-        tms, cnt = kt[k]
-        if cnt == 0:
-            continue
-        if k == "filter":
-            flops = FLOPS_PER_PT["filter"] * pts_int * cnt
-        elif k == "convgrad":
-            per_stage = 2 * FLOPS_PER_PT["convgrad"] + FLOPS_PER_PT["convgrad_last"]
-            flops = per_stage / 3.0 * pts_int * cnt
-        else:
-            per_stage = 2 * FLOPS_PER_PT["visc"] + FLOPS_PER_PT["visc_last"]
-            flops = per_stage / 3.0 * pts_int * cnt
-        nbytes = BYTES_PER_PT[k] * pts_int * cnt
-        classes[k] = {"ms": tms, "launches": cnt, "avg_ms": tms / cnt,
-                      "tflops": flops / (tms / 1e3) / 1e12, "gbs": nbytes / (tms / 1e3) / 1e9,
-                      "flops_per_launch": flops / cnt, "bytes_per_launch": nbytes / cnt}
-    dom = max(classes, key=lambda k: classes[k]["ms"])
+
+def run_gpu(args, rank, world, dist):
+    from astr_gb300 import capi
+
+    n = args.n
+    t0 = time.perf_counter()
+    metrics, st = tgv_inputs(n)
+    deltat = st["deltat"]
+    t_setup = time.perf_counter() - t0
+    pts = float(n) ** 3
+    pts_int = float(n + 1) ** 3
+    steps_total = args.warmup + args.steps
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except Exception:
         pass
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
-    traffic = None
-    try:
-        prof = json.load(open(os.path.join(ROOT, "profiles", "ncu_traffic.json")))
-        traffic = prof.get(dom, {}).get("bytes_per_launch_512")
-    except Exception:
-        pass
-    dc = classes[dom]
-    roofline = {
-        "bound": "fp64",
-        "kernel": dom,
-        "achieved": round(dc["tflops"], 4),
-        "peak": round(tf_peak, 4),
-        "unit": "TFLOP/s",
-        "frac": round(dc["tflops"] / tf_peak, 4),
-        "peak_source": "FP64 FMA loop measured live in this run (astr_gpu_measure_fp64_peak)",
-        "traffic": traffic,
-        "hbm_achieved_gbs": round(dc["gbs"], 1),
-        "hbm_frac_of_measured": round(dc["gbs"] / hbm_peak, 4),
-        "classes": {k: {kk: (round(vv, 4) if isinstance(vv, float) else vv) for kk, vv in v.items()}
-                    for k, v in classes.items()},
-    }
+    fp64_peak = ctypes_peak()
 
-    # end to end through the C ABI with page-locked host buffers
+    forms = {}
+    finals = {}
+    clocks = {}
+    runs = [("fp64", capi.FP64), ("fp32_storage", capi.FP32_STORAGE)]
+    if args.form != "both":
+        # one form only (for profiling); no error against FP64
+        runs = [r for r in runs if r[0] == args.form]
+    for name, prec in runs:
+        g = make_solver(n, prec, metrics, st)
+        ms, kt, clk, hist0 = time_form(g, args, dist)
+        forms[name] = {
+            "value": round(world * pts * 3 * args.steps / (ms / 1e3) / 1e6, 3),
+            "ms_per_step": round(ms / args.steps, 3),
+            "roofline": form_roofline(kt, prec == capi.FP32_STORAGE, pts_int, fp64_peak, hbm_peak),
+            "footprint_gb": round(capi.load().astr_gpu_footprint(g.dims, g.params) / 1e9, 2),
+            "stats_first_step": {"kenergy": float(hist0[0, 0]), "enstrophy": float(hist0[0, 1])},
+        }
+        clocks[name] = clk
+        finals[name] = interior_q(g, n) if rank == 0 else None
+        if name == runs[-1][0]:
+            head = g
+        else:
+            g.close()
+    err = None
+    if rank == 0 and len(runs) == 2:
+        err = state_error(finals["fp32_storage"], finals["fp64"])
+        err["steps"] = steps_total
+        err["reference"] = "plain FP64 GPU form, same initial state and steps"
+    finals.clear()
+
+    # end to end through the C ABI with page-locked host buffers (headline form)
+    g = head
     pinned = {}
     for k in ("q", "rho", "vel", "prs", "tmp"):
         pa = capi.PinnedArray(st[k].shape)
@@ -294,7 +411,6 @@ def run_gpu(args, rank, world, dist):
     e2e_value = world * pts * 3 * e2e_steps / t_e2e / 1e6
     for pa in list(pinned.values()) + [qout]:
         pa.free()
-    launches_per_step = None
     g0 = g.launches
     g.timed_steps(1)
     launches_per_step = g.launches - g0
@@ -304,29 +420,75 @@ def run_gpu(args, rank, world, dist):
     if rank == 0 and not args.no_cpu:
         v, cores, dt = cpu_port_throughput(128, 4, threads=os.cpu_count())
         cpu = {"value": round(v, 3), "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": f"C++ restatement of the reference routines (oracle/), TGV 128^3 "
+               "sample": f"C++ restatement of the reference routines (oracle/), FP64, TGV 128^3 "
                          f"main-solver ordering, 4 RK3 steps in {dt:.1f} s, {cores} OpenMP threads"}
     if rank == 0:
+        f32 = forms[runs[-1][0]]
         line = {
-            "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
+            "metric": METRIC, "value": f32["value"], "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "ms_per_step": f32["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 storage, f64 accumulate",
+            "data": "synthetic",
             "config": {"workload": f"Taylor-Green vortex {n}^3 ({n + 1}^3 stored nodes), Re 1600, "
                                    "Mach 0.1, 643c compact scheme + compact filter alpha 0.49, "
-                                   "RK3 dt 1e-3, main-solver stage order",
-                       "form": "plain FP64", "parallelism": f"replicas x{world}",
-                       "l2": "inputs resident in HBM (~50 GB) >> 129 MB L2, no flush",
+                                   f"RK3 at CFL {CFL} (dt {deltat:.4e}), main-solver stage order",
+                       "form": "FP32 storage / FP64 accumulate (headline); plain FP64 beside it",
+                       "parallelism": f"replicas x{world}",
+                       "l2": "inputs resident in HBM (37-50 GB) >> 129 MB L2, no flush",
                        "setup_s": round(t_setup, 1)},
+            "forms": forms,
+            "fp32_over_fp64": (round(f32["value"] / forms["fp64"]["value"], 3)
+                               if len(forms) == 2 else None),
+            "error_vs_fp64": err,
             "gpu_launches": launches_per_step * args.steps,
-            "roofline": roofline,
+            "roofline": f32["roofline"],
             "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "steps": e2e_steps},
             "cpu_baseline": cpu,
-            "clocks": clk,
-            "stats_first_step": {"kenergy": float(hist0[0, 0]), "enstrophy": float(hist0[0, 1])},
+            "clocks": clocks[runs[-1][0]],
+            "clocks_fp64": clocks.get("fp64"),
         }
         print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_history(args, rank, world, dist):
+    """Both forms N steps with per-step statistics; the largest relative
+    difference of the kinetic-energy / enstrophy histories and the final
+    state error."""
+    from astr_gb300 import capi
+    if rank != 0:
+        return 0
+    n = args.n
+    metrics, st = tgv_inputs(n)
+    hist, finals, ms = {}, {}, {}
+    for name, prec in (("fp64", capi.FP64), ("fp32_storage", capi.FP32_STORAGE)):
+        g = make_solver(n, prec, metrics, st)
+        t0 = time.perf_counter()
+        hist[name] = g.time_integration_rk(args.history)
+        ms[name] = 1e3 * (time.perf_counter() - t0) / args.history
+        finals[name] = interior_q(g, n)
+        g.close()
+    h64, h32 = hist["fp64"], hist["fp32_storage"]
+    rel = np.abs(h32 - h64) / np.abs(h64)
+    err = state_error(finals["fp32_storage"], finals["fp64"])
+    line = {
+        "workload": f"Taylor-Green vortex {n}^3, Re 1600, Mach 0.1, main-solver order, "
+                    f"CFL {CFL} (dt {st['deltat']:.4e})",
+        "steps": args.history,
+        "kenergy_max_rel_diff": float(rel[:, 0].max()),
+        "enstrophy_max_rel_diff": float(rel[:, 1].max()),
+        "kenergy_first_last_fp64": [float(h64[0, 0]), float(h64[-1, 0])],
+        "enstrophy_first_last_fp64": [float(h64[0, 1]), float(h64[-1, 1])],
+        "final_state_error": err,
+        "wall_ms_per_step_with_stats": {k: round(v, 2) for k, v in ms.items()},
+    }
+    print(json.dumps(line), flush=True)
+    if args.history_out:
+        os.makedirs(os.path.dirname(os.path.abspath(args.history_out)), exist_ok=True)
+        np.savetxt(args.history_out, np.column_stack([np.arange(1, args.history + 1), h64, h32]),
+                   header="step ke_fp64 enstrophy_fp64 ke_fp32s enstrophy_fp32s")
     return 0
 
 
@@ -347,12 +509,17 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=512)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--form", default="both", choices=["both", "fp64", "fp32_storage"])
+    ap.add_argument("--history", type=int, default=0)
+    ap.add_argument("--history-out", default="")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     rank, world, dist = dist_setup()
     if args.impl == "reference":
         return run_reference(args, rank, world, dist)
+    if args.history:
+        return run_history(args, rank, world, dist)
     return run_gpu(args, rank, world, dist)
 
 
