@@ -286,6 +286,109 @@ def tgv_state(im, jm, km, mach=0.1, x=None, y=None, z=None):
     return _pack_state(im, jm, km, rho, u, v, w, p, T, q5)
 
 
+def vortex_fields(x, y, t=0.0, beta=5.0, gamma=1.4, half=5.0, uinf=(1.0, 1.0)):
+    """Isentropic vortex of strength beta (Shu, NASA/CR-97-206253 / ICASE
+    97-65, 1997, sec. 4.3.5; Yee, Sandham & Djomehri, JCP 150, 1999): on the
+    periodic box [-half, half)^2 with freestream (u, v) = uinf, rho = p = T =
+    1 far away, the exact solution at time t is the initial vortex advected
+    to centre uinf * t (nearest periodic image):
+        du, dv = beta/(2 pi) exp((1 - r^2)/2) (-ybar, xbar)
+        dT = -(gamma - 1) beta^2 / (8 gamma pi^2) exp(1 - r^2)
+        rho = T^(1/(gamma-1)),  p = rho T.
+    In ASTR's nondimensional variables with mach = 1/sqrt(gamma), p_inf =
+    1/(gamma mach^2) = 1 and T = p/rho * gamma mach^2 = p/rho, so these are
+    the solver's own rho, u, v, p, T."""
+    L = 2.0 * half
+    X = np.asarray(x).reshape(-1, 1)
+    Y = np.asarray(y).reshape(1, -1)
+    xb = np.mod(X - uinf[0] * t + half, L) - half
+    yb = np.mod(Y - uinf[1] * t + half, L) - half
+    r2 = xb * xb + yb * yb
+    e = np.exp(0.5 * (1.0 - r2))
+    u = uinf[0] - beta / (2.0 * PI) * e * yb
+    v = uinf[1] + beta / (2.0 * PI) * e * xb
+    T = 1.0 - (gamma - 1.0) * beta * beta / (8.0 * gamma * PI * PI) * e * e
+    rho = T ** (1.0 / (gamma - 1.0))
+    p = rho * T
+    return rho, u, v, p, T
+
+
+def vortex_grid(n, half=5.0):
+    """gridcube-style nodes of the 2-D periodic box [-half, half]: x(0:n),
+    y(0:n), z = 0 (a 2-D case has km = 0)."""
+    x, y, z = gridcube(n, n, 0, 2.0 * half, 2.0 * half, 0.0)
+    return x - half, y - half, z
+
+
+def vortex_state(n, t=0.0, beta=5.0, gamma=1.4, half=5.0):
+    """Halo-layout state (q, rho, vel, prs, tmp; km = 0) of the isentropic
+    vortex on the n^2 grid at time t, with interior nodes set."""
+    x, y, _ = vortex_grid(n, half)
+    rho, u, v, p, T = vortex_fields(x, y, t, beta, gamma, half)
+    mach = 1.0 / np.sqrt(gamma)
+    c = refcal(mach, 1.0, gamma=gamma)
+    rho3, u3, v3 = (a[:, :, None] for a in (rho, u, v))
+    p3, T3 = p[:, :, None], T[:, :, None]
+    w3 = np.zeros_like(rho3)
+    q5 = rho3 * (T3 * c["const1"] + 0.5 * (u3 * u3 + v3 * v3))
+    return _pack_state(n, n, 0, rho3, u3, v3, w3, p3, T3, q5)
+
+
+def channel_grid(ia, ja, ka, lx=2.0 * PI, ly=2.0, lz=PI, stretch=2.0, varc=None):
+    """Channel nodes: x and z uniform (grichan, src/gridgeneration.F90:
+    272-340, box 2 pi x 2 x pi with ref_len = 1), y on [0, ly] clustered at
+    both walls.  Default: y = ly/2 (1 + tanh(s (2j/ja - 1)) / tanh s) with
+    stretch s; varc given: grichan's own y = ly/2 (1 + varc tanh(atanh(1/varc)
+    (2j/ja - 1)))."""
+    x = np.array([lx / float(ia) * float(i) for i in range(ia + 1)])
+    eta = np.array([2.0 * float(j) / float(ja) - 1.0 for j in range(ja + 1)])
+    if varc is None:
+        y = 0.5 * ly * (1.0 + np.tanh(stretch * eta) / np.tanh(stretch))
+    else:
+        y = 0.5 * ly * (1.0 + varc * np.tanh(np.arctanh(1.0 / varc) * eta))
+    y[0], y[-1] = 0.0, ly
+    z = np.array([0.0] if ka == 0 else [lz / float(ka) * float(k) for k in range(ka + 1)])
+    return x, y, z
+
+
+def splitmix64_uniform(seed, counter):
+    """Counter-based uniform numbers in [0, 1): the splitmix64 output
+    function (Steele, Lea & Flood, OOPSLA 2014) applied to seed + (counter
+    + 1) * golden gamma; 53 high bits.  Vectorised over integer counters, so
+    a node's numbers do not depend on the grid traversal order."""
+    with np.errstate(over="ignore"):
+        z = np.uint64(seed) + (np.asarray(counter, dtype=np.uint64) + np.uint64(1)) * \
+            np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return (z >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+
+
+def channel_state(ia, ja, ka, y, mach=0.5, prandtl=0.72, gamma=1.4, seed=20261203, amp=0.05):
+    """Channel initial state (after chanini, src/initialisation.F90:749-1001,
+    ref_len = 1): laminar profile U = 1.5 (1 - (y-1)^2), T = 1 + (gamma-1)
+    Pr M^2/3 * 1.5 (1 - (y-1)^4), rho = 1, p = rho T / (gamma M^2), plus a
+    uniform random velocity perturbation of relative size amp on all three
+    components, u' = amp U r, r in [-1, 1) from splitmix64 with the given
+    seed and counter 3*(i + (ia+1)(j + (ja+1) k)) + component (the
+    reference draws its perturbation from Fortran's random_number)."""
+    c = refcal(mach, 1.0, prandtl, gamma)
+    shape = (ia + 1, ja + 1, ka + 1)
+    Y = np.asarray(y).reshape(1, -1, 1)
+    U = 1.5 * (1.0 - (Y - 1.0) ** 2) * np.ones(shape)
+    node = np.arange(int(np.prod(shape)), dtype=np.uint64).reshape(shape, order="F")
+    r = [2.0 * splitmix64_uniform(seed, np.uint64(3) * node + np.uint64(m)) - 1.0 for m in range(3)]
+    u = U * (1.0 + amp * r[0])
+    v = amp * U * r[1]
+    w = amp * U * r[2] if ka > 0 else np.zeros(shape)
+    T = (1.0 + (gamma - 1.0) * prandtl * mach ** 2 / 3.0 * 1.5 * (1.0 - (Y - 1.0) ** 4)) * np.ones(shape)
+    rho = np.ones(shape)
+    p = rho * T / c["const2"]
+    q5 = rho * (T * c["const1"] + 0.5 * (u * u + v * v + w * w))
+    return _pack_state(ia, ja, ka, rho, u, v, w, p, T, q5)
+
+
 def _pack_state(im, jm, km, rho, u, v, w, p, T, q5):
     full = (im + 2 * HM + 1, jm + 2 * HM + 1, km + 2 * HM + 1)
     sl = (slice(HM, HM + im + 1), slice(HM, HM + jm + 1), slice(HM, HM + km + 1))

@@ -492,6 +492,68 @@ def run_history(args, rank, world, dist):
     return 0
 
 
+def run_vortex(args, rank, world, dist):
+    """2-D isentropic vortex transport (periodic [-5,5]^2, beta 5, freestream
+    (1,1), inviscid, CFL 0.5): both forms for args.vortex_steps steps, each
+    scored by relative L2 / Linf error against the analytic translated
+    vortex and the FP32-storage form against the FP64 form."""
+    from astr_gb300 import capi, cases
+    from astr_gb300.solver import GpuSolver
+    if rank != 0:
+        return 0
+    n = args.vortex_n
+    gamma = 1.4
+    mach = 1.0 / np.sqrt(gamma)
+    st = cases.vortex_state(n)
+    x, y, z = cases.vortex_grid(n)
+    (d11, d22, d33), J = cases.rect_metrics(x, y, z, diag_only=True)
+    dt = cases.cfl_deltat(st, (d11, d22, d33), mach, CFL)
+    steps = args.vortex_steps
+    t_end = steps * dt
+    ex = cases.vortex_state(n, t=t_end)
+    h = 5
+    sl = (slice(h, h + n + 1), slice(h, h + n + 1), h)
+
+    def errs(s, ref):
+        out = {}
+        for name, a, b in (("rho", s["rho"][sl], ref["rho"][sl]),
+                           ("u", s["vel"][sl + (0,)], ref["vel"][sl + (0,)]),
+                           ("v", s["vel"][sl + (1,)], ref["vel"][sl + (1,)]),
+                           ("p", s["prs"][sl], ref["prs"][sl])):
+            d = a - b
+            out[name] = {"rel_l2": float(np.linalg.norm(d) / np.linalg.norm(b)),
+                         "rel_linf": float(np.abs(d).max() / np.abs(b).max())}
+        return out
+
+    forms, finals = {}, {}
+    for name, prec in (("fp64", capi.FP64), ("fp32_storage", capi.FP32_STORAGE)):
+        g = GpuSolver(n, n, 0, precision=prec, diffterm=False, mach=mach, reynolds=1e4, deltat=dt)
+        g.set_metrics_diag(d11, d22, d33, J)
+        g.upload_state(st["q"], st["rho"], st["vel"], st["prs"], st["tmp"])
+        g.timed_steps(args.warmup)
+        g.upload_state(st["q"], st["rho"], st["vel"], st["prs"], st["tmp"])
+        ms = g.timed_steps(steps)
+        s = g.download_state()
+        g.close()
+        forms[name] = {"value": round(float(n) ** 2 * 3 * steps / (ms / 1e3) / 1e6, 3),
+                       "ms_per_step": round(ms / steps, 4),
+                       "error_vs_analytic": errs(s, ex)}
+        finals[name] = s
+    forms["fp32_storage"]["error_vs_fp64"] = errs(finals["fp32_storage"], finals["fp64"])
+    line = {
+        "case": "vortex2d",
+        "workload": f"isentropic vortex beta 5, periodic [-5,5]^2, {n}^2, freestream (1,1), "
+                    f"inviscid, filter alpha 0.49, CFL {CFL} (dt {dt:.4e}), {steps} RK3 steps "
+                    f"(t = {t_end:.4f})",
+        "unit": UNIT, "forms": forms,
+        "fp32_over_fp64": round(forms["fp32_storage"]["value"] / forms["fp64"]["value"], 3),
+        "note": "analytic solution: the initial vortex translated by (t, t), nearest periodic "
+                "image; device time of the stepping loop (no statistics), state resident in HBM",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def ctypes_peak():
     import ctypes
     from astr_gb300 import capi
@@ -510,6 +572,9 @@ def main():
     ap.add_argument("--n", type=int, default=512)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--form", default="both", choices=["both", "fp64", "fp32_storage"])
+    ap.add_argument("--case", default="tgv", choices=["tgv", "vortex2d"])
+    ap.add_argument("--vortex-n", type=int, default=512)
+    ap.add_argument("--vortex-steps", type=int, default=1000)
     ap.add_argument("--history", type=int, default=0)
     ap.add_argument("--history-out", default="")
     args = ap.parse_args()
@@ -518,6 +583,8 @@ def main():
     rank, world, dist = dist_setup()
     if args.impl == "reference":
         return run_reference(args, rank, world, dist)
+    if args.case == "vortex2d":
+        return run_vortex(args, rank, world, dist)
     if args.history:
         return run_history(args, rank, world, dist)
     return run_gpu(args, rank, world, dist)

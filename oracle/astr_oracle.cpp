@@ -78,6 +78,9 @@ struct orc_ctx {
   std::vector<double> qrhs, qsave, dvel, dtmp;
   double force[3] = {0, 0, 0};
   double massflux_target = 0.0;
+  double massflux = 0.0, fbcx = 0.0;  // last statcal values (channel)
+  long nstep = 0;                     // completed time steps
+  bool rkfirst_called = false;        // rkfirst's firstcall flag
 
   inline long h(int i, int j, int k) const {
     return (long)(i + HM) + NI * ((long)(j + HM) + NJ * (long)(k + HM));
@@ -948,7 +951,118 @@ void orc_qswap(orc_ctx* c) {
   }
 }
 
-void orc_boucon(orc_ctx* c) { (void)c; }
+// boucon (src/bc.F90:327-409): for the channel, noslip isothermal walls
+// at j = 0 and j = jm (bctype 41; noslip, src/bc.F90:6423-6611): u = 0,
+// T = T_w, p extrapolated (4 p(1) - p(2))/3, rho = p/T*const2 (thermal,
+// src/fludyna.F90:45-110), q = fvar2q with pressure (312-376).
+void orc_boucon(orc_ctx* c) {
+  if (!c->cfg.channel || c->cfg.npdcj != 4) return;
+  const long nh = c->nh;
+  const double tw = c->cfg.twall;
+  for (int side = 0; side < 2; ++side) {
+    const int j = side == 0 ? 0 : c->jm;
+    const int j1 = side == 0 ? 1 : c->jm - 1, j2 = side == 0 ? 2 : c->jm - 2;
+    for (int k = 0; k <= c->km; ++k)
+      for (int i = 0; i <= c->im; ++i) {
+        const long p = c->h(i, j, k);
+        const double pe = NUM1D3 * (4.0 * c->prs[c->h(i, j1, k)] - c->prs[c->h(i, j2, k)]);
+        c->vel[p] = 0.0;
+        c->vel[p + nh] = 0.0;
+        c->vel[p + 2 * nh] = 0.0;
+        c->prs[p] = pe;
+        c->tmp[p] = tw;
+        c->rho[p] = c->prs[p] / c->tmp[p] * c->const2;
+        fvar2q_prs_node(*c, p);
+      }
+  }
+}
+
+namespace {
+
+// Trapezoid sums over y of 0.5*(f(j-1)+f(j))*dy, i = 1..im, j = 1..jm,
+// k = 1..km (k = 0 in 2-D): the bulk integrals of src_chan and
+// massfluxchan (src/solver.F90:295-353, src/statistic.F90:1437-1476).
+double ytrapezoid(const orc_ctx& c, int m) {
+  const int k1 = c.ndims == 3 ? 1 : 0, k2 = c.ndims == 3 ? c.km : 0;
+  const long nh = c.nh;
+  double s = 0.0;
+  for (int k = k1; k <= k2; ++k)
+    for (int j = 1; j <= c.jm; ++j)
+      for (int i = 1; i <= c.im; ++i) {
+        const double dy = c.x[c.h(i, j, k) + nh] - c.x[c.h(i, j - 1, k) + nh];
+        s = s + 0.5 * (c.q[c.h(i, j - 1, k) + m * nh] + c.q[c.h(i, j, k) + m * nh]) * dy;
+      }
+  return s;
+}
+
+// src_chan, src/solver.F90:295-353: body force and its work.
+void src_chan(orc_ctx& c) {
+  double robulk = ytrapezoid(c, 0);
+  double u1 = ytrapezoid(c, 1) / robulk;
+  double u2 = ytrapezoid(c, 2) / robulk;
+  double u3 = ytrapezoid(c, 3) / robulk;
+  const long n0 = c.n0;
+  for (int k = 0; k <= c.km; ++k)
+    for (int j = 0; j <= c.jm; ++j)
+      for (int i = 0; i <= c.im; ++i) {
+        const long z = c.z(i, j, k);
+        const double J = c.jacob[c.h(i, j, k)];
+        c.qrhs[z + 1 * n0] = c.qrhs[z + 1 * n0] + c.force[0] * J;
+        c.qrhs[z + 2 * n0] = c.qrhs[z + 2 * n0] + c.force[1] * J;
+        c.qrhs[z + 3 * n0] = c.qrhs[z + 3 * n0] + c.force[2] * J;
+        c.qrhs[z + 4 * n0] =
+            c.qrhs[z + 4 * n0] + (c.force[0] * u1 + c.force[1] * u2 + c.force[2] * u3) * J;
+      }
+}
+
+// statcal for flowtype 'channel' (src/statistic.F90:641-657): wall friction
+// fbcxchan (1303-1367), mass flux massfluxchan (1437-1476), the target set
+// on the first call, and the body force from chanfoce (1494-1533).
+void chan_statcal(orc_ctx& c) {
+  const int k1 = c.ndims == 3 ? 1 : 0, k2 = c.ndims == 3 ? c.km : 0;
+  const double norm = c.ndims == 3 ? (double)c.cfg.ia * (double)c.cfg.ka : (double)c.cfg.ia;
+  const long n0 = c.n0;
+  double fb = 0.0;
+  for (int side = 0; side < 2; ++side) {
+    const int j = side == 0 ? 0 : c.jm;
+    for (int k = k1; k <= k2; ++k)
+      for (int i = 1; i <= c.im; ++i) {
+        const double T = c.tmp[c.h(i, j, k)];
+        const double miu = T * std::sqrt(T) * c.tempconst1 / (T + c.tempconst) / c.cfg.reynolds;
+        const double dudy = c.dvel[c.z(i, j, k) + 3 * n0];  // dvel(i,j,k,1,2)
+        fb = side == 0 ? fb + miu * dudy : fb - miu * dudy;
+      }
+  }
+  c.fbcx = fb / norm;
+  c.massflux = ytrapezoid(c, 1) / norm;
+  if (std::fabs(c.massflux_target) < 1e-16) {
+    c.massflux_target = c.massflux;
+    c.force[0] = c.force[1] = c.force[2] = 0.0;
+  }
+  const double ly = c.x[c.h(0, c.jm, 0) + c.nh] - c.x[c.h(0, 0, 0) + c.nh];
+  const double f = c.force[0];
+  double fnew;
+  if (c.nstep == 0) {
+    fnew = c.fbcx / ly;
+  } else {
+    const double gn = ly * f - c.fbcx;
+    const double qn1 = c.massflux + c.cfg.deltat * gn;
+    const double ref_len = 1.0;  // nondimensional reference length, src/solver.F90:126
+    fnew = f - (2.0 * (qn1 - c.massflux_target) - 0.2 * (c.massflux - c.massflux_target)) / ly *
+                   (c.uinf / ref_len);
+  }
+  c.force[0] = fnew;
+}
+
+}  // namespace
+
+void orc_chan_state(orc_ctx* c, double* out) {
+  out[0] = c->force[0];
+  out[1] = c->massflux;
+  out[2] = c->massflux_target;
+  out[3] = c->fbcx;
+  out[4] = (double)c->nstep;
+}
 
 // gradcal, src/comsolver.F90:244-497 (main) ; tgvsolver.F90:450-537 (mini-app)
 void orc_gradcal(orc_ctx* c) {
@@ -1167,6 +1281,7 @@ void orc_rhscal(orc_ctx* c) {
   orc_convrsdcal6(c);
   for (auto& r : c->qrhs) r = -r;
   if (c->cfg.diffterm) orc_diffrsdcal6(c);
+  if (c->cfg.channel) src_chan(*c);
 }
 
 // updatefvar -> q2fvar_3da on 0:im (src/fludyna.F90:191-242)
@@ -1288,6 +1403,9 @@ void orc_rk3_step(orc_ctx* c, double* stats) {
                 c->qsave[c->z(i, j, k) + n * n0] = c->q[p + n * nh] * c->jacob[p];
               }
         if (stats) { stats[0] = orc_kenergy(c); stats[1] = orc_enstrophy(c); }
+        // rkfirst (src/mainloop.F90:614-697): statcal from the second call on
+        if (c->cfg.channel && c->rkfirst_called) chan_statcal(*c);
+        c->rkfirst_called = true;
       }
       orc_rhscal(c);
 #pragma omp parallel for collapse(2)
@@ -1304,6 +1422,7 @@ void orc_rk3_step(orc_ctx* c, double* stats) {
       orc_updatefvar(c);
     }
   }
+  c->nstep = c->nstep + 1;
 }
 
 void orc_rk3_steps(orc_ctx* c, int nsteps, double* stats) {

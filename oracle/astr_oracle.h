@@ -75,7 +75,10 @@ void orc_updateq(orc_ctx* c);       /* q from primitives at 0:im (fvar2q with T)
 /* Hot-path restatements (each acts on the context's arrays). */
 void orc_filterq(orc_ctx* c);
 void orc_qswap(orc_ctx* c);
-void orc_boucon(orc_ctx* c);
+void orc_boucon(orc_ctx* c);       /* channel: noslip isothermal j-walls; else no-op */
+/* Channel controller state: force(1), mass flux, its target, wall friction,
+ * completed steps (5 doubles). */
+void orc_chan_state(orc_ctx* c, double* out5);
 void orc_gradcal(orc_ctx* c);
 void orc_convrsdcal6(orc_ctx* c);
 void orc_diffrsdcal6(orc_ctx* c);

@@ -81,6 +81,7 @@ def lib():
                      "orc_boucon", "orc_gradcal", "orc_convrsdcal6", "orc_diffrsdcal6",
                      "orc_rhscal", "orc_updatefvar", "orc_bchomo"):
             getattr(L, name).argtypes = [vp]
+        L.orc_chan_state.argtypes = [vp, dp]
         L.orc_rk3_step.argtypes = [vp, dp]
         L.orc_rk3_steps.argtypes = [vp, ctypes.c_int, dp]
         L.orc_line_derivative.argtypes = [vp, ctypes.c_int, dp, dp]
@@ -173,6 +174,22 @@ class Oracle:
     def gridcube(self, lx, ly, lz):
         self.L.orc_gridcube(self.h, lx, ly, lz)
 
+    def set_grid(self, x, y, z):
+        """Rectilinear node coordinates x(0:im), y(0:jm), z(0:km) into the
+        interior of the coordinate array (gridgeom fills the halos)."""
+        X = self.field("x")
+        h = HM
+        sl = (slice(h, h + self.im + 1), slice(h, h + self.jm + 1), slice(h, h + self.km + 1))
+        X[sl + (0,)] = np.asarray(x).reshape(-1, 1, 1)
+        X[sl + (1,)] = np.asarray(y).reshape(1, -1, 1)
+        X[sl + (2,)] = np.asarray(z).reshape(1, 1, -1)
+
+    def chan_state(self):
+        """(force(1), mass flux, target mass flux, wall friction, steps)."""
+        out = np.zeros(5)
+        self.L.orc_chan_state(self.h, _dptr(out))
+        return out
+
     def call(self, name: str):
         getattr(self.L, "orc_" + name)(self.h)
 
@@ -227,4 +244,21 @@ def tgv_miniapp(n: int, **kw) -> Oracle:
     kw.setdefault("beter_bound", 1.09)
     o = Oracle(n, n, n, mode=MODE_MINIAPP, **kw)
     o.call("init_tgv")
+    return o
+
+
+def from_state(st, dims, *, lx=None, ly=None, lz=None, grid=None, **kw) -> Oracle:
+    """An oracle case on a gridcube box (lx, ly, lz), or on the rectilinear
+    grid = (x, y, z), with metrics from gridgeom and the given halo-layout
+    state (q, rho, vel, prs, tmp) written into its interior nodes (the
+    filter's own halo swaps fill the halos)."""
+    im, jm, km = dims
+    o = Oracle(im, jm, km, mode=MODE_MAIN, **kw)
+    if grid is not None:
+        o.set_grid(*grid)
+    else:
+        o.gridcube(lx, ly, lz)
+    o.call("gridgeom")
+    for name in ("q", "rho", "vel", "prs", "tmp"):
+        o.field(name)[...] = st[name]
     return o
