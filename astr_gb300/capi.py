@@ -37,7 +37,8 @@ EXPORTS = [
     "astr_gpu_footprint", "astr_gpu_launch_count", "astr_gpu_set_metrics_diag",
     "astr_gpu_host_alloc", "astr_gpu_host_free", "astr_gpu_timed_steps",
     "astr_gpu_set_profiling", "astr_gpu_kernel_times", "astr_gpu_measure_fp64_peak",
-    "astr_gpu_stats_noalloc",
+    "astr_gpu_stats_noalloc", "astr_gpu_set_grid", "astr_gpu_channel_state",
+    "astr_gpu_boucon",
 ]
 NOALLOC_STATS_MAX_BLOCKS = 65536
 KERNEL_CLASSES = ["filter", "halo", "convgrad", "visc", "pointwise", "stats"]
@@ -56,7 +57,8 @@ class AstrParams(ctypes.Structure):
                 ("beter_bound", ctypes.c_double), ("mach", ctypes.c_double),
                 ("reynolds", ctypes.c_double), ("prandtl", ctypes.c_double),
                 ("ref_tem", ctypes.c_double), ("suth_const", ctypes.c_double),
-                ("deltat", ctypes.c_double)]
+                ("deltat", ctypes.c_double), ("channel", ctypes.c_int),
+                ("twall", ctypes.c_double)]
 
 
 class AstrStatus(ctypes.Structure):
@@ -94,7 +96,7 @@ def load(path: str = LIB_PATH):
     L.astr_gpu_download_rhs.argtypes = [vp, dp, dp, dp]
     L.astr_gpu_rk3_step.argtypes = [vp, ip, dp, ctypes.POINTER(AstrStatus)]
     for n in ("astr_gpu_filterq", "astr_gpu_qswap", "astr_gpu_gradcal", "astr_gpu_rhscal",
-              "astr_gpu_updatefvar", "astr_gpu_synchronize"):
+              "astr_gpu_updatefvar", "astr_gpu_synchronize", "astr_gpu_boucon"):
         getattr(L, n).argtypes = [vp]
         getattr(L, n).restype = ip
     L.astr_gpu_reduce_stats.argtypes = [vp, dp, dp]
@@ -120,6 +122,10 @@ def load(path: str = LIB_PATH):
     L.astr_gpu_stats_noalloc.argtypes = [vp, vp, vp, ctypes.POINTER(AstrDims), ctypes.c_double,
                                          vp, dp, dp]
     L.astr_gpu_stats_noalloc.restype = ip
+    L.astr_gpu_set_grid.argtypes = [vp, dp]
+    L.astr_gpu_set_grid.restype = ip
+    L.astr_gpu_channel_state.argtypes = [vp, dp]
+    L.astr_gpu_channel_state.restype = ip
     for n in ("astr_gpu_set_metrics", "astr_gpu_upload_state", "astr_gpu_download_state",
               "astr_gpu_download_rhs", "astr_gpu_rk3_step", "astr_gpu_reduce_stats"):
         getattr(L, n).restype = ip

@@ -110,6 +110,22 @@ def _extend(c: np.ndarray, dim: int, flat: bool) -> np.ndarray:
     return h
 
 
+def grid_halo(x, y, z):
+    """x(-hm:..,1:3) in the halo layout (Fortran order) for rectilinear node
+    vectors, halos filled as gridsendrecv does on one rank
+    (src/parallel.F90:2861-2866, 2930-2960, 3010-3030)."""
+    im, jm, km = len(x) - 1, len(y) - 1, len(z) - 1
+    X = _extend(x, im, False).reshape(-1, 1, 1)
+    Y = _extend(y, jm, jm == 0).reshape(1, -1, 1)
+    Z = _extend(z, km, km == 0).reshape(1, 1, -1)
+    full = (im + 2 * HM + 1, jm + 2 * HM + 1, km + 2 * HM + 1)
+    out = np.zeros(full + (3,), order="F")
+    out[..., 0] = np.broadcast_to(X, full)
+    out[..., 1] = np.broadcast_to(Y, full)
+    out[..., 2] = np.broadcast_to(Z, full)
+    return out
+
+
 def _wrap_halo(a: np.ndarray, dims, per) -> np.ndarray:
     """dataswap of an interior-valued array onto halo layout: periodic axes
     copy im-5..im-1 / 1..5 into the halos; other halos are zero."""

@@ -132,6 +132,152 @@ __global__ void k_rkupdate(Geo g, DevT<T> d, Phys ph, int q2f) {
   if (q2f) q2fvar_store(g, d, ph, p);
 }
 
+// noslip isothermal wall at j = 0 and j = jm (src/bc.F90:6423-6611): u = 0,
+// T = T_w, p = (4 p(1) - p(2))/3, rho = p/T*const2, q = fvar2q with
+// pressure (src/fludyna.F90:312-376).  The FP32 form also sets the FP64
+// master at the wall nodes.
+template <typename T>
+__global__ void k_noslip(Geo g, DevT<T> d, Phys ph, double tw, double const6) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long ncol = (long long)g.I * (g.km + 1);
+  if (idx >= 2 * ncol) return;
+  const int side = idx >= ncol ? 1 : 0;
+  const long long col = idx - side * ncol;
+  const int i = (int)(col % g.I), k = (int)(col / g.I);
+  const int j = side ? g.jm : 0, j1 = side ? g.jm - 1 : 1, j2 = side ? g.jm - 2 : 2;
+  const long long nh = g.nh;
+  const long long p = hidx(g, i, j, k);
+  const double p1 = (double)d.pr[hidx(g, i, j1, k) + 4 * nh];
+  const double p2 = (double)d.pr[hidx(g, i, j2, k) + 4 * nh];
+  const double pe = (4.0 * p1 - p2) / 3.0;
+  const double ro = pe / tw * ph.const2;
+  const double e = pe * const6;
+  d.pr[p] = (T)ro;
+  d.pr[p + nh] = T(0);
+  d.pr[p + 2 * nh] = T(0);
+  d.pr[p + 3 * nh] = T(0);
+  d.pr[p + 4 * nh] = (T)pe;
+  d.pr[p + 5 * nh] = (T)tw;
+  d.q[p] = (T)ro;
+  d.q[p + nh] = T(0);
+  d.q[p + 2 * nh] = T(0);
+  d.q[p + 3 * nh] = T(0);
+  d.q[p + 4 * nh] = (T)e;
+  if (d.qm) {
+    const long long z = zidx(g, i, j, k), n0 = g.n0;
+    d.qm[z] = ro;
+    d.qm[z + n0] = 0.0;
+    d.qm[z + 2 * n0] = 0.0;
+    d.qm[z + 3 * n0] = 0.0;
+    d.qm[z + 4 * n0] = e;
+  }
+}
+
+// Channel volume sums, one thread per (i, k) column, i = 1..im, k = 1..km
+// (k = 0 in 2-D), fixed order within a column and across the block:
+// [0..3] trapezoid integrals over y of q(1..4) (src_chan,
+// src/solver.F90:317-331; massfluxchan, src/statistic.F90:1437-1476);
+// [4] the wall friction sum of fbcxchan (src/statistic.F90:1303-1367),
+// miu(T) * du/dy at j = 0 minus at j = jm.  Block partials: 5 per block.
+template <typename T>
+__global__ void k_chan_sums(Geo g, DevT<T> d, Phys ph, const double* ycoord, double* part) {
+  __shared__ double sh[5][256];
+  const long long ncol = (long long)g.im * (g.ndims == 3 ? g.km : 1);
+  const long long col = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  if (col < ncol) {
+    const int i = 1 + (int)(col % g.im);
+    const int k = g.ndims == 3 ? 1 + (int)(col / g.im) : 0;
+    const long long nh = g.nh, n0 = g.n0;
+    double prev[4];
+    long long p = hidx(g, i, 0, k), z = zidx(g, i, 0, k);
+    for (int m = 0; m < 4; ++m) prev[m] = q64(d, p, z, m, nh, n0);
+    double yprev = ycoord[p];
+    for (int j = 1; j <= g.jm; ++j) {
+      p = hidx(g, i, j, k);
+      z = zidx(g, i, j, k);
+      const double yj = ycoord[p];
+      const double dy = yj - yprev;
+      yprev = yj;
+      for (int m = 0; m < 4; ++m) {
+        const double cur = q64(d, p, z, m, nh, n0);
+        acc[m] = acc[m] + 0.5 * (prev[m] + cur) * dy;
+        prev[m] = cur;
+      }
+    }
+    for (int side = 0; side < 2; ++side) {
+      const int j = side ? g.jm : 0;
+      const double tt = (double)d.pr[hidx(g, i, j, k) + 5 * nh];
+      const double miu = tt * sqrt(tt) * ph.tempconst1 / (tt + ph.tempconst) * ph.rreynolds;
+      const double dudy = (double)d.grad[3 * n0 + zidx(g, i, j, k)];  // dvel(i,j,k,1,2)
+      acc[4] = side ? acc[4] - miu * dudy : acc[4] + miu * dudy;
+    }
+  }
+  for (int m = 0; m < 5; ++m) sh[m][threadIdx.x] = acc[m];
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s)
+      for (int m = 0; m < 5; ++m) sh[m][threadIdx.x] += sh[m][threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x < 5) part[5 * blockIdx.x + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+// Channel controller, one thread: bulk velocity for src_chan every stage;
+// at stage 1 from the second step on, statcal's mass flux, wall friction,
+// target and the body force of chanfoce (src/statistic.F90:641-657,
+// 1494-1533; uinf = ref_len = 1).
+__global__ void k_chan_final(const double* part, int nblk, double* chan, double norm, double ly,
+                             double dt, long long nstep, int statcal) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double sum[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int b = 0; b < nblk; ++b)
+    for (int m = 0; m < 5; ++m) sum[m] += part[5 * b + m];
+  if (statcal) {
+    const double fbcx = sum[4] / norm;
+    const double massflux = sum[1] / norm;
+    chan[CHAN_FBCX] = fbcx;
+    chan[CHAN_MASSFLUX] = massflux;
+    if (fabs(chan[CHAN_TARGET]) < 1e-16) {
+      chan[CHAN_TARGET] = massflux;
+      chan[CHAN_FORCE] = 0.0;
+      chan[CHAN_FORCE + 1] = 0.0;
+      chan[CHAN_FORCE + 2] = 0.0;
+    }
+    const double f = chan[CHAN_FORCE], tgt = chan[CHAN_TARGET];
+    double fnew;
+    if (nstep == 0) {
+      fnew = fbcx / ly;
+    } else {
+      const double gn = ly * f - fbcx;
+      const double qn1 = massflux + dt * gn;
+      fnew = f - (2.0 * (qn1 - tgt) - 0.2 * (massflux - tgt)) / ly;
+    }
+    chan[CHAN_FORCE] = fnew;
+  }
+  chan[CHAN_UBULK] = sum[1] / sum[0];
+  chan[CHAN_UBULK + 1] = sum[2] / sum[0];
+  chan[CHAN_UBULK + 2] = sum[3] / sum[0];
+}
+
+// src_chan applied to qrhs itself (the per-routine rhscal entry point; the
+// stage loop folds it into the RK3 update instead).
+template <typename T>
+__global__ void k_chan_src(Geo g, DevT<T> d) {
+  int i, j, k;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (!point_of(g, idx, i, j, k)) return;
+  const double J = d.jac64[hidx(g, i, j, k)];
+  const double* C = d.chan;
+  for (int m = 1; m < 5; ++m) {
+    const double f = m < 4 ? C[CHAN_FORCE + m - 1]
+                           : C[CHAN_FORCE] * C[CHAN_UBULK] + C[CHAN_FORCE + 1] * C[CHAN_UBULK + 1] +
+                                 C[CHAN_FORCE + 2] * C[CHAN_UBULK + 2];
+    T* R = d.qrhs + m * g.n0 + idx;
+    *R = (T)((double)*R + f * J);
+  }
+}
+
 // Fixed-order reduction of the per-warp statistics partials.
 __global__ void k_stats_final(const double* part, long long nw, double* out) {
   __shared__ double sk[1024], se[1024];
@@ -388,6 +534,15 @@ struct astr_ctx {
   long long launches = 0;
   bool metrics_set = false, state_set = false;
   double l0 = 1.0;
+  // channel (flowtype 'channel')
+  bool channel = false, grid_set = false;
+  double* chan_dev = nullptr;   // CHAN_N doubles
+  double* chan_part = nullptr;  // 5 per block of k_chan_sums
+  int chan_nblk = 0;
+  double* ycoord = nullptr;     // y coordinates, halo layout
+  double chan_ly = 0.0;         // ymax - ymin
+  long long nstep = 0;          // completed time steps (statcal's nstep)
+  bool rkfirst_called = false;  // rkfirst's firstcall flag
   std::vector<void*> allocs;
   // profiling: event pairs per launch, by kernel class
   bool prof = false;
@@ -619,6 +774,36 @@ int rk_pointwise(astr_ctx* c, int q2f) {
   return after_launch(c, "k_rkupdate");
 }
 
+constexpr int CHAN_THREADS = 256;
+
+template <typename T>
+int run_noslip(astr_ctx* c) {
+  const long long n = 2LL * c->g.I * (c->g.km + 1);
+  prof_begin(c, KC_HALO);
+  k_noslip<T><<<point_grid(n), 256, 0, c->st>>>(c->g, dev<T>(c), c->ph, c->pm.twall,
+                                                  1.0 / c->ph.rconst6);
+  prof_end(c);
+  return after_launch(c, "k_noslip");
+}
+
+// Channel bulk sums and controller for one stage; statcal at stage 1 from
+// the second step on (rkfirst, src/mainloop.F90:614-697).
+template <typename T>
+int run_chan(astr_ctx* c, bool stage1) {
+  const bool statcal = stage1 && c->rkfirst_called;
+  const double norm = c->g.ndims == 3 ? (double)c->dm.ia * (double)c->dm.ka : (double)c->dm.ia;
+  prof_begin(c, KC_STATS);
+  k_chan_sums<T><<<c->chan_nblk, CHAN_THREADS, 0, c->st>>>(c->g, dev<T>(c), c->ph, c->ycoord,
+                                                          c->chan_part);
+  prof_end(c);
+  RC(after_launch(c, "k_chan_sums"));
+  k_chan_final<<<1, 32, 0, c->st>>>(c->chan_part, c->chan_nblk, c->chan_dev, norm, c->chan_ly,
+                                     c->pm.deltat, c->nstep, statcal ? 1 : 0);
+  RC(after_launch(c, "k_chan_final"));
+  if (stage1) c->rkfirst_called = true;
+  return ASTR_OK;
+}
+
 template <typename T>
 int one_step(astr_ctx* c, double* stats) {
   const bool mini = c->pm.order == ASTR_ORDER_MINIAPP;
@@ -633,13 +818,16 @@ int one_step(astr_ctx* c, double* stats) {
       RC(run_filter<T>(c, true));
     } else {
       if (c->pm.lfilter) RC(run_filter<T>(c, false));
+      if (c->channel) RC(run_noslip<T>(c));
       RC(run_qswap<T>(c));
       RC(run_convgrad<T>(c, true, true, c->pm.diffterm != 0, st1 && stats, st1));
+      if (c->channel) RC(run_chan<T>(c, st1));
       if (c->pm.diffterm) RC(run_visc<T>(c, true, true));
       else RC(rk_pointwise<T>(c, 1));
     }
     if (st1 && stats) RC(stats_finish(c, stats));
   }
+  c->nstep += 1;
   return ASTR_OK;
 }
 
@@ -682,6 +870,12 @@ int rhscal_t(astr_ctx* c) {
     RC(after_launch(c, "k_sigma"));
     RC(run_visc<T>(c, false, false));
   }
+  if (c->channel) {
+    // src_chan with the current force (the force changes at statcal only)
+    RC(run_chan<T>(c, false));
+    k_chan_src<T><<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, dev<T>(c));
+    RC(after_launch(c, "k_chan_src"));
+  }
   return ASTR_OK;
 }
 
@@ -703,6 +897,7 @@ size_t astr_gpu_footprint(const astr_dims* dims, const astr_params* params) {
   // qsave 5 (FP64); FP32 form: J, master q 5 and a staging array in FP64
   size_t b = w * (15 * nh + 26 * n0) + 8 * (nh + 5 * n0);
   if (f32) b += 8 * (2 * nh + 5 * n0);
+  if (params && params->channel) b += 8 * nh;  // y coordinates
   return b;
 }
 
@@ -721,6 +916,8 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
   if (params->order == ASTR_ORDER_MINIAPP && (npdc[0] != 3 || npdc[1] != 3 || (ndims == 3 && npdc[2] != 3)))
     return fail(nullptr, ASTR_ERR_ARG, "mini-app ordering is periodic only");
   if (ndims == 2 && npdc[2] != 3) return fail(nullptr, ASTR_ERR_ARG, "2-D cases need npdck = 3");
+  if (params->channel && (npdc[1] != 4 || params->order != ASTR_ORDER_MAIN || !(params->twall > 0.0)))
+    return fail(nullptr, ASTR_ERR_ARG, "a channel needs npdcj = 4, the main ordering and twall > 0");
 
   c = new astr_ctx();
   c->dm = *dims;
@@ -803,6 +1000,14 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
   double* part = (double*)alloc(2 * nw * 8);
   int* flag = (int*)alloc(64);
   c->stats_dev = (double*)alloc(64);
+  c->channel = params->channel != 0;
+  if (c->channel) {
+    const long long ncol = (long long)g.im * (ndims == 3 ? g.km : 1);
+    c->chan_nblk = (int)((ncol + CHAN_THREADS - 1) / CHAN_THREADS);
+    c->chan_dev = (double*)alloc(CHAN_N * 8);
+    c->chan_part = (double*)alloc(5 * (size_t)c->chan_nblk * 8);
+    c->ycoord = (double*)alloc(nh * 8);
+  }
   // schemes: per direction derivative + filter, in both precisions
   std::vector<HostScheme> hs;
   for (int dd = 0; dd < 3; ++dd) {
@@ -851,6 +1056,7 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
   if (e == cudaSuccess) e = cudaMemset(qrhs, 0, 5 * n0 * w);
   if (e == cudaSuccess) e = cudaMemset(grad, 0, 12 * n0 * w);
   if (e == cudaSuccess) e = cudaMemset(flag, 0, 64);
+  if (e == cudaSuccess && c->channel) e = cudaMemset(c->chan_dev, 0, CHAN_N * 8);
   if (e != cudaSuccess) {
     std::string m = std::string("initialisation: ") + cudaGetErrorString(e);
     astr_gpu_destroy(c);
@@ -861,7 +1067,7 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
     D.q = (TT*)q; D.pr = (TT*)pr; D.xd = (const TT*)xd; D.jac = (const TT*)jac;
     D.jac64 = c->jac64; D.rjac64 = c->rjac64;
     D.qrhs = (TT*)qrhs; D.qsave = qsave; D.qm = qm; D.grad = (TT*)grad; D.sig = (TT*)sig;
-    D.qf = (TT*)qf; D.part = part; D.flag = flag;
+    D.qf = (TT*)qf; D.part = part; D.flag = flag; D.chan = c->chan_dev;
   };
   fill(c->d64, (double*)nullptr);
   fill(c->d32, (float*)nullptr);
@@ -895,17 +1101,61 @@ static int metrics_common(astr_ctx* c, const double* const src[3], const double*
 int astr_gpu_set_metrics(astr_ctx* c, const double* dxi, const double* jacob) {
   if (!c || !dxi || !jacob) return fail(c, ASTR_ERR_ARG, "null argument");
   const size_t nh = (size_t)c->g.nh;
-  // Only diagonal metrics are built: every off-diagonal dxi must be 0.
+  // Only diagonal metrics are built.  Off-diagonals up to 1e-10 of the
+  // largest diagonal entry are gridgeom's rounding residue on a stretched
+  // rectilinear grid and are taken as zero.
+  double dmax = 0.0;
+  for (int dd = 0; dd < 3; ++dd) {
+    const double* p = dxi + (size_t)(dd + 3 * dd) * nh;
+    for (size_t i = 0; i < nh; ++i) dmax = std::max(dmax, std::fabs(p[i]));
+  }
+  const double tol = 1e-10 * dmax;
   for (int m = 0; m < 3; ++m)
     for (int dd = 0; dd < 3; ++dd) {
       if (m == dd) continue;
       const double* p = dxi + (size_t)(dd + 3 * m) * nh;
       for (size_t i = 0; i < nh; ++i)
-        if (p[i] != 0.0)
+        if (std::fabs(p[i]) > tol)
           return fail(c, ASTR_ERR_UNSUPPORTED, "non-diagonal grid metrics are not supported");
     }
   const double* const src[3] = {dxi, dxi + 4 * nh, dxi + 8 * nh};
   return metrics_common(c, src, jacob);
+}
+
+int astr_gpu_set_grid(astr_ctx* c, const double* x) {
+  if (!c || !x) return fail(c, ASTR_ERR_ARG, "null argument");
+  if (!c->channel) return ASTR_OK;
+  const size_t nh = (size_t)c->g.nh;
+  const double* y = x + nh;  // x(..,2)
+  CK(cudaMemcpyAsync(c->ycoord, y, nh * 8, cudaMemcpyHostToDevice, c->st));
+  const long long NI = c->g.NI, NJ = c->g.NJ;
+  auto h = [&](int i, int j, int k) {
+    return (size_t)((i + HMD) + NI * ((j + HMD) + NJ * (long long)(k + HMD)));
+  };
+  c->chan_ly = y[h(0, c->g.jm, 0)] - y[h(0, 0, 0)];
+  CK(cudaStreamSynchronize(c->st));
+  c->grid_set = true;
+  return ASTR_OK;
+}
+
+int astr_gpu_channel_state(astr_ctx* c, double* out) {
+  if (!c || !out) return fail(c, ASTR_ERR_ARG, "null argument");
+  if (!c->channel) return fail(c, ASTR_ERR_STATE, "not a channel context");
+  double h[CHAN_N];
+  CK(cudaMemcpyAsync(h, c->chan_dev, sizeof(h), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  out[0] = h[CHAN_FORCE];
+  out[1] = h[CHAN_MASSFLUX];
+  out[2] = h[CHAN_TARGET];
+  out[3] = h[CHAN_FBCX];
+  out[4] = (double)c->nstep;
+  return ASTR_OK;
+}
+
+int astr_gpu_boucon(astr_ctx* c) {
+  if (!c) return fail(c, ASTR_ERR_ARG, "null context");
+  if (!c->channel) return ASTR_OK;
+  return c->prec == ASTR_FP64 ? run_noslip<double>(c) : run_noslip<float>(c);
 }
 
 int astr_gpu_set_metrics_diag(astr_ctx* c, const double* x11, const double* x22, const double* x33,
@@ -989,6 +1239,8 @@ static int ready(astr_ctx* c) {
   if (!c->metrics_set && c->pm.order == ASTR_ORDER_MAIN)
     return fail(c, ASTR_ERR_STATE, "metrics not set (astr_gpu_set_metrics)");
   if (!c->state_set) return fail(c, ASTR_ERR_STATE, "state not uploaded (astr_gpu_upload_state)");
+  if (c->channel && !c->grid_set)
+    return fail(c, ASTR_ERR_STATE, "channel grid not set (astr_gpu_set_grid)");
   return ASTR_OK;
 }
 

@@ -87,6 +87,17 @@ struct DevT {
   T* qf;            // 3 interior arrays
   double* part;     // statistics partial sums, 2 per warp
   int* flag;        // crash flag
+  const double* chan;  // channel controller state (CHAN_*), null unless a channel
+};
+
+// Channel controller state in device memory (FP64).
+enum {
+  CHAN_FORCE = 0,     // body force(1..3)
+  CHAN_UBULK = 3,     // bulk velocity (1..3), src_chan
+  CHAN_MASSFLUX = 6,  // massfluxchan of the last statcal
+  CHAN_FBCX = 7,      // fbcxchan of the last statcal
+  CHAN_TARGET = 8,    // target mass flux
+  CHAN_N = 16
 };
 
 struct Phys {
@@ -567,6 +578,15 @@ __device__ __forceinline__ void rk_update(const Geo& g, const DevT<T>& d, const 
   const double qv = q64(d, p, z, m, nh, n0);
   const double qs = d.qsave[m * n0 + z];
   double v;
+  if (d.chan) {
+    // src_chan (src/solver.F90:335-346): body force and its work, times J
+    const double* C = d.chan;
+    const double f = m == 0 ? 0.0
+                   : (m < 4 ? C[CHAN_FORCE + m - 1]
+                            : C[CHAN_FORCE] * C[CHAN_UBULK] + C[CHAN_FORCE + 1] * C[CHAN_UBULK + 1] +
+                                  C[CHAN_FORCE + 2] * C[CHAN_UBULK + 2]);
+    rhs = rhs + f * J;
+  }
   if (ph.mini) v = ph.rk1 * qs + ph.rk2 * qv + ph.rk3 * rhs * ph.dt;
   else v = (ph.rk1 * qs + ph.rk2 * qv * J + ph.rk3 * rhs * ph.dt) * rj;
   d.q[m * nh + p] = (T)v;

@@ -44,7 +44,8 @@ class GpuSolver:
     def __init__(self, im, jm, km, *, order=capi.ORDER_MAIN, precision=capi.FP64,
                  npdc=(3, 3, 3), lfilter=True, diffterm=True, alfa_filter=0.49,
                  beter_halo=1.11, beter_bound=0.98, mach=0.1, reynolds=1600.0, prandtl=0.72,
-                 ref_tem=273.15, suth_const=None, deltat=1e-3, ia=None, ja=None, ka=None):
+                 ref_tem=273.15, suth_const=None, deltat=1e-3, ia=None, ja=None, ka=None,
+                 channel=False, twall=1.0):
         L = capi.load()
         if suth_const is None:
             suth_const = 110.4 if order == capi.ORDER_MINIAPP else 110.3
@@ -53,7 +54,7 @@ class GpuSolver:
                                   km if ka is None else ka, *npdc)
         self.params = capi.AstrParams(order, precision, int(lfilter), int(diffterm), alfa_filter,
                                       beter_halo, beter_bound, mach, reynolds, prandtl, ref_tem,
-                                      suth_const, deltat)
+                                      suth_const, deltat, int(channel), twall)
         h = ctypes.c_void_p()
         rc = L.astr_gpu_create(ctypes.byref(self.dims), ctypes.byref(self.params), ctypes.byref(h))
         if rc != capi.ASTR_OK:
@@ -93,6 +94,22 @@ class GpuSolver:
         shp = halo_shape(self.im, self.jm, self.km)
         arrs = [_f(a, shp) for a in (dxi11, dxi22, dxi33, jacob)]
         self._c(self.L.astr_gpu_set_metrics_diag(self.h, *(capi.dptr(a) for a in arrs)))
+
+    def set_grid(self, x):
+        """Node coordinates x(-hm:..,1:3) (halo layout, Fortran order), or
+        the rectilinear node vectors (x, y, z) of the interior, which are
+        laid out with gridgeom's single-rank halo extension."""
+        if isinstance(x, (tuple, list)):
+            from .cases import grid_halo
+            x = grid_halo(*x)
+        x = _f(x, halo_shape(self.im, self.jm, self.km, 3))
+        self._c(self.L.astr_gpu_set_grid(self.h, capi.dptr(x)))
+
+    def channel_state(self):
+        """(force(1), mass flux, target mass flux, wall friction, steps)."""
+        out = np.zeros(5)
+        self._c(self.L.astr_gpu_channel_state(self.h, capi.dptr(out)))
+        return out
 
     def upload_state(self, q, rho, vel, prs, tmp):
         im, jm, km = self.im, self.jm, self.km
@@ -149,6 +166,9 @@ class GpuSolver:
 
     def rhscal(self):
         self._c(self.L.astr_gpu_rhscal(self.h))
+
+    def boucon(self):
+        self._c(self.L.astr_gpu_boucon(self.h))
 
     def updatefvar(self):
         self._c(self.L.astr_gpu_updatefvar(self.h))

@@ -64,6 +64,12 @@ typedef struct {
   double ref_tem;          /* reference temperature (Sutherland)           */
   double suth_const;       /* Sutherland constant (110.3 main, 110.4 mini-app) */
   double deltat;
+  int channel;             /* flowtype 'channel': noslip isothermal j-walls
+                              (boucon, src/bc.F90:327-409, 6423-6611), src_chan
+                              (src/solver.F90:295-353) and the mass-flux
+                              controller (src/statistic.F90:641-657, 1494-1533);
+                              needs npdcj = 4 and the grid (astr_gpu_set_grid) */
+  double twall;            /* isothermal wall temperature (twall, bctype 41) */
 } astr_params;
 
 typedef struct {
@@ -81,8 +87,27 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
 void astr_gpu_destroy(astr_ctx* ctx);
 
 /* Copy the grid metrics: dxi(-hm:..,1:3,1:3) and jacob(-hm:..) in Fortran
- * layout, as produced by gridgeom (src/geom.F90:99-930).  Host pointers. */
+ * layout, as produced by gridgeom (src/geom.F90:99-930).  Host pointers.
+ * The kernels take rectilinear (diagonal) metrics.  gridgeom's symmetric
+ * conservative form leaves rounding residue in the off-diagonals of a
+ * stretched rectilinear grid (about 1e-12 of the diagonal); off-diagonals
+ * no larger than 1e-10 of the largest diagonal entry are taken as zero, any
+ * larger one returns ASTR_ERR_UNSUPPORTED. */
 int astr_gpu_set_metrics(astr_ctx* ctx, const double* dxi, const double* jacob);
+
+/* Node coordinates x(-hm:..,1:3) in Fortran layout (gridgeom's x after its
+ * halo fill).  A channel context keeps the y coordinates for the bulk
+ * integrals of src_chan and massfluxchan; others ignore the call. */
+int astr_gpu_set_grid(astr_ctx* ctx, const double* x);
+
+/* boucon (src/bc.F90:327-409) for the per-routine drop-in: the noslip
+ * isothermal j-walls of a channel context; no-op otherwise. */
+int astr_gpu_boucon(astr_ctx* ctx);
+
+/* Channel controller state: out[0] force(1), out[1] mass flux and out[2]
+ * its target at the last statcal, out[3] wall friction (fbcxchan), out[4]
+ * completed time steps.  ASTR_ERR_STATE unless the context is a channel. */
+int astr_gpu_channel_state(astr_ctx* ctx, double* out5);
 
 /* Upload the conserved variables q(-hm:..,1:5) (halo layout) and the
  * primitive arrays rho, vel(..,1:3), prs, tmp (halo layout).  The
