@@ -302,7 +302,7 @@ def tgv_state(im, jm, km, mach=0.1, x=None, y=None, z=None):
     return _pack_state(im, jm, km, rho, u, v, w, p, T, q5)
 
 
-def vortex_fields(x, y, t=0.0, beta=5.0, gamma=1.4, half=5.0, uinf=(1.0, 1.0)):
+def vortex_fields(x, y, t=0.0, beta=5.0, gamma=1.4, half=5.0, uinf=(1.0, 1.0), mach=None):
     """Isentropic vortex of strength beta (Shu, NASA/CR-97-206253 / ICASE
     97-65, 1997, sec. 4.3.5; Yee, Sandham & Djomehri, JCP 150, 1999): on the
     periodic box [-half, half)^2 with freestream (u, v) = uinf, rho = p = T =
@@ -313,7 +313,11 @@ def vortex_fields(x, y, t=0.0, beta=5.0, gamma=1.4, half=5.0, uinf=(1.0, 1.0)):
         rho = T^(1/(gamma-1)),  p = rho T.
     In ASTR's nondimensional variables with mach = 1/sqrt(gamma), p_inf =
     1/(gamma mach^2) = 1 and T = p/rho * gamma mach^2 = p/rho, so these are
-    the solver's own rho, u, v, p, T."""
+    the solver's own rho, u, v, p, T.  For another reference Mach number M
+    (same velocity scale, T_inf = 1, p_inf = 1/(gamma M^2)) the radial
+    momentum balance of the isentropic vortex gives dT = -(gamma - 1) M^2
+    beta^2 / (8 pi^2) exp(1 - r^2), rho = T^(1/(gamma-1)), p = rho T /
+    (gamma M^2); M = 1/sqrt(gamma) is the form above."""
     L = 2.0 * half
     X = np.asarray(x).reshape(-1, 1)
     Y = np.asarray(y).reshape(1, -1)
@@ -323,9 +327,14 @@ def vortex_fields(x, y, t=0.0, beta=5.0, gamma=1.4, half=5.0, uinf=(1.0, 1.0)):
     e = np.exp(0.5 * (1.0 - r2))
     u = uinf[0] - beta / (2.0 * PI) * e * yb
     v = uinf[1] + beta / (2.0 * PI) * e * xb
-    T = 1.0 - (gamma - 1.0) * beta * beta / (8.0 * gamma * PI * PI) * e * e
-    rho = T ** (1.0 / (gamma - 1.0))
-    p = rho * T
+    if mach is None:
+        T = 1.0 - (gamma - 1.0) * beta * beta / (8.0 * gamma * PI * PI) * e * e
+        rho = T ** (1.0 / (gamma - 1.0))
+        p = rho * T
+    else:
+        T = 1.0 - (gamma - 1.0) * mach * mach * beta * beta / (8.0 * PI * PI) * e * e
+        rho = T ** (1.0 / (gamma - 1.0))
+        p = rho * T / (gamma * mach * mach)
     return rho, u, v, p, T
 
 
@@ -336,12 +345,14 @@ def vortex_grid(n, half=5.0):
     return x - half, y - half, z
 
 
-def vortex_state(n, t=0.0, beta=5.0, gamma=1.4, half=5.0):
+def vortex_state(n, t=0.0, beta=5.0, gamma=1.4, half=5.0, mach=None):
     """Halo-layout state (q, rho, vel, prs, tmp; km = 0) of the isentropic
-    vortex on the n^2 grid at time t, with interior nodes set."""
+    vortex on the n^2 grid at time t, with interior nodes set; mach None is
+    the classic form (mach = 1/sqrt(gamma))."""
     x, y, _ = vortex_grid(n, half)
-    rho, u, v, p, T = vortex_fields(x, y, t, beta, gamma, half)
-    mach = 1.0 / np.sqrt(gamma)
+    rho, u, v, p, T = vortex_fields(x, y, t, beta, gamma, half, mach=mach)
+    if mach is None:
+        mach = 1.0 / np.sqrt(gamma)
     c = refcal(mach, 1.0, gamma=gamma)
     rho3, u3, v3 = (a[:, :, None] for a in (rho, u, v))
     p3, T3 = p[:, :, None], T[:, :, None]

@@ -543,6 +543,9 @@ struct astr_ctx {
   double chan_ly = 0.0;         // ymax - ymin
   long long nstep = 0;          // completed time steps (statcal's nstep)
   bool rkfirst_called = false;  // rkfirst's firstcall flag
+  // one RK3 step captured as a CUDA graph (asynchronous stepping)
+  cudaGraphExec_t step_graph = nullptr;
+  long long graph_kernels = 0;  // kernel launches in one captured step
   std::vector<void*> allocs;
   // profiling: event pairs per launch, by kernel class
   bool prof = false;
@@ -1078,6 +1081,7 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
 void astr_gpu_destroy(astr_ctx* c) {
   if (!c) return;
   if (c->st) cudaStreamSynchronize(c->st);
+  if (c->step_graph) cudaGraphExecDestroy(c->step_graph);
   for (cudaEvent_t e : c->ev) cudaEventDestroy(e);
   for (void* p : c->allocs) cudaFree(p);
   if (c->st) cudaStreamDestroy(c->st);
@@ -1353,6 +1357,48 @@ int astr_gpu_timed_steps(astr_ctx* c, int nsteps, double* elapsed_ms) {
   cudaEventDestroy(e1);
   *elapsed_ms = ms;
   return rc;
+}
+
+int astr_gpu_step_async(astr_ctx* c, int nsteps) {
+  RC(ready(c));
+  if (nsteps < 0) return fail(c, ASTR_ERR_ARG, "nsteps < 0");
+  if (c->channel)
+    return fail(c, ASTR_ERR_UNSUPPORTED, "a channel step depends on host counters; use astr_gpu_rk3_step");
+  if (c->prof) return fail(c, ASTR_ERR_STATE, "profiling is on");
+  if (nsteps == 0) return ASTR_OK;
+  if (!c->step_graph) {
+    // capture one step (no statistics, no host synchronisation inside)
+    cudaGraph_t graph = nullptr;
+    const long long l0 = c->launches;
+    CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+    const int rc = step(c, nullptr);
+    const cudaError_t e = cudaStreamEndCapture(c->st, &graph);
+    c->nstep -= 1;  // the captured step has not run
+    if (rc != ASTR_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    CK(e);
+    const cudaError_t ei = cudaGraphInstantiate(&c->step_graph, graph, 0);
+    cudaGraphDestroy(graph);
+    CK(ei);
+    c->graph_kernels = c->launches - l0;
+    c->launches = l0;
+  }
+  for (int s = 0; s < nsteps; ++s) {
+    CK(cudaGraphLaunch(c->step_graph, c->st));
+    c->launches += c->graph_kernels;
+    c->nstep += 1;
+  }
+  return ASTR_OK;
+}
+
+int astr_gpu_poll(astr_ctx* c) {
+  if (!c) return fail(c, ASTR_ERR_ARG, "null context");
+  const cudaError_t e = cudaStreamQuery(c->st);
+  if (e == cudaSuccess) return 1;
+  if (e == cudaErrorNotReady) return 0;
+  return fail(c, ASTR_ERR_CUDA, std::string("astr_gpu_poll: ") + cudaGetErrorString(e));
 }
 
 int astr_gpu_set_profiling(astr_ctx* c, int on) {

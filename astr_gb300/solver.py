@@ -185,6 +185,18 @@ class GpuSolver:
         self._c(self.L.astr_gpu_timed_steps(self.h, int(nsteps), ctypes.byref(ms)))
         return ms.value
 
+    def step_async(self, nsteps: int):
+        """Enqueue nsteps RK3 steps (one CUDA graph launch each) and return
+        without waiting."""
+        self._c(self.L.astr_gpu_step_async(self.h, int(nsteps)))
+
+    def poll(self) -> bool:
+        """True when every enqueued step has finished."""
+        rc = self.L.astr_gpu_poll(self.h)
+        if rc < 0:
+            self._c(rc)
+        return rc == 1
+
     def set_profiling(self, on: bool):
         self._c(self.L.astr_gpu_set_profiling(self.h, int(on)))
 

@@ -612,6 +612,47 @@ def run_channel(args, rank, world, dist):
     return 0
 
 
+def run_serve(args, rank, world, dist):
+    """Serving: a Poisson stream of independent cases (3-D TGV / 2-D vortex,
+    50/50; edge log-uniform 32-192 / 64-1024; Re log-uniform 100-3000; Mach
+    uniform 0.05-0.3; steps uniform 50-500) at args.serve_rate per second,
+    the first args.serve_cases requests of the stream.  FP32-storage cases
+    under continuous batching (admission by slots and free HBM, every
+    admitted case's steps as graph launches on its own stream) against the
+    same requests solved one at a time in plain FP64."""
+    import torch  # noqa: F401  (CUDA context for the memory query)
+    from astr_gb300 import capi, serve
+    if rank != 0:
+        return 0
+    reqs = serve.make_requests(args.serve_cases, rate=args.serve_rate, seed=20261203)
+    free, total = torch.cuda.mem_get_info()
+    budget = int(0.8 * free)
+    be = serve.GpuBackend(capi.FP32_STORAGE)
+    srv = serve.Server(be, budget, max_active=args.serve_slots)
+    recs = serve.serve(reqs, srv)
+    batched = serve.summarize(reqs, recs)
+    batched.update({"peak_active": srv.peak_active, "peak_hbm_gb": round(srv.peak_used / 1e9, 2),
+                    "gpu_launches": srv.launches})
+    seq = serve.summarize(reqs, serve.serve_sequential(reqs, serve.GpuBackend(capi.FP64)))
+    work = sum(serve.request_points(q) * 3 * q.steps for q in reqs)
+    line = {
+        "case": "serve",
+        "workload": f"first {len(reqs)} requests of the seeded Poisson stream at "
+                    f"{args.serve_rate:g}/s (seed 20261203): TGV 3-D / vortex 2-D 50/50, edge "
+                    "log-U 32-192 / 64-1024, Re log-U 100-3000, Mach U(0.05,0.3), steps "
+                    "U{50..500}, CFL 0.5",
+        "offered_mpts_stages": round(work / 1e6, 1),
+        "continuous_batching_fp32_storage": batched,
+        "sequential_fp64": seq,
+        "hbm_budget_gb": round(budget / 1e9, 1), "slots": args.serve_slots,
+        "note": "time to solution = finish - arrival (wall clock, host-driven loop incl. case "
+                "set-up, upload and download); the offered load exceeds one GPU, so latency "
+                "includes queueing",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def ctypes_peak():
     import ctypes
     from astr_gb300 import capi
@@ -630,7 +671,10 @@ def main():
     ap.add_argument("--n", type=int, default=512)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--form", default="both", choices=["both", "fp64", "fp32_storage"])
-    ap.add_argument("--case", default="tgv", choices=["tgv", "vortex2d", "channel"])
+    ap.add_argument("--case", default="tgv", choices=["tgv", "vortex2d", "channel", "serve"])
+    ap.add_argument("--serve-cases", type=int, default=100)
+    ap.add_argument("--serve-rate", type=float, default=50.0)
+    ap.add_argument("--serve-slots", type=int, default=32)
     ap.add_argument("--channel-dims", type=int, nargs=3, default=[256, 192, 128])
     ap.add_argument("--channel-steps", type=int, default=500)
     ap.add_argument("--vortex-n", type=int, default=512)
@@ -647,6 +691,8 @@ def main():
         return run_vortex(args, rank, world, dist)
     if args.case == "channel":
         return run_channel(args, rank, world, dist)
+    if args.case == "serve":
+        return run_serve(args, rank, world, dist)
     if args.history:
         return run_history(args, rank, world, dist)
     return run_gpu(args, rank, world, dist)

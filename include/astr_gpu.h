@@ -100,6 +100,19 @@ int astr_gpu_set_metrics(astr_ctx* ctx, const double* dxi, const double* jacob);
  * integrals of src_chan and massfluxchan; others ignore the call. */
 int astr_gpu_set_grid(astr_ctx* ctx, const double* x);
 
+/* Asynchronous stepping (no counterpart in the reference; used by the
+ * request loop that serves many independent cases on one GPU): enqueue
+ * nsteps RK3 steps on the context's stream and return at once, without
+ * statistics.  The first call captures one step as a CUDA graph on the
+ * context's stream (no other work may be issued to that stream meanwhile);
+ * every step is then one graph launch.  Contexts on different streams run
+ * concurrently.  Not for channel contexts (their controller counts steps on
+ * the host). */
+int astr_gpu_step_async(astr_ctx* ctx, int nsteps);
+/* 1 when all work enqueued on the context has finished, 0 while it is in
+ * flight, < 0 on a CUDA error. */
+int astr_gpu_poll(astr_ctx* ctx);
+
 /* boucon (src/bc.F90:327-409) for the per-routine drop-in: the noslip
  * isothermal j-walls of a channel context; no-op otherwise. */
 int astr_gpu_boucon(astr_ctx* ctx);

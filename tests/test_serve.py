@@ -1,0 +1,77 @@
+"""Host-side tests of the serving loop: the request stream and the
+scheduler (first come first served, slots, HBM budget, continuous
+admission), against a simulated processor-sharing device."""
+import math
+
+import numpy as np
+import pytest
+
+from astr_gb300 import serve
+
+
+def test_request_stream():
+    reqs = serve.make_requests(2000, rate=50.0, seed=20261203)
+    assert [r.rid for r in reqs] == list(range(2000))
+    arr = np.array([r.arrival for r in reqs])
+    assert np.all(np.diff(arr) > 0)
+    assert abs(len(reqs) / arr[-1] - 50.0) < 5.0  # Poisson rate
+    n3 = [r.n for r in reqs if r.kind == "tgv3d"]
+    n2 = [r.n for r in reqs if r.kind == "vortex2d"]
+    assert 0.4 < len(n3) / len(reqs) < 0.6
+    assert min(n3) >= 32 and max(n3) <= 192 and min(n2) >= 64 and max(n2) <= 1024
+    # log-uniform edges: the median near the geometric mean
+    assert abs(math.log(np.median(n3)) - 0.5 * math.log(32 * 192)) < 0.15
+    assert all(100 <= r.reynolds <= 3000 and 0.05 <= r.mach <= 0.3 and 50 <= r.steps <= 500
+               for r in reqs)
+    again = serve.make_requests(2000, rate=50.0, seed=20261203)
+    assert again == reqs
+
+
+def _run(reqs, budget, slots, rate=1e6):
+    dev = serve.FakeDevice(rate=rate)
+    be = serve.FakeBackend(dev)
+    srv = serve.Server(be, budget, max_active=slots)
+    recs = serve.serve(reqs, srv, clock=serve.FakeClock(dev), poll_interval=1e-3)
+    return srv, be, recs
+
+
+def test_scheduler_fifo_budget_slots():
+    reqs = serve.make_requests(60, rate=50.0, seed=7, edge3d=(8, 24), edge2d=(16, 64),
+                               steps=(5, 20))
+    budget = int(max(serve.request_points(r) for r in reqs) * 100 * 3)
+    srv, be, recs = _run(reqs, budget, slots=4)
+    assert len(recs) == 60 and all(r.finished >= r.admitted >= r.arrival for r in recs)
+    assert be.started == sorted(be.started)  # admitted in arrival order
+    assert srv.peak_active <= 4 and srv.peak_used <= budget
+    assert srv.used == 0 and not srv.active
+
+
+def test_continuous_admission_overlaps_work():
+    # slow device: the second request arrives while the first is running and
+    # is admitted before the first finishes
+    reqs = [serve.Request(0, "tgv3d", 32, 1000.0, 0.1, 100, 0.0),
+            serve.Request(1, "vortex2d", 64, 1000.0, 0.1, 50, 0.05)]
+    srv, be, recs = _run(reqs, budget=10**12, slots=8, rate=2e6)
+    assert recs[1].admitted < recs[0].finished
+    # sharing the device: the first case takes longer than alone
+    alone = serve.request_points(reqs[0]) * 3 * reqs[0].steps / 2e6
+    assert recs[0].latency > alone
+
+
+def test_sequential_baseline_and_summary():
+    reqs = serve.make_requests(20, rate=50.0, seed=3, edge3d=(8, 16), edge2d=(16, 32),
+                               steps=(5, 10))
+    dev = serve.FakeDevice(rate=1e5)
+    recs = serve.serve_sequential(reqs, serve.FakeBackend(dev), clock=serve.FakeClock(dev),
+                                  poll_interval=1e-3)
+    for a, b in zip(recs, recs[1:]):
+        assert b.admitted >= a.finished - 1e-12
+    s = serve.summarize(reqs, recs)
+    assert s["cases"] == 20 and s["latency_p99_s"] >= s["latency_p50_s"] > 0
+
+
+def test_oversize_request_rejected():
+    dev = serve.FakeDevice()
+    srv = serve.Server(serve.FakeBackend(dev), hbm_budget=1000)
+    with pytest.raises(ValueError):
+        srv.submit(serve.Request(0, "tgv3d", 64, 100.0, 0.1, 10, 0.0))
