@@ -36,17 +36,20 @@ def _stale(obj: str, deps) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(verbose: bool = False, force: bool = False) -> str:
-    os.makedirs(BUILD, exist_ok=True)
+def build(verbose: bool = False, force: bool = False, out_dir: str = BUILD, defines=()) -> str:
+    """Compile (what is stale) and link; `out_dir` and `defines` (-D flags,
+    e.g. launch-shape constants) build a variant beside the default one."""
+    os.makedirs(out_dir, exist_ok=True)
+    lib = os.path.join(out_dir, "libastr_gb300.so")
     headers = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".cuh", ".h"))]
     headers.append(os.path.join(HERE, "..", "include", "astr_gpu.h"))
     objs, jobs = [], []
     for src in SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src.replace(".cu", ".o"))
+        o = os.path.join(out_dir, src.replace(".cu", ".o"))
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            cmd = [nvcc()] + ARCH + FLAGS + ["-c", s, "-o", o + ".tmp"]
+            cmd = [nvcc()] + ARCH + FLAGS + [f"-D{d}" for d in defines] + ["-c", s, "-o", o + ".tmp"]
             if verbose:
                 cmd.insert(1, "-Xptxas=-v")
             jobs.append((cmd, o))
@@ -64,11 +67,11 @@ def build(verbose: bool = False, force: bool = False) -> str:
             for out in ex.map(run, jobs):
                 if verbose and out:
                     sys.stderr.write(out)
-    if jobs or not os.path.exists(LIB):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs + ["-lcudart"]
+    if jobs or not os.path.exists(lib):
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", lib + ".tmp"] + objs + ["-lcudart"]
         subprocess.check_call(cmd)
-        os.replace(LIB + ".tmp", LIB)
-    return LIB
+        os.replace(lib + ".tmp", lib)
+    return lib
 
 
 if __name__ == "__main__":

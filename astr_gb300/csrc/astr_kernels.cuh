@@ -32,9 +32,26 @@
 namespace astr {
 
 constexpr int HMD = 5;       // halo width (src/commvar.F90:184)
-constexpr int NCH = 32;      // chunks per line
-constexpr int YZ_LINES = 16; // lines per block for y/z sweeps
-constexpr int X_LINES = 8;   // lines (warps) per block for x sweeps
+// Launch shape (lines per block, resident blocks per SM asked of the
+// compiler), chosen by timing the 512^3 TGV step: several smaller blocks
+// per SM overlap one block's loads with another's line solves.
+#ifndef ASTR_YZ_LINES
+#define ASTR_YZ_LINES 8
+#endif
+#ifndef ASTR_X_LINES
+#define ASTR_X_LINES 4
+#endif
+#ifndef ASTR_MINB_YZ
+#define ASTR_MINB_YZ 3
+#endif
+#ifndef ASTR_MINB_X
+#define ASTR_MINB_X 4
+#endif
+constexpr int NCH = 32;                // chunks per line
+constexpr int YZ_LINES = ASTR_YZ_LINES;  // lines per block for y/z sweeps
+constexpr int X_LINES = ASTR_X_LINES;    // lines (warps) per block for x sweeps
+constexpr int MINB_YZ = ASTR_MINB_YZ;    // resident blocks per SM asked of the compiler
+constexpr int MINB_X = ASTR_MINB_X;
 
 // One compact scheme (derivative or filter) of one direction, with the
 // chunk carry weights for the chunk length used on that direction.
@@ -379,38 +396,57 @@ __device__ __noinline__ T filter_special_row(const DScheme<T>& S, const FTab<T>&
   return r > 0 ? d * S.ac2[r] : d;
 }
 
-// Right-hand side of the compact filter (compact_filter_rhs,
-// src/filter.F90:156-285) for the rows of chunk c, scaled by ac2.  The
-// interior stencil uses FK[m] = c10i(m) * ac2 with the centre weight doubled
-// (the reference's f+f, exact).
+// The filter input of chunk c, loaded once: nodes first + c*CH - 5 ..
+// first + c*CH + CH + 4 into w.  A periodic line wraps nodes below 0 and
+// above dim onto the interior (as the reference's extended system reads
+// them); only the end chunks need that, the others read straight through.
+// Nodes no row of the chunk uses (rows past the system end) read as 0.
 template <int CH, typename T>
-__device__ __forceinline__ void filter_rhs(T (&y)[CH], const DScheme<T>& S, const FTab<T>& Tb,
-                                           int c, const T* v, long long base, long long hs,
-                                           int per) {
-  const int s = c * CH;
+__device__ __forceinline__ void filter_window(T (&w)[CH + 10], const DScheme<T>& S, int c,
+                                              const T* v, long long base, long long hs,
+                                              int per) {
   const int dim = S.dim;
-  auto f = [&](int node) -> T {
-    int nd = node;
-    if (per) nd = nd < 0 ? nd + dim : (nd > dim ? nd - dim : nd);
-    return v[base + hs * nd];
-  };
+  const int nb = S.first + c * CH - 5;
+  if (nb >= 0 && nb + CH + 9 <= dim) {
+    const T* p = v + base + hs * nb;
+#pragma unroll
+    for (int t = 0; t < CH + 10; ++t) w[t] = p[hs * t];
+  } else {
+#pragma unroll
+    for (int t = 0; t < CH + 10; ++t) {
+      int nd = nb + t;
+      if (per) nd = nd < 0 ? nd + dim : (nd > dim ? nd - dim : nd);
+      w[t] = (nd >= -HMD && nd <= dim + HMD) ? v[base + hs * nd] : T(0);
+    }
+  }
+}
+
+// Right-hand side of the compact filter (compact_filter_rhs,
+// src/filter.F90:156-285) for the rows of chunk c, scaled by ac2, from the
+// chunk's window w.  The interior stencil uses FK[m] = c10i(m) * ac2 with
+// the centre weight doubled (the reference's f+f, exact).
+template <int CH, typename T>
+__device__ __forceinline__ void filter_rhs(T (&y)[CH], const T (&w)[CH + 10], const DScheme<T>& S,
+                                           const FTab<T>& Tb, int c, const T* v, long long base,
+                                           long long hs, int per) {
+  const int s = c * CH;
   const T* FK = S.K;
   const int n = S.n;
 #pragma unroll
   for (int t = 0; t < CH; ++t) {
     const int r = s + t;
+    const T* W = w + t + 5;
     T d = T(0);
     if (r < n) {
       const bool special = S.ntype == 4 ? (r <= 4 || r >= n - 5) : (r <= 2 || r >= n - 3);
       if (special) {
         d = filter_special_row(S, Tb, r, v, base, hs, per);
       } else {
-        const int j = S.first + r;
-        d = __ldg(FK + r) * f(j) + __ldg(FK + n + r) * (f(j + 1) + f(j - 1)) +
-            __ldg(FK + 2 * n + r) * (f(j + 2) + f(j - 2)) +
-            __ldg(FK + 3 * n + r) * (f(j + 3) + f(j - 3)) +
-            __ldg(FK + 4 * n + r) * (f(j + 4) + f(j - 4)) +
-            __ldg(FK + 5 * n + r) * (f(j + 5) + f(j - 5));
+        d = __ldg(FK + r) * W[0] + __ldg(FK + n + r) * (W[1] + W[-1]) +
+            __ldg(FK + 2 * n + r) * (W[2] + W[-2]) +
+            __ldg(FK + 3 * n + r) * (W[3] + W[-3]) +
+            __ldg(FK + 4 * n + r) * (W[4] + W[-4]) +
+            __ldg(FK + 5 * n + r) * (W[5] + W[-5]);
       }
     }
     y[t] = d;
@@ -448,34 +484,29 @@ __device__ __noinline__ T filter_special_delta(const DScheme<T>& S, const FTab<T
 }
 
 template <int CH, typename T>
-__device__ __forceinline__ void filter_rhs_delta(T (&y)[CH], const DScheme<T>& S,
-                                                 const FTab<T>& Tb, int c, const T* v,
-                                                 long long base, long long hs, int per) {
+__device__ __forceinline__ void filter_rhs_delta(T (&y)[CH], const T (&w)[CH + 10],
+                                                 const DScheme<T>& S, const FTab<T>& Tb, int c,
+                                                 const T* v, long long base, long long hs,
+                                                 int per) {
   const int s = c * CH;
-  const int dim = S.dim;
-  auto f = [&](int node) -> T {
-    int nd = node;
-    if (per) nd = nd < 0 ? nd + dim : (nd > dim ? nd - dim : nd);
-    return v[base + hs * nd];
-  };
   const T* KD = S.KD;
   const int n = S.n;
 #pragma unroll
   for (int t = 0; t < CH; ++t) {
     const int r = s + t;
+    const T* W = w + t + 5;
     T d = T(0);
     if (r < n) {
       const bool special = S.ntype == 4 ? (r <= 4 || r >= n - 5) : (r <= 2 || r >= n - 3);
       if (special) {
         d = filter_special_delta(S, Tb, r, v, base, hs, per);
       } else {
-        const int j = S.first + r;
-        const T f0 = f(j);
-        d = __ldg(KD + r) * ((f(j + 1) - f0) + (f(j - 1) - f0)) +
-            __ldg(KD + n + r) * ((f(j + 2) - f0) + (f(j - 2) - f0)) +
-            __ldg(KD + 2 * n + r) * ((f(j + 3) - f0) + (f(j - 3) - f0)) +
-            __ldg(KD + 3 * n + r) * ((f(j + 4) - f0) + (f(j - 4) - f0)) +
-            __ldg(KD + 4 * n + r) * ((f(j + 5) - f0) + (f(j - 5) - f0));
+        const T f0 = W[0];
+        d = __ldg(KD + r) * ((W[1] - f0) + (W[-1] - f0)) +
+            __ldg(KD + n + r) * ((W[2] - f0) + (W[-2] - f0)) +
+            __ldg(KD + 2 * n + r) * ((W[3] - f0) + (W[-3] - f0)) +
+            __ldg(KD + 3 * n + r) * ((W[4] - f0) + (W[-4] - f0)) +
+            __ldg(KD + 4 * n + r) * ((W[5] - f0) + (W[-5] - f0));
       }
     }
     y[t] = d;

@@ -9,12 +9,14 @@ namespace astr {
 
 template <int DIR>
 constexpr int block_threads() { return DIR == 0 ? NCH * X_LINES : NCH * YZ_LINES; }
+template <int DIR>
+constexpr int min_blocks() { return DIR == 0 ? MINB_X : MINB_YZ; }
 
 // filterq (src/comsolver.F90:514-632): one direction, all five variables,
 // in place.  do_q2f (mini-app ordering, last direction): recover the
 // primitives of the filtered state.
 template <typename T, int DIR, int CH>
-__global__ void __launch_bounds__(block_threads<DIR>())
+__global__ void __launch_bounds__(block_threads<DIR>(), min_blocks<DIR>())
 k_filter(Geo g, DevT<T> d, DScheme<T> S, FTab<T> Tb, Phys ph, int do_q2f) {
   __shared__ T sm[SCAN_SMEM_WORDS];
   LineMap<DIR> lm(g);
@@ -34,17 +36,11 @@ k_filter(Geo g, DevT<T> d, DScheme<T> S, FTab<T> Tb, Phys ph, int do_q2f) {
     // increment added to the FP64 master so that none of it is lost below
     // the FP32 spacing of f.
     constexpr bool delta = sizeof(T) == 4;
+    T w[CH + 10];
+    filter_window<CH>(w, S, lm.c, v, base, hs, per);
     T y[CH];
-    if (delta) filter_rhs_delta<CH>(y, S, Tb, lm.c, v, base, hs, per);
-    else filter_rhs<CH>(y, S, Tb, lm.c, v, base, hs, per);
-    T fv[CH];
-    if (delta) {
-#pragma unroll
-      for (int t = 0; t < CH; ++t) {
-        const int node = S.first + lm.c * CH + t;
-        fv[t] = (node >= 0 && node <= dim) ? v[base + hs * node] : T(0);
-      }
-    }
+    if (delta) filter_rhs_delta<CH>(y, w, S, Tb, lm.c, v, base, hs, per);
+    else filter_rhs<CH>(y, w, S, Tb, lm.c, v, base, hs, per);
     chunk_solve<CH, DIR>(y, S, lm.c, sm);
     if (DIR == 0) __syncwarp();
     if (lm.active) {
@@ -60,7 +56,7 @@ k_filter(Geo g, DevT<T> d, DScheme<T> S, FTab<T> Tb, Phys ph, int do_q2f) {
             *M = nv;
             v[base + hs * node] = (T)nv;
           } else {
-            v[base + hs * node] = delta ? fv[t] + y[t] : y[t];
+            v[base + hs * node] = delta ? w[t + 5] + y[t] : y[t];
           }
         }
       }
@@ -78,7 +74,7 @@ k_filter(Geo g, DevT<T> d, DScheme<T> S, FTab<T> Tb, Phys ph, int do_q2f) {
 // convrsdcal6 (src/solver.F90:2173-2341) and gradcal
 // (src/comsolver.F90:244-497), one direction, diagonal metrics.
 template <typename T, int DIR, int CH>
-__global__ void __launch_bounds__(block_threads<DIR>())
+__global__ void __launch_bounds__(block_threads<DIR>(), min_blocks<DIR>())
 k_convgrad(Geo g, DevT<T> d, DScheme<T> S, Phys ph, CGFlags fl) {
   __shared__ T sm[SCAN_SMEM_WORDS];
   LineMap<DIR> lm(g);
@@ -231,7 +227,7 @@ k_convgrad(Geo g, DevT<T> d, DScheme<T> S, Phys ph, CGFlags fl) {
 // diffrsdcal6 sweeps (src/solver.F90:2619-2852), one direction.  The last
 // direction applies the RK3 update (and, main ordering, q2fvar).
 template <typename T, int DIR, int CH>
-__global__ void __launch_bounds__(block_threads<DIR>())
+__global__ void __launch_bounds__(block_threads<DIR>(), min_blocks<DIR>())
 k_visc(Geo g, DevT<T> d, DScheme<T> S, Phys ph, VFlags fl) {
   __shared__ T sm[SCAN_SMEM_WORDS];
   LineMap<DIR> lm(g);
