@@ -36,16 +36,16 @@ constexpr int HMD = 5;       // halo width (src/commvar.F90:184)
 // compiler), chosen by timing the 512^3 TGV step: several smaller blocks
 // per SM overlap one block's loads with another's line solves.
 #ifndef ASTR_YZ_LINES
-#define ASTR_YZ_LINES 8
+#define ASTR_YZ_LINES 16
 #endif
 #ifndef ASTR_X_LINES
 #define ASTR_X_LINES 4
 #endif
 #ifndef ASTR_MINB_YZ
-#define ASTR_MINB_YZ 3
+#define ASTR_MINB_YZ 2
 #endif
 #ifndef ASTR_MINB_X
-#define ASTR_MINB_X 4
+#define ASTR_MINB_X 6
 #endif
 constexpr int NCH = 32;                // chunks per line
 constexpr int YZ_LINES = ASTR_YZ_LINES;  // lines per block for y/z sweeps
