@@ -45,16 +45,16 @@ if ROOT not in sys.path:
 METRIC = "Mpts*RKstages/s (TGV 512^3, FP32 storage / FP64 accumulate, at stated error vs FP64)"
 UNIT = "Mpts*stages/s"
 
-# Algorithmic work of the FP64 form per interior point per launch, from the
-# reference's arithmetic with diagonal metrics (Thomas: 3 flops forward +
-# 2 backward per row; a divide or square root counts as one flop).
+# Algorithmic work per interior point per launch, from the reference's
+# arithmetic with diagonal metrics (Thomas: 3 flops forward + 2 backward per
+# row; a divide or square root counts as one flop).
 #   filter: RHS 17 + Thomas 5 per value, 5 variables
 #   convgrad: fluxes 14, 5 derivatives (RHS 5 + Thomas 5) + accumulate 5,
-#             4 gradients (10 + 1 metric multiply); the last direction adds
-#             the viscous stress and heat flux (48)
+#             4 gradients (10 + 1 metric multiply)
+#   point (k_sigma): viscous stress and heat flux at every point (48)
 #   visc: fluxes 8, 4 derivatives (40), accumulate 4; the last direction
 #         adds the RK3 update (40) and primitive recovery (14)
-FLOPS_PER_PT = {"filter": 110.0, "convgrad": 113.0, "convgrad_last": 161.0,
+FLOPS_PER_PT = {"filter": 110.0, "convgrad": 113.0, "pointwise": 48.0,
                 "visc": 52.0, "visc_last": 106.0}
 
 
@@ -64,9 +64,11 @@ def bytes_per_pt(kind, d, stage1, f32):
     m = FP64 word of the RK3 base, the FP32 form's master state and 1/J.
       filter: q 5 in, 5 out (FP32 form: + master 5 in, 5 out)
       convgrad x: q 5, u v w p T, dxi, J in; qrhs 5 + 4 gradients out;
-        stage 1 adds the RK3 base: qsave 5 out (FP32 form: + master 5 and
-        an FP64 J in); y adds qrhs 5 in; z adds 8 gradients in, stress 6 +
-        heat flux 3 out, stage 1 adds rho for the statistics
+        stage 1 adds the RK3 base: qsave 5 out (FP32 form: + master 5 and an
+        FP64 J in); y and z add qrhs 5 in; stage 1 z adds rho and 6
+        gradients in for the statistics
+      pointwise (k_sigma): 12 gradients, T, u v w in; stress 6 + heat flux
+        3 out
       visc x, y: stress 3 + heat flux 1, dxi, J, qrhs 4 in; qrhs 4 out
       visc z: stress/heat 4, dxi, J, qrhs 5, q 5 in, qsave 5 and 1/J (FP64)
         in; q 5 + primitives 6 out (FP32 form: + FP64 J, master 5 in, 5 out)
@@ -76,12 +78,14 @@ def bytes_per_pt(kind, d, stage1, f32):
     if kind == "filter":
         return 10 * w + (10 * m if f32 else 0.0)
     if kind == "convgrad":
-        b = [21 * w, 26 * w, 43 * w][d]
+        b = [21 * w, 26 * w, 26 * w][d]
         if stage1 and d == 0:
             b += 5 * m + (6 * m if f32 else 0.0)
         if stage1 and d == 2:
-            b += w
+            b += 7 * w
         return b
+    if kind == "pointwise":
+        return 25 * w
     if kind == "visc":
         if d < 2:
             return 14 * w
@@ -93,15 +97,16 @@ def bytes_per_pt(kind, d, stage1, f32):
 
 def class_work(kind, f32, launches, pts):
     """Algorithmic bytes and flops of `launches` launches of one kernel class
-    over whole RK3 steps (3 directions x 3 stages per step)."""
-    per_step_b = sum(bytes_per_pt(kind, d, s == 0, f32) for s in range(3) for d in range(3))
-    if kind == "filter":
-        per_step_f = 9 * FLOPS_PER_PT["filter"]
-    elif kind == "convgrad":
-        per_step_f = 3 * (2 * FLOPS_PER_PT["convgrad"] + FLOPS_PER_PT["convgrad_last"])
-    else:
+    over whole RK3 steps (per step: 3 stages x 3 directions, or 3 stages x 1
+    point launch)."""
+    dirs = (0,) if kind == "pointwise" else (0, 1, 2)
+    per_step_b = sum(bytes_per_pt(kind, d, s == 0, f32) for s in range(3) for d in dirs)
+    if kind == "visc":
         per_step_f = 3 * (2 * FLOPS_PER_PT["visc"] + FLOPS_PER_PT["visc_last"])
-    return per_step_b / 9.0 * pts * launches, per_step_f / 9.0 * pts * launches
+    else:
+        per_step_f = 3 * len(dirs) * FLOPS_PER_PT[kind]
+    n = 3 * len(dirs)
+    return per_step_b / n * pts * launches, per_step_f / n * pts * launches
 
 
 def env_int(name, default):
@@ -287,7 +292,7 @@ def state_error(q, ref):
 
 def form_roofline(kt, f32, pts_int, fp64_peak, hbm_peak):
     classes = {}
-    for k in ("filter", "convgrad", "visc"):
+    for k in ("filter", "convgrad", "pointwise", "visc"):
         tms, cnt = kt[k]
         if cnt == 0:
             continue
