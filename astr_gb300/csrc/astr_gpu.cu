@@ -528,6 +528,11 @@ struct astr_ctx {
   int CH[3] = {0, 0, 0};
   double* stats_dev = nullptr;
   double* staging = nullptr;  // nh doubles (FP32 form: host <-> device conversions)
+  double* staging2 = nullptr; // second buffer: copies overlap conversions
+  cudaStream_t cst = nullptr; // copy stream of the host <-> device transfers
+  cudaEvent_t ev_copy[2] = {nullptr, nullptr}, ev_use[2] = {nullptr, nullptr};
+  cudaEvent_t ev_begin = nullptr;  // the copy stream waits for the context stream
+  int xfer = 0;               // transfers issued through the double buffer
   double* jac64 = nullptr;
   double* rjac64 = nullptr;
   cudaStream_t st = nullptr;
@@ -860,14 +865,68 @@ int step(astr_ctx* c, double* stats) {
 // --- host <-> device in the storage precision ---------------------------
 size_t wsize(const astr_ctx* c) { return c->prec == ASTR_FP64 ? 8 : 4; }
 
+// Host <-> device transfers.  The FP64 form copies straight between host
+// arrays and fields on the context stream.  The FP32 form goes through two
+// FP64 staging buffers: the copy stream moves array k into (or out of)
+// buffer k%2 while the context stream converts the other one; events order
+// each buffer's copy against its conversion.
+
+// Start of a batch of transfers: the copy stream waits for every kernel
+// already queued on the context stream.
+int xfer_begin(astr_ctx* c) {
+  CK(cudaEventRecord(c->ev_begin, c->st));
+  CK(cudaStreamWaitEvent(c->cst, c->ev_begin, 0));
+  return ASTR_OK;
+}
+
+// Upload: host FP64 array -> staging buffer, ready for conversion on c->st.
+int xfer_in(astr_ctx* c, const double* src, size_t n, double** buf) {
+  const int b = c->xfer++ & 1;
+  *buf = b ? c->staging2 : c->staging;
+  CK(cudaStreamWaitEvent(c->cst, c->ev_use[b], 0));
+  CK(cudaMemcpyAsync(*buf, src, n * 8, cudaMemcpyHostToDevice, c->cst));
+  CK(cudaEventRecord(c->ev_copy[b], c->cst));
+  CK(cudaStreamWaitEvent(c->st, c->ev_copy[b], 0));
+  return ASTR_OK;
+}
+// After the conversion kernels that read (upload) or wrote (download) buf.
+int xfer_used(astr_ctx* c, const double* buf) {
+  const int b = buf == c->staging2 ? 1 : 0;
+  CK(cudaEventRecord(c->ev_use[b], c->st));
+  return ASTR_OK;
+}
+// Download: the next free staging buffer for conversions on c->st.
+int xfer_out_buf(astr_ctx* c, double** buf) {
+  const int b = c->xfer++ & 1;
+  *buf = b ? c->staging2 : c->staging;
+  CK(cudaStreamWaitEvent(c->st, c->ev_copy[b], 0));  // its previous copy-out is done
+  return ASTR_OK;
+}
+// Download: staging buffer (converted on c->st) -> host array on the copy stream.
+int xfer_out(astr_ctx* c, double* dst, const double* buf, size_t n) {
+  const int b = buf == c->staging2 ? 1 : 0;
+  CK(cudaEventRecord(c->ev_use[b], c->st));
+  CK(cudaStreamWaitEvent(c->cst, c->ev_use[b], 0));
+  CK(cudaMemcpyAsync(dst, buf, n * 8, cudaMemcpyDeviceToHost, c->cst));
+  CK(cudaEventRecord(c->ev_copy[b], c->cst));
+  return ASTR_OK;
+}
+int xfer_sync(astr_ctx* c) {
+  CK(cudaStreamSynchronize(c->cst));
+  CK(cudaStreamSynchronize(c->st));
+  return ASTR_OK;
+}
+
 int upload_array(astr_ctx* c, void* dst, const double* src, size_t n) {
   if (c->prec == ASTR_FP64) {
     CK(cudaMemcpyAsync(dst, src, n * 8, cudaMemcpyHostToDevice, c->st));
     return ASTR_OK;
   }
-  CK(cudaMemcpyAsync(c->staging, src, n * 8, cudaMemcpyHostToDevice, c->st));
-  k_to_float<<<point_grid((long long)n), 256, 0, c->st>>>(c->staging, (float*)dst, (long long)n);
-  return after_launch(c, "k_to_float");
+  double* buf = nullptr;
+  RC(xfer_in(c, src, n, &buf));
+  k_to_float<<<point_grid((long long)n), 256, 0, c->st>>>(buf, (float*)dst, (long long)n);
+  RC(after_launch(c, "k_to_float"));
+  return xfer_used(c, buf);
 }
 
 int download_array(astr_ctx* c, double* dst, const void* src, size_t n) {
@@ -875,11 +934,11 @@ int download_array(astr_ctx* c, double* dst, const void* src, size_t n) {
     CK(cudaMemcpyAsync(dst, src, n * 8, cudaMemcpyDeviceToHost, c->st));
     return ASTR_OK;
   }
-  k_to_double<<<point_grid((long long)n), 256, 0, c->st>>>((const float*)src, c->staging, (long long)n);
+  double* buf = nullptr;
+  RC(xfer_out_buf(c, &buf));
+  k_to_double<<<point_grid((long long)n), 256, 0, c->st>>>((const float*)src, buf, (long long)n);
   RC(after_launch(c, "k_to_double"));
-  CK(cudaMemcpyAsync(dst, c->staging, n * 8, cudaMemcpyDeviceToHost, c->st));
-  CK(cudaStreamSynchronize(c->st));  // the staging buffer is reused by the next call
-  return ASTR_OK;
+  return xfer_out(c, dst, buf, n);
 }
 
 template <typename T>
@@ -916,9 +975,9 @@ size_t astr_gpu_footprint(const astr_dims* dims, const astr_params* params) {
   const size_t w = f32 ? 4 : 8;
   // q 5, primitives 6, metrics 4 (halo arrays, storage type); 1/J (FP64);
   // qrhs 5, gradients 12, sigma 6, heat flux 3 (interior, storage type);
-  // qsave 5 (FP64); FP32 form: J, master q 5 and a staging array in FP64
+  // qsave 5 (FP64); FP32 form: J, master q 5 and two staging arrays in FP64
   size_t b = w * (15 * nh + 26 * n0) + 8 * (nh + 5 * n0);
-  if (f32) b += 8 * (2 * nh + 5 * n0);
+  if (f32) b += 8 * (3 * nh + 5 * n0);
   if (params && params->channel) b += 8 * nh;  // y coordinates
   return b;
 }
@@ -991,6 +1050,12 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
   c->ft32 = cast_ftab<float>(hft);
 
   cudaError_t e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->cst, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_begin, cudaEventDisableTiming);
+  for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
+    e = cudaEventCreateWithFlags(&c->ev_copy[b], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_use[b], cudaEventDisableTiming);
+  }
   if (e != cudaSuccess) {
     std::string m = std::string("cudaStreamCreate: ") + cudaGetErrorString(e);
     delete c;
@@ -1016,6 +1081,7 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
   double* qsave = (double*)alloc(5 * n0 * 8);
   double* qm = f32 ? (double*)alloc(5 * n0 * 8) : nullptr;
   c->staging = f32 ? (double*)alloc(nh * 8) : nullptr;
+  c->staging2 = f32 ? (double*)alloc(nh * 8) : nullptr;
   c->jac64 = f32 ? (double*)alloc(nh * 8) : (double*)jac;
   c->rjac64 = (double*)alloc(nh * 8);
   long long nw = std::max(sweep_warps<0>(g), std::max(sweep_warps<1>(g), sweep_warps<2>(g)));
@@ -1102,17 +1168,26 @@ void astr_gpu_destroy(astr_ctx* c) {
   if (!c) return;
   if (c->st) cudaStreamSynchronize(c->st);
   if (c->step_graph) cudaGraphExecDestroy(c->step_graph);
+  if (c->cst) cudaStreamSynchronize(c->cst);
+  for (int b = 0; b < 2; ++b) {
+    if (c->ev_copy[b]) cudaEventDestroy(c->ev_copy[b]);
+    if (c->ev_use[b]) cudaEventDestroy(c->ev_use[b]);
+  }
+  if (c->ev_begin) cudaEventDestroy(c->ev_begin);
   for (cudaEvent_t e : c->ev) cudaEventDestroy(e);
   for (void* p : c->allocs) cudaFree(p);
   if (c->st) cudaStreamDestroy(c->st);
+  if (c->cst) cudaStreamDestroy(c->cst);
   delete c;
 }
 
 static int metrics_common(astr_ctx* c, const double* const src[3], const double* jacob) {
   const size_t nh = (size_t)c->g.nh, w = wsize(c);
   char* xd = (char*)c->d64.xd;
+  RC(xfer_begin(c));
   for (int dd = 0; dd < 3; ++dd) RC(upload_array(c, xd + dd * nh * w, src[dd], nh));
   RC(upload_array(c, (void*)c->d64.jac, jacob, nh));
+  RC(xfer_sync(c));
   if (c->prec == ASTR_FP32_STORAGE)
     CK(cudaMemcpyAsync(c->jac64, jacob, nh * 8, cudaMemcpyHostToDevice, c->st));
   k_reciprocal<<<point_grid((long long)nh), 256, 0, c->st>>>(c->jac64, c->rjac64, (long long)nh);
@@ -1195,20 +1270,27 @@ int astr_gpu_upload_state(astr_ctx* c, const double* q, const double* rho, const
   const size_t nh = (size_t)c->g.nh, w = wsize(c);
   char* dq = (char*)c->d64.q;
   char* dp = (char*)c->d64.pr;
+  RC(xfer_begin(c));
   for (int m = 0; m < 5; ++m) {
-    RC(upload_array(c, dq + m * nh * w, q + m * nh, nh));
-    if (c->prec == ASTR_FP32_STORAGE) {
+    if (c->prec == ASTR_FP64) {
+      RC(upload_array(c, dq + m * nh * w, q + m * nh, nh));
+    } else {
+      double* buf = nullptr;
+      RC(xfer_in(c, q + m * nh, nh, &buf));
+      k_to_float<<<point_grid((long long)nh), 256, 0, c->st>>>(buf, (float*)(dq + m * nh * w),
+                                                                 (long long)nh);
+      RC(after_launch(c, "k_to_float"));
       // the FP64 master takes the uploaded interior values directly
-      k_halo_to_interior<<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, c->staging,
-                                                                 c->d32.qm + m * c->g.n0);
+      k_halo_to_interior<<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, buf, c->d32.qm + m * c->g.n0);
       RC(after_launch(c, "k_halo_to_interior"));
+      RC(xfer_used(c, buf));
     }
   }
   RC(upload_array(c, dp, rho, nh));
   for (int m = 0; m < 3; ++m) RC(upload_array(c, dp + (1 + m) * nh * w, vel + m * nh, nh));
   RC(upload_array(c, dp + 4 * nh * w, prs, nh));
   RC(upload_array(c, dp + 5 * nh * w, tmp, nh));
-  CK(cudaStreamSynchronize(c->st));
+  RC(xfer_sync(c));
   c->state_set = true;
   return ASTR_OK;
 }
@@ -1218,20 +1300,21 @@ int astr_gpu_download_state(astr_ctx* c, double* q, double* rho, double* vel, do
   const size_t nh = (size_t)c->g.nh, w = wsize(c);
   const char* dq = (const char*)c->d64.q;
   const char* dp = (const char*)c->d64.pr;
+  RC(xfer_begin(c));
   if (q) {
     for (int m = 0; m < 5; ++m) {
       if (c->prec == ASTR_FP64) {
-        CK(cudaMemcpyAsync(q + m * nh, dq + m * nh * w, nh * 8, cudaMemcpyDeviceToHost, c->st));
+        RC(download_array(c, q + m * nh, dq + m * nh * w, nh));
       } else {
         // halos from the FP32 copy, interior from the FP64 master
+        double* buf = nullptr;
+        RC(xfer_out_buf(c, &buf));
         k_to_double<<<point_grid((long long)nh), 256, 0, c->st>>>((const float*)(dq + m * nh * w),
-                                                                   c->staging, (long long)nh);
+                                                                   buf, (long long)nh);
         RC(after_launch(c, "k_to_double"));
-        k_master_to_halo<<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, c->d32.qm + m * c->g.n0,
-                                                                 c->staging);
+        k_master_to_halo<<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, c->d32.qm + m * c->g.n0, buf);
         RC(after_launch(c, "k_master_to_halo"));
-        CK(cudaMemcpyAsync(q + m * nh, c->staging, nh * 8, cudaMemcpyDeviceToHost, c->st));
-        CK(cudaStreamSynchronize(c->st));
+        RC(xfer_out(c, q + m * nh, buf, nh));
       }
     }
   }
@@ -1240,13 +1323,13 @@ int astr_gpu_download_state(astr_ctx* c, double* q, double* rho, double* vel, do
     for (int m = 0; m < 3; ++m) RC(download_array(c, vel + m * nh, dp + (1 + m) * nh * w, nh));
   if (prs) RC(download_array(c, prs, dp + 4 * nh * w, nh));
   if (tmp) RC(download_array(c, tmp, dp + 5 * nh * w, nh));
-  CK(cudaStreamSynchronize(c->st));
-  return ASTR_OK;
+  return xfer_sync(c);
 }
 
 int astr_gpu_download_rhs(astr_ctx* c, double* qrhs, double* dvel, double* dtmp) {
   if (!c) return fail(c, ASTR_ERR_ARG, "null context");
   const size_t n0 = (size_t)c->g.n0, w = wsize(c);
+  RC(xfer_begin(c));
   if (qrhs)
     for (int m = 0; m < 5; ++m) RC(download_array(c, qrhs + m * n0, (char*)c->d64.qrhs + m * n0 * w, n0));
   if (dvel)
@@ -1254,8 +1337,7 @@ int astr_gpu_download_rhs(astr_ctx* c, double* qrhs, double* dvel, double* dtmp)
   if (dtmp)
     for (int m = 0; m < 3; ++m)
       RC(download_array(c, dtmp + m * n0, (char*)c->d64.grad + (9 + m) * n0 * w, n0));
-  CK(cudaStreamSynchronize(c->st));
-  return ASTR_OK;
+  return xfer_sync(c);
 }
 
 static int ready(astr_ctx* c) {
