@@ -366,6 +366,32 @@ struct HostScheme {
   int first = 0, n = 0, ntype = 3, dim = 0;
   bool filter = false;
   std::vector<double> a, c, ac1, ac2, ac3, G, H, K, KD;
+  int ulo = 1, uhi = 0;  // uniform chunks (empty range by default)
+  double u_ac1 = 0.0, u_ac3 = 0.0, u_K[6] = {0, 0, 0, 0, 0, 0}, u_KD[5] = {0, 0, 0, 0, 0};
+
+  // Chunks whose rows all carry the steady Thomas factors bit for bit and
+  // no boundary row (derivative: row 0, n-1, and with walls 1, n-2; filter:
+  // 3 end rows, 5 with walls).
+  void find_uniform(int CH) {
+    const int spec = filter ? (ntype == 4 ? 5 : 3) : (ntype == 4 ? 2 : 1);
+    const int m = n / 2;
+    if (m < spec || m > n - 1 - spec) return;
+    auto same = [&](int r) {
+      return ac1[r] == ac1[m] && ac2[r] == ac2[m] && ac3[r] == ac3[m] && a[r] == a[m] &&
+             c[r] == c[m];
+    };
+    int rlo = m, rhi = m;
+    while (rlo - 1 >= spec && same(rlo - 1)) --rlo;
+    while (rhi + 1 <= n - 1 - spec && same(rhi + 1)) ++rhi;
+    ulo = (rlo + CH - 1) / CH;
+    uhi = (rhi + 1) / CH - 1;
+    u_ac1 = ac1[m];
+    u_ac3 = ac3[m];
+    const int nk = filter ? 6 : 2;
+    for (int j = 0; j < nk; ++j) u_K[j] = K[(size_t)j * n + m];
+    if (filter)
+      for (int j = 0; j < 5; ++j) u_KD[j] = KD[(size_t)j * n + m];
+  }
   void finish(int CH, const HostFTab& t) {
     ac1.assign(n, 0.0); ac2.assign(n, 0.0); ac3.assign(n, 0.0);
     ac1[0] = c[0];
@@ -400,6 +426,7 @@ struct HostScheme {
         K[n + r] = H_NUM1D36 * ac2[r];
       }
     }
+    find_uniform(CH);
   }
 };
 
@@ -1134,6 +1161,11 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
     d4.K = coef32 + off + 6 * n; d4.KD = nkd ? coef32 + off + 6 * n + nk : nullptr;
     d8.n = d4.n = s.n; d8.first = d4.first = s.first; d8.ntype = d4.ntype = s.ntype;
     d8.dim = d4.dim = s.dim;
+    d8.ulo = d4.ulo = s.ulo; d8.uhi = d4.uhi = s.uhi;
+    d8.u_ac1 = s.u_ac1; d8.u_ac3 = s.u_ac3;
+    d4.u_ac1 = (float)s.u_ac1; d4.u_ac3 = (float)s.u_ac3;
+    for (int j = 0; j < 6; ++j) { d8.u_K[j] = s.u_K[j]; d4.u_K[j] = (float)s.u_K[j]; }
+    for (int j = 0; j < 5; ++j) { d8.u_KD[j] = s.u_KD[j]; d4.u_KD[j] = (float)s.u_KD[j]; }
     if (idx % 2 == 0) { c->fd64[idx / 2] = d8; c->fd32[idx / 2] = d4; }
     else { c->fl64[idx / 2] = d8; c->fl32[idx / 2] = d4; }
     off += len;

@@ -20,6 +20,7 @@ __global__ void __launch_bounds__(block_threads<DIR>(), min_blocks<DIR>())
 k_filter(Geo g, DevT<T> d, DScheme<T> S, FTab<T> Tb, Phys ph, int do_q2f) {
   __shared__ T sm[SCAN_SMEM_WORDS];
   LineMap<DIR> lm(g);
+  const bool uni = uniform_chunk<DIR>(S, lm.c);
   if (DIR == 0 && !lm.active) return;  // whole warp: x-lines own a warp
   const long long hs = hstride<DIR>(g);
   int i0, j0, k0;
@@ -39,9 +40,9 @@ k_filter(Geo g, DevT<T> d, DScheme<T> S, FTab<T> Tb, Phys ph, int do_q2f) {
     T w[CH + 10];
     filter_window<CH>(w, S, lm.c, v, base, hs, per);
     T y[CH];
-    if (delta) filter_rhs_delta<CH>(y, w, S, Tb, lm.c, v, base, hs, per);
-    else filter_rhs<CH>(y, w, S, Tb, lm.c, v, base, hs, per);
-    chunk_solve<CH, DIR>(y, S, lm.c, sm);
+    if (delta) filter_rhs_delta<CH>(y, w, S, Tb, lm.c, v, base, hs, per, uni);
+    else filter_rhs<CH>(y, w, S, Tb, lm.c, v, base, hs, per, uni);
+    chunk_solve<CH, DIR>(y, S, lm.c, sm, uni);
     if (DIR == 0) __syncwarp();
     if (lm.active) {
 #pragma unroll
@@ -78,6 +79,7 @@ __global__ void __launch_bounds__(block_threads<DIR>(), min_blocks<DIR>())
 k_convgrad(Geo g, DevT<T> d, DScheme<T> S, Phys ph, CGFlags fl) {
   __shared__ T sm[SCAN_SMEM_WORDS];
   LineMap<DIR> lm(g);
+  const bool uni = uniform_chunk<DIR>(S, lm.c);
   if (DIR == 0 && !lm.active) {  // whole warp: x-lines own a warp
     if (fl.stats && threadIdx.x == 0) {
       const long long wid = (long long)blockIdx.x * X_LINES + threadIdx.y;
@@ -123,8 +125,8 @@ k_convgrad(Geo g, DevT<T> d, DScheme<T> S, Phys ph, CGFlags fl) {
         return J * (qn * uu);
       };
       T y[CH];
-      deriv_rhs<CH>(y, S, lm.c, f);
-      chunk_solve<CH, DIR>(y, S, lm.c, sm);
+      deriv_rhs<CH>(y, S, lm.c, f, uni);
+      chunk_solve<CH, DIR>(y, S, lm.c, sm, uni);
       if (lm.active) {
 #pragma unroll
         for (int t = 0; t < CH; ++t) {
@@ -147,8 +149,8 @@ k_convgrad(Geo g, DevT<T> d, DScheme<T> S, Phys ph, CGFlags fl) {
       const T* src = d.pr + (n < 3 ? 1 + n : 5) * nh;
       auto f = [&](int node) -> T { return src[bh + hs * node]; };
       T y[CH];
-      deriv_rhs<CH>(y, S, lm.c, f);
-      chunk_solve<CH, DIR>(y, S, lm.c, sm);
+      deriv_rhs<CH>(y, S, lm.c, f, uni);
+      chunk_solve<CH, DIR>(y, S, lm.c, sm, uni);
       const int comp = n < 3 ? n + 3 * DIR : 9 + DIR;
       if (lm.active) {
 #pragma unroll
@@ -231,6 +233,7 @@ __global__ void __launch_bounds__(block_threads<DIR>(), min_blocks<DIR>())
 k_visc(Geo g, DevT<T> d, DScheme<T> S, Phys ph, VFlags fl) {
   __shared__ T sm[SCAN_SMEM_WORDS];
   LineMap<DIR> lm(g);
+  const bool uni = uniform_chunk<DIR>(S, lm.c);
   if (DIR == 0 && !lm.active) return;  // whole warp: x-lines own a warp
   const long long hs = hstride<DIR>(g), zs = zstride<DIR>(g);
   int i0, j0, k0;
@@ -260,8 +263,8 @@ k_visc(Geo g, DevT<T> d, DScheme<T> S, Phys ph, VFlags fl) {
       return (sv * xd[p]) * d.jac[p];
     };
     T y[CH];
-    deriv_rhs<CH>(y, S, lm.c, f);
-    chunk_solve<CH, DIR>(y, S, lm.c, sm);
+    deriv_rhs<CH>(y, S, lm.c, f, uni);
+    chunk_solve<CH, DIR>(y, S, lm.c, sm, uni);
     if (lm.active) {
 #pragma unroll
       for (int t = 0; t < CH; ++t) {
