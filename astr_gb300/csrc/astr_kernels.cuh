@@ -175,14 +175,21 @@ __device__ __forceinline__ void line_ijk(int a, int b, int l, int& i, int& j, in
   else { i = a; j = b; k = l; }
 }
 
+// Line layout.  x sweeps with XB false hold one line per warp (lane = chunk,
+// shuffle scans); every other sweep uses blocks of YZ_LINES lines x 32
+// chunks with shared-memory scans (XB: the x filter, measured faster that
+// way; the x derivative sweeps are faster one line per warp).
+template <int DIR, bool XB = false>
+constexpr bool warp_lines() { return DIR == 0 && !XB; }
+
 // Thread -> (line, chunk) mapping.  Threads past the last line still take
 // part in block-wide synchronisation (y/z); x-line warps past the end exit.
-template <int DIR>
+template <int DIR, bool XB = false>
 struct LineMap {
   int a, b, c;
   bool active;
   __device__ __forceinline__ LineMap(const Geo& g) {
-    if (DIR == 0) {
+    if (warp_lines<DIR, XB>()) {
       c = threadIdx.x;
       const long long line = (long long)blockIdx.x * X_LINES + threadIdx.y;
       const long long na = g.jm + 1, nl = na * (g.km + 1);
@@ -192,9 +199,10 @@ struct LineMap {
       b = (int)(L / na);
     } else {
       c = threadIdx.y;
+      const int amax = DIR == 0 ? g.jm : g.im;
       const int ai = blockIdx.x * YZ_LINES + threadIdx.x;
-      active = ai <= g.im;
-      a = active ? ai : g.im;
+      active = ai <= amax;
+      a = active ? ai : amax;
       b = blockIdx.y;
     }
   }
@@ -276,14 +284,14 @@ __device__ __forceinline__ T scan_block(T M, T L, T* sm) {
 // Taken by the FP32 sweeps only: in the FP64 ones the second code path
 // costs more in registers (64 per thread) than the loads it saves (3 %
 // slower on the 512^3 step, 7 % faster in FP32).
-template <int DIR, typename T>
+template <int DIR, bool XB, typename T>
 __device__ __forceinline__ bool uniform_chunk(const DScheme<T>& S, int c) {
-  return sizeof(T) == 4 && DIR != 0 && c >= S.ulo && c <= S.uhi;
+  return sizeof(T) == 4 && !warp_lines<DIR, XB>() && c >= S.ulo && c <= S.uhi;
 }
 
 // In: y[t] = ac2-scaled right-hand side of row c*CH+t (row 0 unscaled).
 // Out: y[t] = solution.
-template <int CH, int DIR, typename T>
+template <int CH, int DIR, bool XB, typename T>
 __device__ __forceinline__ void chunk_solve(T (&y)[CH], const DScheme<T>& S, int c, T* sm,
                                             bool uni) {
   const int s = c * CH;
@@ -307,7 +315,7 @@ __device__ __forceinline__ void chunk_solve(T (&y)[CH], const DScheme<T>& S, int
       }
     }
   }
-  const T Yp = (DIR == 0) ? scan_fwd_warp(M, L, c) : scan_block<true>(M, L, sm);
+  const T Yp = warp_lines<DIR, XB>() ? scan_fwd_warp(M, L, c) : scan_block<true>(M, L, sm);
   if (uni) {
     const T a3 = S.u_ac3;
     T gw = T(1);
@@ -342,7 +350,7 @@ __device__ __forceinline__ void chunk_solve(T (&y)[CH], const DScheme<T>& S, int
       Mb = __ldg(S.H + s);
     }
   }
-  const T Xn = (DIR == 0) ? scan_bwd_warp(Mb, Lb, c) : scan_block<false>(Mb, Lb, sm);
+  const T Xn = warp_lines<DIR, XB>() ? scan_bwd_warp(Mb, Lb, c) : scan_block<false>(Mb, Lb, sm);
   if (uni) {
     const T a1 = S.u_ac1;
     T hw = T(1);

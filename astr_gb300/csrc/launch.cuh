@@ -6,17 +6,20 @@
 
 namespace astr {
 
-template <int DIR>
-inline dim3 sweep_block() { return DIR == 0 ? dim3(NCH, X_LINES) : dim3(YZ_LINES, NCH); }
+template <int DIR, bool XB = false>
+inline dim3 sweep_block() { return warp_lines<DIR, XB>() ? dim3(NCH, X_LINES) : dim3(YZ_LINES, NCH); }
 
-template <int DIR>
+template <int DIR, bool XB = false>
 inline dim3 sweep_grid(const Geo& g) {
-  if (DIR == 0) {
+  if (warp_lines<DIR, XB>()) {
     long long nl = (long long)(g.jm + 1) * (g.km + 1);
     return dim3((unsigned)((nl + X_LINES - 1) / X_LINES), 1);
   }
-  const unsigned gx = (unsigned)((g.im + YZ_LINES) / YZ_LINES);
-  return dim3(gx, DIR == 1 ? g.km + 1 : g.jm + 1);
+  // lines: a = i (y, z sweeps) or j (x sweeps) across the block, b = the
+  // remaining transverse index across blockIdx.y
+  const int amax = DIR == 0 ? g.jm : g.im;
+  const unsigned gx = (unsigned)((amax + YZ_LINES) / YZ_LINES);
+  return dim3(gx, DIR == 1 ? g.km + 1 : (DIR == 0 ? g.km + 1 : g.jm + 1));
 }
 
 template <typename T, int DIR>

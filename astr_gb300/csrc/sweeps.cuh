@@ -7,21 +7,21 @@
 
 namespace astr {
 
-template <int DIR>
-constexpr int block_threads() { return DIR == 0 ? NCH * X_LINES : NCH * YZ_LINES; }
-template <int DIR>
-constexpr int min_blocks() { return DIR == 0 ? MINB_X : MINB_YZ; }
+template <int DIR, bool XB = false>
+constexpr int block_threads() { return warp_lines<DIR, XB>() ? NCH * X_LINES : NCH * YZ_LINES; }
+template <int DIR, bool XB = false>
+constexpr int min_blocks() { return warp_lines<DIR, XB>() ? MINB_X : MINB_YZ; }
 
 // filterq (src/comsolver.F90:514-632): one direction, all five variables,
 // in place.  do_q2f (mini-app ordering, last direction): recover the
 // primitives of the filtered state.
 template <typename T, int DIR, int CH>
-__global__ void __launch_bounds__(block_threads<DIR>(), min_blocks<DIR>())
+__global__ void __launch_bounds__(block_threads<DIR, true>(), min_blocks<DIR, true>())
 k_filter(Geo g, DevT<T> d, DScheme<T> S, FTab<T> Tb, Phys ph, int do_q2f) {
   __shared__ T sm[SCAN_SMEM_WORDS];
-  LineMap<DIR> lm(g);
-  const bool uni = uniform_chunk<DIR>(S, lm.c);
-  if (DIR == 0 && !lm.active) return;  // whole warp: x-lines own a warp
+  LineMap<DIR, true> lm(g);
+  const bool uni = uniform_chunk<DIR, true>(S, lm.c);
+  if (warp_lines<DIR, true>() && !lm.active) return;  // whole warp: x-lines own a warp
   const long long hs = hstride<DIR>(g);
   int i0, j0, k0;
   line_ijk<DIR>(lm.a, lm.b, 0, i0, j0, k0);
@@ -42,8 +42,8 @@ k_filter(Geo g, DevT<T> d, DScheme<T> S, FTab<T> Tb, Phys ph, int do_q2f) {
     T y[CH];
     if (delta) filter_rhs_delta<CH>(y, w, S, Tb, lm.c, v, base, hs, per, uni);
     else filter_rhs<CH>(y, w, S, Tb, lm.c, v, base, hs, per, uni);
-    chunk_solve<CH, DIR>(y, S, lm.c, sm, uni);
-    if (DIR == 0) __syncwarp();
+    chunk_solve<CH, DIR, true>(y, S, lm.c, sm, uni);
+    if (warp_lines<DIR, true>()) __syncwarp();
     if (lm.active) {
 #pragma unroll
       for (int t = 0; t < CH; ++t) {
@@ -79,8 +79,8 @@ __global__ void __launch_bounds__(block_threads<DIR>(), min_blocks<DIR>())
 k_convgrad(Geo g, DevT<T> d, DScheme<T> S, Phys ph, CGFlags fl) {
   __shared__ T sm[SCAN_SMEM_WORDS];
   LineMap<DIR> lm(g);
-  const bool uni = uniform_chunk<DIR>(S, lm.c);
-  if (DIR == 0 && !lm.active) {  // whole warp: x-lines own a warp
+  const bool uni = uniform_chunk<DIR, false>(S, lm.c);
+  if (warp_lines<DIR>() && !lm.active) {  // whole warp: x-lines own a warp
     if (fl.stats && threadIdx.x == 0) {
       const long long wid = (long long)blockIdx.x * X_LINES + threadIdx.y;
       d.part[2 * wid] = 0.0;
@@ -126,7 +126,7 @@ k_convgrad(Geo g, DevT<T> d, DScheme<T> S, Phys ph, CGFlags fl) {
       };
       T y[CH];
       deriv_rhs<CH>(y, S, lm.c, f, uni);
-      chunk_solve<CH, DIR>(y, S, lm.c, sm, uni);
+      chunk_solve<CH, DIR, false>(y, S, lm.c, sm, uni);
       if (lm.active) {
 #pragma unroll
         for (int t = 0; t < CH; ++t) {
@@ -150,7 +150,7 @@ k_convgrad(Geo g, DevT<T> d, DScheme<T> S, Phys ph, CGFlags fl) {
       auto f = [&](int node) -> T { return src[bh + hs * node]; };
       T y[CH];
       deriv_rhs<CH>(y, S, lm.c, f, uni);
-      chunk_solve<CH, DIR>(y, S, lm.c, sm, uni);
+      chunk_solve<CH, DIR, false>(y, S, lm.c, sm, uni);
       const int comp = n < 3 ? n + 3 * DIR : 9 + DIR;
       if (lm.active) {
 #pragma unroll
@@ -233,8 +233,8 @@ __global__ void __launch_bounds__(block_threads<DIR>(), min_blocks<DIR>())
 k_visc(Geo g, DevT<T> d, DScheme<T> S, Phys ph, VFlags fl) {
   __shared__ T sm[SCAN_SMEM_WORDS];
   LineMap<DIR> lm(g);
-  const bool uni = uniform_chunk<DIR>(S, lm.c);
-  if (DIR == 0 && !lm.active) return;  // whole warp: x-lines own a warp
+  const bool uni = uniform_chunk<DIR, false>(S, lm.c);
+  if (warp_lines<DIR>() && !lm.active) return;  // whole warp: x-lines own a warp
   const long long hs = hstride<DIR>(g), zs = zstride<DIR>(g);
   int i0, j0, k0;
   line_ijk<DIR>(lm.a, lm.b, 0, i0, j0, k0);
@@ -264,7 +264,7 @@ k_visc(Geo g, DevT<T> d, DScheme<T> S, Phys ph, VFlags fl) {
     };
     T y[CH];
     deriv_rhs<CH>(y, S, lm.c, f, uni);
-    chunk_solve<CH, DIR>(y, S, lm.c, sm, uni);
+    chunk_solve<CH, DIR, false>(y, S, lm.c, sm, uni);
     if (lm.active) {
 #pragma unroll
       for (int t = 0; t < CH; ++t) {
@@ -306,7 +306,7 @@ k_visc(Geo g, DevT<T> d, DScheme<T> S, Phys ph, VFlags fl) {
 template <typename T, int DIR>
 cudaError_t launch_filter(const SweepCtx<T>& c, const DScheme<T>& S, const FTab<T>& Tb, int CH,
                           int do_q2f) {
-  const dim3 gr = sweep_grid<DIR>(c.g), bl = sweep_block<DIR>();
+  const dim3 gr = sweep_grid<DIR, true>(c.g), bl = sweep_block<DIR, true>();
   ASTR_CH_SWITCH(CH, (k_filter<T, DIR, CHC><<<gr, bl, 0, c.st>>>(c.g, c.d, S, Tb, c.ph, do_q2f)));
   return cudaGetLastError();
 }
