@@ -74,10 +74,23 @@ k_filter(Geo g, DevT<T> d, DScheme<T> S, FTab<T> Tb, Phys ph, int do_q2f) {
 
 // convrsdcal6 (src/solver.F90:2173-2341) and gradcal
 // (src/comsolver.F90:244-497), one direction, diagonal metrics.
+// FP32 convective sweeps stage the two flux factors shared by the five
+// conserved variables in dynamic shared memory, once per direction: main
+// ordering A = J*(dxi*u_d), B = J*(dxi*p); mini-app A = u_d, B = p.  A line
+// has rows -3 .. n+2 of them; y/z blocks store them node-major
+// (row*YZ_LINES + line), x warps line-major (line*(n+6) + row), both
+// conflict-free for the chunk-strided reads.
+template <typename T>
+constexpr bool stage_flux() { return sizeof(T) == 4; }
+
+template <typename T, int DIR>
+__host__ __device__ constexpr int flux_lines() { return warp_lines<DIR>() ? X_LINES : YZ_LINES; }
+
 template <typename T, int DIR, int CH>
 __global__ void __launch_bounds__(block_threads<DIR>(), min_blocks<DIR>())
 k_convgrad(Geo g, DevT<T> d, DScheme<T> S, Phys ph, CGFlags fl) {
   __shared__ T sm[SCAN_SMEM_WORDS];
+  extern __shared__ __align__(16) unsigned char conv_smem[];
   LineMap<DIR> lm(g);
   const bool uni = uniform_chunk<DIR, false>(S, lm.c);
   if (warp_lines<DIR>() && !lm.active) {  // whole warp: x-lines own a warp
@@ -103,13 +116,57 @@ k_convgrad(Geo g, DevT<T> d, DScheme<T> S, Phys ph, CGFlags fl) {
   const T* xd = d.xd + DIR * nh;
 
   if (fl.conv) {
+    constexpr bool stg = stage_flux<T>();
+    constexpr int NL = flux_lines<T, DIR>();
+    T* fa = reinterpret_cast<T*>(conv_smem);
+    const int np = S.n + 6;  // rows -3 .. n+2
+    T* fb = fa + (size_t)np * NL;
+    const int li = warp_lines<DIR>() ? (int)threadIdx.y : (int)threadIdx.x;
+    auto sidx = [&](int rho) -> int {
+      return warp_lines<DIR>() ? li * np + (rho + 3) : (rho + 3) * NL + li;
+    };
+    if (stg) {
+      // this chunk's rows; chunk 0 adds rows -3..-1, the chunk of row n-1
+      // adds rows n..n+2 (the windows of the end rows)
+      const int s0 = lm.c * CH;
+      const int r0 = lm.c == 0 ? -3 : s0;
+      const int r1 = (s0 <= S.n - 1 && S.n - 1 < s0 + CH) ? S.n + 2 : min(s0 + CH, S.n) - 1;
+      for (int rho = r0; rho <= r1; ++rho) {
+        const long long p = bh + hs * (S.first + rho);
+        const T pp = d.pr[p + 4 * nh];
+        const T ud = d.pr[p + (1 + DIR) * nh];
+        T A = ud, B = pp;
+        if (!ph.mini) {
+          const T x = xd[p];
+          const T J = d.jac[p];
+          A = J * (x * ud);
+          B = J * (x * pp);
+        }
+        fa[sidx(rho)] = A;
+        fb[sidx(rho)] = B;
+      }
+      if (warp_lines<DIR>()) __syncwarp();
+      else __syncthreads();
+    }
 #pragma unroll 1
     for (int n = 0; n < 5; ++n) {
       auto f = [&](int node) -> T {
         const long long p = bh + hs * node;
+        const T qn = d.q[p + n * nh];
+        if (stg) {
+          const int rho = node - S.first;
+          const T A = fa[sidx(rho)], B = fb[sidx(rho)];
+          if (ph.mini) {
+            if (n == 4) return (qn + B) * A;
+            if (n == 1 + DIR) return qn * A + B;
+            return qn * A;
+          }
+          if (n == 4) return (qn + d.pr[p + 4 * nh]) * A;
+          if (n == 1 + DIR) return qn * A + B;
+          return qn * A;
+        }
         const T pp = d.pr[p + 4 * nh];
         const T ud = d.pr[p + (1 + DIR) * nh];
-        const T qn = d.q[p + n * nh];
         if (ph.mini) {
           const T uu = ud;
           if (n == 4) return (qn + pp) * uu;
@@ -311,11 +368,36 @@ cudaError_t launch_filter(const SweepCtx<T>& c, const DScheme<T>& S, const FTab<
   return cudaGetLastError();
 }
 
+template <typename T, int DIR, int CH>
+cudaError_t launch_convgrad_ch(const SweepCtx<T>& c, const DScheme<T>& S, CGFlags f) {
+  const dim3 gr = sweep_grid<DIR>(c.g), bl = sweep_block<DIR>();
+  const size_t dyn =
+      (stage_flux<T>() && f.conv) ? 2 * (size_t)(S.n + 6) * flux_lines<T, DIR>() * sizeof(T) : 0;
+  static size_t attr_bytes = 48 * 1024;  // dynamic shared memory allowed so far (per instantiation)
+  if (dyn > attr_bytes) {
+    const cudaError_t ea = cudaFuncSetAttribute(k_convgrad<T, DIR, CH>,
+                                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    if (ea != cudaSuccess) return ea;
+    attr_bytes = dyn;
+  }
+  k_convgrad<T, DIR, CH><<<gr, bl, dyn, c.st>>>(c.g, c.d, S, c.ph, f);
+  return cudaGetLastError();
+}
+
+// The same switch for a call that returns the launch status.
+#define ASTR_CH_RETURN(CHV, ...)                                   \
+  switch (CHV) {                                                   \
+    case 3: { constexpr int CHC = 3; return __VA_ARGS__; }         \
+    case 5: { constexpr int CHC = 5; return __VA_ARGS__; }         \
+    case 9: { constexpr int CHC = 9; return __VA_ARGS__; }         \
+    case 17: { constexpr int CHC = 17; return __VA_ARGS__; }       \
+    case 33: { constexpr int CHC = 33; return __VA_ARGS__; }       \
+    default: return cudaErrorInvalidValue;                         \
+  }
+
 template <typename T, int DIR>
 cudaError_t launch_convgrad(const SweepCtx<T>& c, const DScheme<T>& S, int CH, CGFlags f) {
-  const dim3 gr = sweep_grid<DIR>(c.g), bl = sweep_block<DIR>();
-  ASTR_CH_SWITCH(CH, (k_convgrad<T, DIR, CHC><<<gr, bl, 0, c.st>>>(c.g, c.d, S, c.ph, f)));
-  return cudaGetLastError();
+  ASTR_CH_RETURN(CH, launch_convgrad_ch<T, DIR, CHC>(c, S, f));
 }
 
 template <typename T, int DIR>
