@@ -38,7 +38,8 @@ EXPORTS = [
     "astr_gpu_host_alloc", "astr_gpu_host_free", "astr_gpu_timed_steps",
     "astr_gpu_set_profiling", "astr_gpu_kernel_times", "astr_gpu_measure_fp64_peak",
     "astr_gpu_stats_noalloc", "astr_gpu_set_grid", "astr_gpu_channel_state",
-    "astr_gpu_boucon", "astr_gpu_step_async", "astr_gpu_poll",
+    "astr_gpu_boucon", "astr_gpu_step_async", "astr_gpu_poll", "astr_gpu_crashcheck",
+    "astr_gpu_cflcal",
 ]
 NOALLOC_STATS_MAX_BLOCKS = 65536
 KERNEL_CLASSES = ["filter", "halo", "convgrad", "visc", "pointwise", "stats"]
@@ -122,6 +123,10 @@ def load(path: str = LIB_PATH):
     L.astr_gpu_stats_noalloc.argtypes = [vp, vp, vp, ctypes.POINTER(AstrDims), ctypes.c_double,
                                          vp, dp, dp]
     L.astr_gpu_stats_noalloc.restype = ip
+    L.astr_gpu_crashcheck.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ip)]
+    L.astr_gpu_crashcheck.restype = ip
+    L.astr_gpu_cflcal.argtypes = [vp, ctypes.c_double, dp, dp]
+    L.astr_gpu_cflcal.restype = ip
     L.astr_gpu_step_async.argtypes = [vp, ip]
     L.astr_gpu_step_async.restype = ip
     L.astr_gpu_poll.argtypes = [vp]

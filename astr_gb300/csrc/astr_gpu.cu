@@ -279,6 +279,48 @@ __global__ void k_chan_src(Geo g, DevT<T> d) {
   }
 }
 
+// crashcheck (src/mainloop.F90:709-812) on every interior node: a node
+// crashes when q1 >= 0 does not hold (negative or NaN density).  out[0]
+// counts them, out[1] keeps the smallest interior linear index.
+template <typename T>
+__global__ void k_crashcheck(Geo g, DevT<T> d, unsigned long long* out) {
+  int i, j, k;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (!point_of(g, idx, i, j, k)) return;
+  const double q1 = q64(d, hidx(g, i, j, k), idx, 0, g.nh, g.n0);
+  if (!(q1 >= 0.0)) {
+    atomicAdd(out, 1ULL);
+    atomicMin(out + 1, (unsigned long long)idx);
+  }
+}
+
+// cflcal (src/commcal.F90:27-87), diagonal metrics: per direction the
+// largest of 0 and dxi(d,d)*u_d + sqrt(T)/mach*|dxi(d,d)| over the interior
+// nodes.  The maxima are non-negative, so their bit patterns order like the
+// values and atomicMax on them is exact and order-independent.
+template <typename T>
+__global__ void k_cflcal(Geo g, DevT<T> d, double rmach, unsigned long long* out3) {
+  int i, j, k;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double m[3] = {0.0, 0.0, 0.0};
+  if (point_of(g, idx, i, j, k)) {
+    const long long p = hidx(g, i, j, k), nh = g.nh;
+    const double css = sqrt((double)d.pr[p + 5 * nh]) * rmach;
+    for (int dd = 0; dd < g.ndims; ++dd) {
+      const double x = (double)d.xd[p + dd * nh];
+      const double ub = x * (double)d.pr[p + (1 + dd) * nh];
+      const double cs = css * fabs(x);
+      m[dd] = fmax(0.0, fmax(ub, fmax(ub - cs, ub + cs)));
+    }
+  }
+  for (int dd = 0; dd < 3; ++dd) {
+    double v = m[dd];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, off));
+    if ((threadIdx.x & 31) == 0 && v > 0.0) atomicMax(out3 + dd, (unsigned long long)__double_as_longlong(v));
+  }
+}
+
 // Fixed-order reduction of the per-warp statistics partials.
 __global__ void k_stats_final(const double* part, long long nw, double* out) {
   __shared__ double sk[1024], se[1024];
@@ -1280,6 +1322,57 @@ int astr_gpu_channel_state(astr_ctx* c, double* out) {
   out[2] = h[CHAN_TARGET];
   out[3] = h[CHAN_FBCX];
   out[4] = (double)c->nstep;
+  return ASTR_OK;
+}
+
+static int ready(astr_ctx* c);
+
+int astr_gpu_crashcheck(astr_ctx* c, long long* ncrash, int* ijk) {
+  RC(ready(c));
+  if (!ncrash) return fail(c, ASTR_ERR_ARG, "null argument");
+  unsigned long long* dv = (unsigned long long*)c->stats_dev;  // 64 B scratch
+  const unsigned long long init[2] = {0ULL, ~0ULL};
+  CK(cudaMemcpyAsync(dv, init, sizeof(init), cudaMemcpyHostToDevice, c->st));
+  if (c->prec == ASTR_FP64)
+    k_crashcheck<double><<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, c->d64, dv);
+  else
+    k_crashcheck<float><<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, c->d32, dv);
+  RC(after_launch(c, "k_crashcheck"));
+  unsigned long long h[2];
+  CK(cudaMemcpyAsync(h, dv, sizeof(h), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  *ncrash = (long long)h[0];
+  if (ijk) {
+    ijk[0] = ijk[1] = ijk[2] = -1;
+    if (h[0]) {
+      const long long z = (long long)h[1];
+      ijk[0] = (int)(z % c->g.I);
+      ijk[1] = (int)((z / c->g.I) % (c->g.jm + 1));
+      ijk[2] = (int)(z / c->g.IJ);
+    }
+  }
+  return ASTR_OK;
+}
+
+int astr_gpu_cflcal(astr_ctx* c, double deltat, double* cfl, double* delta3) {
+  RC(ready(c));
+  if (!cfl) return fail(c, ASTR_ERR_ARG, "null argument");
+  unsigned long long* dv = (unsigned long long*)c->stats_dev;
+  CK(cudaMemsetAsync(dv, 0, 3 * sizeof(unsigned long long), c->st));
+  const double rmach = 1.0 / c->pm.mach;
+  if (c->prec == ASTR_FP64)
+    k_cflcal<double><<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, c->d64, rmach, dv);
+  else
+    k_cflcal<float><<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, c->d32, rmach, dv);
+  RC(after_launch(c, "k_cflcal"));
+  unsigned long long h[3];
+  CK(cudaMemcpyAsync(h, dv, sizeof(h), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  double dl[3];
+  for (int dd = 0; dd < 3; ++dd) std::memcpy(&dl[dd], &h[dd], 8);
+  *cfl = deltat * (dl[0] + dl[1] + dl[2]);
+  if (delta3)
+    for (int dd = 0; dd < 3; ++dd) delta3[dd] = dl[dd];
   return ASTR_OK;
 }
 

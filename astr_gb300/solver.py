@@ -167,6 +167,22 @@ class GpuSolver:
     def rhscal(self):
         self._c(self.L.astr_gpu_rhscal(self.h))
 
+    def crashcheck(self):
+        """(number of interior nodes with rho < 0 or NaN, first such (i, j, k)
+        or None) — crashcheck, src/mainloop.F90:709-812."""
+        n = ctypes.c_longlong()
+        ijk = (ctypes.c_int * 3)()
+        self._c(self.L.astr_gpu_crashcheck(self.h, ctypes.byref(n), ijk))
+        return n.value, (tuple(ijk) if n.value else None)
+
+    def cflcal(self, deltat: float):
+        """(CFL number of the resident state at this time step, (Di, Dj, Dk))
+        — cflcal, src/commcal.F90:27-87."""
+        cfl = ctypes.c_double()
+        d3 = np.zeros(3)
+        self._c(self.L.astr_gpu_cflcal(self.h, float(deltat), ctypes.byref(cfl), capi.dptr(d3)))
+        return cfl.value, d3
+
     def boucon(self):
         self._c(self.L.astr_gpu_boucon(self.h))
 

@@ -113,6 +113,18 @@ int astr_gpu_step_async(astr_ctx* ctx, int nsteps);
  * flight, < 0 on a CUDA error. */
 int astr_gpu_poll(astr_ctx* ctx);
 
+/* crashcheck (src/mainloop.F90:709-812): count the interior nodes whose
+ * density is negative or not a number; ijk (may be NULL) receives the
+ * first such node (i fastest), or -1s.  The state is not modified. */
+int astr_gpu_crashcheck(astr_ctx* ctx, long long* ncrash, int* ijk);
+
+/* cflcal (src/commcal.F90:27-87) on the resident state: *cfl = deltat *
+ * (Di + Dj + Dk), D the largest of 0 and the contravariant velocity plus
+ * sound speed (sqrt(T)/mach) along each computational direction over the
+ * interior nodes; delta3 (may be NULL) receives Di, Dj, Dk.  Diagonal
+ * metrics, as everywhere in this library. */
+int astr_gpu_cflcal(astr_ctx* ctx, double deltat, double* cfl, double* delta3);
+
 /* boucon (src/bc.F90:327-409) for the per-routine drop-in: the noslip
  * isothermal j-walls of a channel context; no-op otherwise. */
 int astr_gpu_boucon(astr_ctx* ctx);
