@@ -307,9 +307,17 @@ __global__ void k_cflcal(Geo g, DevT<T> d, double rmach, unsigned long long* out
     const long long p = hidx(g, i, j, k), nh = g.nh;
     const double css = sqrt((double)d.pr[p + 5 * nh]) * rmach;
     for (int dd = 0; dd < g.ndims; ++dd) {
-      const double x = (double)d.xd[p + dd * nh];
-      const double ub = x * (double)d.pr[p + (1 + dd) * nh];
-      const double cs = css * fabs(x);
+      double ub, cs;
+      if (d.xg) {  // general metrics: the whole row of dxi
+        const double x0 = (double)d.xg[(3 * dd) * nh + p], x1 = (double)d.xg[(3 * dd + 1) * nh + p];
+        const double x2 = (double)d.xg[(3 * dd + 2) * nh + p];
+        ub = x0 * (double)d.pr[p + nh] + x1 * (double)d.pr[p + 2 * nh] + x2 * (double)d.pr[p + 3 * nh];
+        cs = css * sqrt(x0 * x0 + x1 * x1 + x2 * x2);
+      } else {
+        const double x = (double)d.xd[p + dd * nh];
+        ub = x * (double)d.pr[p + (1 + dd) * nh];
+        cs = css * fabs(x);
+      }
       m[dd] = fmax(0.0, fmax(ub, fmax(ub - cs, ub + cs)));
     }
   }
@@ -318,6 +326,71 @@ __global__ void k_cflcal(Geo g, DevT<T> d, double rmach, unsigned long long* out
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, off));
     if ((threadIdx.x & 31) == 0 && v > 0.0) atomicMax(out3 + dd, (unsigned long long)__double_as_longlong(v));
+  }
+}
+
+// General metrics: the gradients the sweeps stored as derivatives along
+// xi_d become physical ones, dvel(n,m) = sum_d d(u_n)/d(xi_d) dxi(d,m) and
+// the same for T, summed over d = x, y(, z) in that order (gradcal,
+// src/comsolver.F90:244-497).
+template <typename T>
+__global__ void k_gradphys(Geo g, DevT<T> d) {
+  int i, j, k;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (!point_of(g, idx, i, j, k)) return;
+  const long long p = hidx(g, i, j, k), nh = g.nh, n0 = g.n0;
+  T* G = d.grad + idx;
+  T r[4][3];
+  for (int v = 0; v < 4; ++v)
+    for (int dd = 0; dd < 3; ++dd)
+      r[v][dd] = dd < g.ndims ? G[(v < 3 ? v + 3 * dd : 9 + dd) * n0] : T(0);
+  for (int v = 0; v < 4; ++v)
+    for (int m = 0; m < 3; ++m) {
+      T acc = r[v][0] * d.xg[(0 + m) * nh + p];
+      acc = acc + r[v][1] * d.xg[(3 + m) * nh + p];
+      if (g.ndims == 3) acc = acc + r[v][2] * d.xg[(6 + m) * nh + p];
+      G[(v < 3 ? v + 3 * m : 9 + m) * n0] = acc;
+    }
+}
+
+// kenergycal / enstophycal (src/statistic.F90:871-992) as a point kernel
+// (general metrics), one partial pair per block, reduced by k_stats_final.
+template <typename T>
+__global__ void k_stats_pt(Geo g, DevT<T> d) {
+  __shared__ double sk[256], se[256];
+  int i, j, k;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double ke = 0.0, en = 0.0;
+  if (point_of(g, idx, i, j, k)) {
+    const bool ink = g.ndims == 3 ? (k >= 1 && k <= g.km) : (k == 0);
+    if (i >= 1 && j >= 1 && ink) {
+      const long long p = hidx(g, i, j, k), nh = g.nh, n0 = g.n0;
+      const double ro = d.pr[p], u = d.pr[p + nh], v = d.pr[p + 2 * nh], w = d.pr[p + 3 * nh];
+      ke = ro * (u * u + v * v + w * w);
+      const T* G = d.grad + idx;
+      const double o3 = (double)G[1 * n0] - (double)G[3 * n0];
+      double om = o3 * o3;
+      if (g.ndims == 3) {
+        const double o1 = (double)G[5 * n0] - (double)G[7 * n0];
+        const double o2 = (double)G[6 * n0] - (double)G[2 * n0];
+        om = o1 * o1 + o2 * o2 + o3 * o3;
+      }
+      en = ro * om;
+    }
+  }
+  sk[threadIdx.x] = ke;
+  se[threadIdx.x] = en;
+  __syncthreads();
+  for (int s2 = blockDim.x / 2; s2 > 0; s2 >>= 1) {
+    if ((int)threadIdx.x < s2) {
+      sk[threadIdx.x] += sk[threadIdx.x + s2];
+      se[threadIdx.x] += se[threadIdx.x + s2];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    d.part[2 * blockIdx.x] = sk[0];
+    d.part[2 * blockIdx.x + 1] = se[0];
   }
 }
 
@@ -625,6 +698,10 @@ struct astr_ctx {
   // Timed on the 512^3 TGV: bit 0 saves 2 % (FP32 storage), bit 1 costs
   // 1 % (the FP64 master update is FP64-bound either way).
   int split_last = 1;
+  // general (non-diagonal) metrics: dxi(d,m) at 3*d + m, allocated when the
+  // first non-diagonal set arrives
+  bool gen = false;
+  void* xg = nullptr;
   // one RK3 step captured as a CUDA graph (asynchronous stepping)
   cudaGraphExec_t step_graph = nullptr;
   long long graph_kernels = 0;  // kernel launches in one captured step
@@ -713,7 +790,7 @@ long long sweep_warps(const Geo& g) {
 
 template <typename T>
 SweepCtx<T> sctx(astr_ctx* c) {
-  return SweepCtx<T>{c->g, dev<T>(c), c->ph, c->st};
+  return SweepCtx<T>{c->g, dev<T>(c), c->ph, c->st, c->gen};
 }
 
 int launch_result(astr_ctx* c, cudaError_t e, const char* what) {
@@ -823,7 +900,11 @@ int run_visc(astr_ctx* c, bool fuse_rk, bool q2f) {
 
 int stats_finish(astr_ctx* c, double* out2) {
   const int last = c->g.ndims - 1;
-  const long long nw = last == 2 ? sweep_warps<2>(c->g) : (last == 1 ? sweep_warps<1>(c->g) : sweep_warps<0>(c->g));
+  // partial sums: one per warp of the last convective sweep, or one per
+  // block of the point statistics kernel (general metrics)
+  const long long nw = c->gen ? (long long)point_grid(c->g.n0).x
+                              : (last == 2 ? sweep_warps<2>(c->g)
+                                           : (last == 1 ? sweep_warps<1>(c->g) : sweep_warps<0>(c->g)));
   prof_begin(c, KC_STATS);
   k_stats_final<<<1, 1024, 0, c->st>>>(c->d64.part, nw, c->stats_dev);
   prof_end(c);
@@ -849,6 +930,22 @@ void set_stage(astr_ctx* c, int s) {
   c->ph.rk1 = rk[s][0];
   c->ph.rk2 = rk[s][1];
   c->ph.rk3 = rk[s][2];
+}
+
+template <typename T>
+int gradphys_pointwise(astr_ctx* c) {
+  prof_begin(c, KC_POINT);
+  k_gradphys<T><<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, dev<T>(c));
+  prof_end(c);
+  return after_launch(c, "k_gradphys");
+}
+
+template <typename T>
+int stats_pointwise(astr_ctx* c) {
+  prof_begin(c, KC_STATS);
+  k_stats_pt<T><<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, dev<T>(c));
+  prof_end(c);
+  return after_launch(c, "k_stats_pt");
 }
 
 template <typename T>
@@ -911,11 +1008,18 @@ int one_step(astr_ctx* c, double* stats) {
       RC(run_filter<T>(c, true));
     } else {
       const bool visc = c->pm.diffterm != 0;
-      const bool split_sig = visc && (c->split_last & 1), split_rk = visc && (c->split_last & 2);
+      const bool split_sig = visc && ((c->split_last & 1) || c->gen);
+      const bool split_rk = visc && (c->split_last & 2);
       if (c->pm.lfilter) RC(run_filter<T>(c, false));
       if (c->channel) RC(run_noslip<T>(c));
       RC(run_qswap<T>(c));
-      RC(run_convgrad<T>(c, true, true, visc && !split_sig, st1 && stats, st1));
+      RC(run_convgrad<T>(c, true, true, visc && !split_sig, st1 && stats && !c->gen, st1));
+      if (c->gen) {
+        // general metrics: gradients contracted with the metrics, then the
+        // statistics from them
+        RC(gradphys_pointwise<T>(c));
+        if (st1 && stats) RC(stats_pointwise<T>(c));
+      }
       if (split_sig) RC(sigma_pointwise<T>(c));
       if (c->channel) RC(run_chan<T>(c, st1));
       if (visc) RC(run_visc<T>(c, !split_rk, !split_rk));
@@ -1154,6 +1258,7 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
   c->jac64 = f32 ? (double*)alloc(nh * 8) : (double*)jac;
   c->rjac64 = (double*)alloc(nh * 8);
   long long nw = std::max(sweep_warps<0>(g), std::max(sweep_warps<1>(g), sweep_warps<2>(g)));
+  nw = std::max(nw, (long long)((g.n0 + 255) / 256));  // point statistics blocks
   double* part = (double*)alloc(2 * nw * 8);
   int* flag = (int*)alloc(64);
   c->stats_dev = (double*)alloc(64);
@@ -1230,7 +1335,7 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
     D.q = (TT*)q; D.pr = (TT*)pr; D.xd = (const TT*)xd; D.jac = (const TT*)jac;
     D.jac64 = c->jac64; D.rjac64 = c->rjac64;
     D.qrhs = (TT*)qrhs; D.qsave = qsave; D.qm = qm; D.grad = (TT*)grad; D.sig = (TT*)sig;
-    D.qf = (TT*)qf; D.part = part; D.flag = flag; D.chan = c->chan_dev;
+    D.qf = (TT*)qf; D.part = part; D.flag = flag; D.chan = c->chan_dev; D.xg = nullptr;
   };
   fill(c->d64, (double*)nullptr);
   fill(c->d32, (float*)nullptr);
@@ -1274,25 +1379,47 @@ static int metrics_common(astr_ctx* c, const double* const src[3], const double*
 int astr_gpu_set_metrics(astr_ctx* c, const double* dxi, const double* jacob) {
   if (!c || !dxi || !jacob) return fail(c, ASTR_ERR_ARG, "null argument");
   const size_t nh = (size_t)c->g.nh;
-  // Only diagonal metrics are built.  Off-diagonals up to 1e-10 of the
-  // largest diagonal entry are gridgeom's rounding residue on a stretched
-  // rectilinear grid and are taken as zero.
-  double dmax = 0.0;
-  for (int dd = 0; dd < 3; ++dd) {
-    const double* p = dxi + (size_t)(dd + 3 * dd) * nh;
-    for (size_t i = 0; i < nh; ++i) dmax = std::max(dmax, std::fabs(p[i]));
-  }
-  const double tol = 1e-10 * dmax;
-  for (int m = 0; m < 3; ++m)
-    for (int dd = 0; dd < 3; ++dd) {
+  // Diagonal metrics (every off-diagonal exactly zero) take the rectilinear
+  // kernels; anything else the general-metric ones.
+  bool diag = true;
+  for (int m = 0; m < 3 && diag; ++m)
+    for (int dd = 0; dd < 3 && diag; ++dd) {
       if (m == dd) continue;
       const double* p = dxi + (size_t)(dd + 3 * m) * nh;
       for (size_t i = 0; i < nh; ++i)
-        if (std::fabs(p[i]) > tol)
-          return fail(c, ASTR_ERR_UNSUPPORTED, "non-diagonal grid metrics are not supported");
+        if (p[i] != 0.0) { diag = false; break; }
     }
+  if (!diag && c->pm.order == ASTR_ORDER_MINIAPP)
+    return fail(c, ASTR_ERR_ARG, "the mini-app ordering takes no metrics");
+  if (c->step_graph) {  // a captured step holds the old metric mode
+    CK(cudaStreamSynchronize(c->st));
+    cudaGraphExecDestroy(c->step_graph);
+    c->step_graph = nullptr;
+  }
   const double* const src[3] = {dxi, dxi + 4 * nh, dxi + 8 * nh};
-  return metrics_common(c, src, jacob);
+  RC(metrics_common(c, src, jacob));
+  if (diag) {
+    c->gen = false;
+    c->d64.xg = nullptr;
+    c->d32.xg = nullptr;
+    return ASTR_OK;
+  }
+  const size_t w = wsize(c);
+  if (!c->xg) {
+    void* p = nullptr;
+    CK(cudaMalloc(&p, 9 * nh * w));
+    c->allocs.push_back(p);
+    c->xg = p;
+  }
+  RC(xfer_begin(c));
+  for (int dd = 0; dd < 3; ++dd)
+    for (int m = 0; m < 3; ++m)
+      RC(upload_array(c, (char*)c->xg + (size_t)(3 * dd + m) * nh * w, dxi + (size_t)(dd + 3 * m) * nh, nh));
+  RC(xfer_sync(c));
+  c->d64.xg = (const double*)c->xg;
+  c->d32.xg = (const float*)c->xg;
+  c->gen = true;
+  return ASTR_OK;
 }
 
 int astr_gpu_set_grid(astr_ctx* c, const double* x) {
@@ -1385,6 +1512,14 @@ int astr_gpu_boucon(astr_ctx* c) {
 int astr_gpu_set_metrics_diag(astr_ctx* c, const double* x11, const double* x22, const double* x33,
                               const double* jacob) {
   if (!c || !x11 || !x22 || !x33 || !jacob) return fail(c, ASTR_ERR_ARG, "null argument");
+  if (c->step_graph) {
+    CK(cudaStreamSynchronize(c->st));
+    cudaGraphExecDestroy(c->step_graph);
+    c->step_graph = nullptr;
+  }
+  c->gen = false;
+  c->d64.xg = nullptr;
+  c->d32.xg = nullptr;
   const double* const src[3] = {x11, x22, x33};
   return metrics_common(c, src, jacob);
 }
@@ -1505,8 +1640,12 @@ int astr_gpu_qswap(astr_ctx* c) {
 
 int astr_gpu_gradcal(astr_ctx* c) {
   RC(ready(c));
-  return c->prec == ASTR_FP64 ? run_convgrad<double>(c, false, true, false, false, false)
-                              : run_convgrad<float>(c, false, true, false, false, false);
+  if (c->prec == ASTR_FP64) {
+    RC(run_convgrad<double>(c, false, true, false, false, false));
+    return c->gen ? gradphys_pointwise<double>(c) : ASTR_OK;
+  }
+  RC(run_convgrad<float>(c, false, true, false, false, false));
+  return c->gen ? gradphys_pointwise<float>(c) : ASTR_OK;
 }
 
 int astr_gpu_rhscal(astr_ctx* c) {

@@ -113,6 +113,8 @@ struct DevT {
   double* part;     // statistics partial sums, 2 per warp
   int* flag;        // crash flag
   const double* chan;  // channel controller state (CHAN_*), null unless a channel
+  const T* xg;      // general metrics: 9 halo arrays, dxi(d,m) at 3*d + m (0-based);
+                    // null for diagonal metrics
 };
 
 // Channel controller state in device memory (FP64).
@@ -152,6 +154,7 @@ struct SweepCtx {
   DevT<T> d;
   Phys ph;
   cudaStream_t st;
+  bool gen;  // general (non-diagonal) metrics
 };
 
 __device__ __forceinline__ long long hidx(const Geo& g, int i, int j, int k) {

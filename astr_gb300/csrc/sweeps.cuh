@@ -86,7 +86,14 @@ constexpr bool stage_flux() { return sizeof(T) == 4; }
 template <typename T, int DIR>
 __host__ __device__ constexpr int flux_lines() { return warp_lines<DIR>() ? X_LINES : YZ_LINES; }
 
-template <typename T, int DIR, int CH>
+// GEN: general metrics.  The convective flux uses the whole metric row
+// (U = dxi(d,1) u + dxi(d,2) v + dxi(d,3) w, pressure terms dxi(d,m) p, as
+// src/solver.F90:2200-2206), and the gradients are stored as derivatives
+// along the computational direction, contracted with the metrics by
+// k_gradphys once all directions are done (gradcal's sum over d,
+// src/comsolver.F90:244-497).  The last-direction stress and statistics are
+// then computed by point kernels.
+template <typename T, int DIR, int CH, bool GEN>
 __global__ void __launch_bounds__(block_threads<DIR>(), min_blocks<DIR>())
 k_convgrad(Geo g, DevT<T> d, DScheme<T> S, Phys ph, CGFlags fl) {
   __shared__ T sm[SCAN_SMEM_WORDS];
@@ -116,7 +123,7 @@ k_convgrad(Geo g, DevT<T> d, DScheme<T> S, Phys ph, CGFlags fl) {
   const T* xd = d.xd + DIR * nh;
 
   if (fl.conv) {
-    constexpr bool stg = stage_flux<T>();
+    constexpr bool stg = stage_flux<T>() && !GEN;
     constexpr int NL = flux_lines<T, DIR>();
     T* fa = reinterpret_cast<T*>(conv_smem);
     const int np = S.n + 6;  // rows -3 .. n+2
@@ -153,6 +160,16 @@ k_convgrad(Geo g, DevT<T> d, DScheme<T> S, Phys ph, CGFlags fl) {
       auto f = [&](int node) -> T {
         const long long p = bh + hs * node;
         const T qn = d.q[p + n * nh];
+        if (GEN) {
+          const T* X = d.xg + (3 * DIR) * nh + p;
+          const T x0 = X[0], x1 = X[nh], x2 = X[2 * nh];
+          const T uu = x0 * d.pr[p + nh] + x1 * d.pr[p + 2 * nh] + x2 * d.pr[p + 3 * nh];
+          const T pp = d.pr[p + 4 * nh];
+          const T J = d.jac[p];
+          if (n == 0) return J * qn * uu;
+          if (n == 4) return J * (qn + pp) * uu;
+          return J * (qn * uu + (n == 1 ? x0 : (n == 2 ? x1 : x2)) * pp);
+        }
         if (stg) {
           const int rho = node - S.first;
           const T A = fa[sidx(rho)], B = fb[sidx(rho)];
@@ -214,7 +231,7 @@ k_convgrad(Geo g, DevT<T> d, DScheme<T> S, Phys ph, CGFlags fl) {
         for (int t = 0; t < CH; ++t) {
           const int node = S.first + lm.c * CH + t;
           if (node >= 0 && node <= dim) {
-            const T gv = ph.mini ? y[t] * rdx : y[t] * xd[bh + hs * node];
+            const T gv = GEN ? y[t] : (ph.mini ? y[t] * rdx : y[t] * xd[bh + hs * node]);
             d.grad[comp * n0 + bz + zs * node] = gv;
           }
         }
@@ -285,7 +302,9 @@ k_convgrad(Geo g, DevT<T> d, DScheme<T> S, Phys ph, CGFlags fl) {
 
 // diffrsdcal6 sweeps (src/solver.F90:2619-2852), one direction.  The last
 // direction applies the RK3 update (and, main ordering, q2fvar).
-template <typename T, int DIR, int CH>
+// GEN: general metrics, fluxes J*(sigma . dxi(d,:)) and J*(qflux . dxi(d,:))
+// (src/solver.F90:2627-2638).
+template <typename T, int DIR, int CH, bool GEN>
 __global__ void __launch_bounds__(block_threads<DIR>(), min_blocks<DIR>())
 k_visc(Geo g, DevT<T> d, DScheme<T> S, Phys ph, VFlags fl) {
   __shared__ T sm[SCAN_SMEM_WORDS];
@@ -314,6 +333,21 @@ k_visc(Geo g, DevT<T> d, DScheme<T> S, Phys ph, VFlags fl) {
       int nd = node;
       if (per) nd = nd < 0 ? nd + dim : (nd > dim ? nd - dim : nd);
       else if (nd < 0 || nd > dim) return T(0);
+      if (GEN) {
+        // sigma rows (1: s11 s12 s13, 2: s12 s22 s23, 3: s13 s23 s33) or qflux
+        const long long zz = bz + zs * nd;
+        const int c0 = n == 0 ? 0 : (n == 1 ? 1 : 2);
+        const int c1 = n == 0 ? 1 : (n == 1 ? 3 : 4);
+        const int c2 = n == 0 ? 2 : (n == 1 ? 4 : 5);
+        const T* Sg = d.sig + zz;
+        const T* Qf = d.qf + zz;
+        const T a0 = n < 3 ? Sg[c0 * n0] : Qf[0];
+        const T a1 = n < 3 ? Sg[c1 * n0] : Qf[n0];
+        const T a2 = n < 3 ? Sg[c2 * n0] : Qf[2 * n0];
+        const long long p = bh + hs * node;
+        const T* X = d.xg + (3 * DIR) * nh + p;
+        return (a0 * X[0] + a1 * X[nh] + a2 * X[2 * nh]) * d.jac[p];
+      }
       const T sv = src[bz + zs * nd];
       if (ph.mini) return sv;
       const long long p = bh + hs * node;
@@ -368,20 +402,27 @@ cudaError_t launch_filter(const SweepCtx<T>& c, const DScheme<T>& S, const FTab<
   return cudaGetLastError();
 }
 
-template <typename T, int DIR, int CH>
-cudaError_t launch_convgrad_ch(const SweepCtx<T>& c, const DScheme<T>& S, CGFlags f) {
+template <typename T, int DIR, int CH, bool GEN>
+cudaError_t launch_convgrad_gen(const SweepCtx<T>& c, const DScheme<T>& S, CGFlags f) {
   const dim3 gr = sweep_grid<DIR>(c.g), bl = sweep_block<DIR>();
-  const size_t dyn =
-      (stage_flux<T>() && f.conv) ? 2 * (size_t)(S.n + 6) * flux_lines<T, DIR>() * sizeof(T) : 0;
+  const size_t dyn = (stage_flux<T>() && !GEN && f.conv)
+                         ? 2 * (size_t)(S.n + 6) * flux_lines<T, DIR>() * sizeof(T)
+                         : 0;
   static size_t attr_bytes = 48 * 1024;  // dynamic shared memory allowed so far (per instantiation)
   if (dyn > attr_bytes) {
-    const cudaError_t ea = cudaFuncSetAttribute(k_convgrad<T, DIR, CH>,
+    const cudaError_t ea = cudaFuncSetAttribute(k_convgrad<T, DIR, CH, GEN>,
                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
     if (ea != cudaSuccess) return ea;
     attr_bytes = dyn;
   }
-  k_convgrad<T, DIR, CH><<<gr, bl, dyn, c.st>>>(c.g, c.d, S, c.ph, f);
+  k_convgrad<T, DIR, CH, GEN><<<gr, bl, dyn, c.st>>>(c.g, c.d, S, c.ph, f);
   return cudaGetLastError();
+}
+
+template <typename T, int DIR, int CH>
+cudaError_t launch_convgrad_ch(const SweepCtx<T>& c, const DScheme<T>& S, CGFlags f) {
+  return c.gen ? launch_convgrad_gen<T, DIR, CH, true>(c, S, f)
+               : launch_convgrad_gen<T, DIR, CH, false>(c, S, f);
 }
 
 // The same switch for a call that returns the launch status.
@@ -403,7 +444,11 @@ cudaError_t launch_convgrad(const SweepCtx<T>& c, const DScheme<T>& S, int CH, C
 template <typename T, int DIR>
 cudaError_t launch_visc(const SweepCtx<T>& c, const DScheme<T>& S, int CH, VFlags f) {
   const dim3 gr = sweep_grid<DIR>(c.g), bl = sweep_block<DIR>();
-  ASTR_CH_SWITCH(CH, (k_visc<T, DIR, CHC><<<gr, bl, 0, c.st>>>(c.g, c.d, S, c.ph, f)));
+  if (c.gen) {
+    ASTR_CH_SWITCH(CH, (k_visc<T, DIR, CHC, true><<<gr, bl, 0, c.st>>>(c.g, c.d, S, c.ph, f)));
+  } else {
+    ASTR_CH_SWITCH(CH, (k_visc<T, DIR, CHC, false><<<gr, bl, 0, c.st>>>(c.g, c.d, S, c.ph, f)));
+  }
   return cudaGetLastError();
 }
 

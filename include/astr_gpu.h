@@ -88,11 +88,11 @@ void astr_gpu_destroy(astr_ctx* ctx);
 
 /* Copy the grid metrics: dxi(-hm:..,1:3,1:3) and jacob(-hm:..) in Fortran
  * layout, as produced by gridgeom (src/geom.F90:99-930).  Host pointers.
- * The kernels take rectilinear (diagonal) metrics.  gridgeom's symmetric
- * conservative form leaves rounding residue in the off-diagonals of a
- * stretched rectilinear grid (about 1e-12 of the diagonal); off-diagonals
- * no larger than 1e-10 of the largest diagonal entry are taken as zero, any
- * larger one returns ASTR_ERR_UNSUPPORTED. */
+ * Metrics whose off-diagonals are all exactly zero run the rectilinear
+ * kernels; any other set (curvilinear grids, or the rounding residue
+ * gridgeom's symmetric conservative form leaves on a stretched rectilinear
+ * grid) runs the general-metric kernels, which hold all nine dxi arrays
+ * (9 more halo arrays of device memory, allocated on first use). */
 int astr_gpu_set_metrics(astr_ctx* ctx, const double* dxi, const double* jacob);
 
 /* Node coordinates x(-hm:..,1:3) in Fortran layout (gridgeom's x after its
