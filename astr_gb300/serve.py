@@ -65,6 +65,13 @@ def make_requests(count, rate=50.0, seed=20261203, edge3d=(32, 192), edge2d=(64,
     return out
 
 
+def partition(requests, rank: int, world: int):
+    """The requests one of `world` independent servers (one per GPU) takes:
+    every world-th request of the stream, so each server sees the same
+    arrival process thinned by `world`."""
+    return [r for r in requests if r.rid % world == rank]
+
+
 def request_points(req: Request) -> float:
     """Unique grid points of a request (periodic: edge^3 or edge^2)."""
     return float(req.n) ** (3 if req.kind == "tgv3d" else 2)

@@ -167,16 +167,20 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def dist_setup():
+def dist_setup(backend=None):
+    """One process per GPU (torchrun environment): the replicas only meet in
+    barriers and in the max-over-ranks of the timings (no data-path
+    collective).  backend defaults to NCCL; gloo serves CPU-only runs."""
     world = env_int("WORLD_SIZE", 1)
     rank = env_int("RANK", 0)
     if world > 1:
         import torch
         import torch.distributed as dist
-        local = env_int("LOCAL_RANK", 0)
-        torch.cuda.set_device(local)
+        backend = backend or os.environ.get("ASTR_DIST_BACKEND", "nccl")
+        if backend == "nccl":
+            torch.cuda.set_device(env_int("LOCAL_RANK", 0))
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
-        dist.init_process_group("nccl")
+        dist.init_process_group(backend)
         return rank, world, dist
     return rank, world, None
 
@@ -190,7 +194,8 @@ def max_over_ranks(dist, v):
     if dist is None:
         return v
     import torch
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -647,18 +652,27 @@ def run_serve(args, rank, world, dist):
     same requests solved one at a time in plain FP64."""
     import torch  # noqa: F401  (CUDA context for the memory query)
     from astr_gb300 import capi, serve
-    if rank != 0:
-        return 0
-    reqs = serve.make_requests(args.serve_cases, rate=args.serve_rate, seed=20261203)
+    allreqs = serve.make_requests(args.serve_cases, rate=args.serve_rate, seed=20261203)
+    # N GPUs: N independent servers, each taking every N-th request
+    reqs = serve.partition(allreqs, rank, world)
     free, total = torch.cuda.mem_get_info()
     budget = int(0.8 * free)
     be = serve.GpuBackend(capi.FP32_STORAGE)
     srv = serve.Server(be, budget, max_active=args.serve_slots)
+    barrier(dist)
     recs = serve.serve(reqs, srv)
     batched = serve.summarize(reqs, recs)
+    batched["makespan_s"] = round(max_over_ranks(dist, batched["makespan_s"]), 3)
+    batched["cases_per_s"] = round(len(allreqs) / batched["makespan_s"], 3)
     batched.update({"peak_active": srv.peak_active, "peak_hbm_gb": round(srv.peak_used / 1e9, 2),
                     "gpu_launches": srv.launches})
+    barrier(dist)
     seq = serve.summarize(reqs, serve.serve_sequential(reqs, serve.GpuBackend(capi.FP64)))
+    seq["makespan_s"] = round(max_over_ranks(dist, seq["makespan_s"]), 3)
+    seq["cases_per_s"] = round(len(allreqs) / seq["makespan_s"], 3)
+    if rank != 0:
+        return 0
+    reqs = allreqs
     work = sum(serve.request_points(q) * 3 * q.steps for q in reqs)
     line = {
         "case": "serve",
@@ -669,7 +683,8 @@ def run_serve(args, rank, world, dist):
         "offered_mpts_stages": round(work / 1e6, 1),
         "continuous_batching_fp32_storage": batched,
         "sequential_fp64": seq,
-        "hbm_budget_gb": round(budget / 1e9, 1), "slots": args.serve_slots,
+        "hbm_budget_gb": round(budget / 1e9, 1), "slots": args.serve_slots, "n_gpus": world,
+        "latency_note": "p50/p99 of rank 0's share when n_gpus > 1",
         "note": "time to solution = finish - arrival (wall clock, host-driven loop incl. case "
                 "set-up, upload and download); the offered load exceeds one GPU, so latency "
                 "includes queueing",

@@ -75,3 +75,10 @@ def test_oversize_request_rejected():
     srv = serve.Server(serve.FakeBackend(dev), hbm_budget=1000)
     with pytest.raises(ValueError):
         srv.submit(serve.Request(0, "tgv3d", 64, 100.0, 0.1, 10, 0.0))
+
+
+def test_partition_across_gpus():
+    reqs = serve.make_requests(50, rate=50.0, seed=11)
+    parts = [serve.partition(reqs, r, 4) for r in range(4)]
+    assert sorted(q.rid for p in parts for q in p) == list(range(50))
+    assert all(q.rid % 4 == r for r, p in enumerate(parts) for q in p)
