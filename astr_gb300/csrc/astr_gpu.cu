@@ -37,7 +37,8 @@ namespace {
 // Halo kernels
 // ---------------------------------------------------------------------------
 template <int DIR>
-__device__ __forceinline__ bool face_line(const Geo& g, int& dim, long long& base, long long& hs) {
+__device__ __forceinline__ bool face_line(const Geo& g, int& dim, long long& base, long long& hs,
+                                          long long* zbase = nullptr, long long* zs = nullptr) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   const int b = blockIdx.y;
   const int na = DIR == 0 ? g.jm : g.im;
@@ -47,6 +48,8 @@ __device__ __forceinline__ bool face_line(const Geo& g, int& dim, long long& bas
   int i0, j0, k0;
   line_ijk<DIR>(a, b, 0, i0, j0, k0);
   base = hidx(g, i0, j0, k0);
+  if (zbase) *zbase = zidx(g, i0, j0, k0);
+  if (zs) *zs = zstride<DIR>(g);
   return true;
 }
 
@@ -55,8 +58,8 @@ __device__ __forceinline__ bool face_line(const Geo& g, int& dim, long long& bas
 template <typename T, int DIR>
 __global__ void k_qswap(Geo g, DevT<T> d, Phys ph) {
   int dim;
-  long long base, hs;
-  if (!face_line<DIR>(g, dim, base, hs)) return;
+  long long base, hs, zb, zs;
+  if (!face_line<DIR>(g, dim, base, hs, &zb, &zs)) return;
   for (int n = 0; n < 5; ++n) {
     T* v = d.q + n * g.nh + base;
     if (dim == 0) {
@@ -64,9 +67,20 @@ __global__ void k_qswap(Geo g, DevT<T> d, Phys ph) {
     } else {
       for (int h = 1; h <= HMD; ++h) v[-hs * h] = v[hs * (dim - h)];
       for (int h = 1; h <= HMD; ++h) v[hs * (dim + h)] = v[hs * h];
-      const T avg = T(0.5) * (v[0] + v[hs * dim]);
-      v[0] = avg;
-      v[hs * dim] = avg;
+      if (d.qm) {
+        // FP32-storage form: average the FP64 master (interior nodes 0 and
+        // dim), so the FP32 copy never departs from it
+        double* M = d.qm + n * g.n0 + zb;
+        const double avg = 0.5 * (M[0] + M[zs * dim]);
+        M[0] = avg;
+        M[zs * dim] = avg;
+        v[0] = (T)avg;
+        v[hs * dim] = (T)avg;
+      } else {
+        const T avg = T(0.5) * (v[0] + v[hs * dim]);
+        v[0] = avg;
+        v[hs * dim] = avg;
+      }
     }
   }
   for (int l = -HMD; l <= 0; ++l) q2fvar_store(g, d, ph, base + hs * l);

@@ -680,9 +680,9 @@ __device__ __forceinline__ void sigma_point(const Geo& g, const DevT<T>& d, cons
 }
 
 // The conserved value q at an interior point with FP64 accuracy: the FP64
-// form reads it; the FP32-storage form adds to the FP64 master every change
-// the FP32 copy received since the last RK3 update (filter, interface
-// averaging).
+// form reads it; the FP32-storage form reads its FP64 master, which every
+// writer of interior q updates with the FP32 copy (RK3 update, filter
+// increments, interface averaging, walls, upload).
 __device__ __forceinline__ double q64(const DevT<double>& d, long long p, long long z, int m,
                                       long long nh, long long n0) {
   (void)z; (void)n0;
@@ -690,9 +690,8 @@ __device__ __forceinline__ double q64(const DevT<double>& d, long long p, long l
 }
 __device__ __forceinline__ double q64(const DevT<float>& d, long long p, long long z, int m,
                                       long long nh, long long n0) {
-  const double master = d.qm[m * n0 + z];
-  const float inc = d.q[m * nh + p] - __double2float_rn(master);
-  return master + (double)inc;
+  (void)p; (void)nh;
+  return d.qm[m * n0 + z];
 }
 
 // RK3 stage update (src/mainloop.F90:441-451) of variable m at one point.
