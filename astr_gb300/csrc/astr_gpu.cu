@@ -656,9 +656,9 @@ FTab<T> cast_ftab(const HostFTab& h) {
 
 const int kCH[] = {3, 5, 9, 17, 33};
 
-int pick_ch(int nmax) {
+int pick_ch(int nmax, int nchunks) {
   for (int ch : kCH)
-    if (NCH * ch >= nmax) return ch;
+    if (nchunks * ch >= nmax) return ch;
   return -1;
 }
 
@@ -681,7 +681,8 @@ struct astr_ctx {
   FTab<float> ft32;
   DScheme<double> fd64[3], fl64[3];
   DScheme<float> fd32[3], fl32[3];
-  int CH[3] = {0, 0, 0};
+  int CH[3] = {0, 0, 0};   // chunk length of the derivative sweeps per direction
+  int CHf[3] = {0, 0, 0};  // chunk length of the filter sweeps per direction
   double* stats_dev = nullptr;
   double* staging = nullptr;  // nh doubles (FP32 form: host <-> device conversions)
   double* staging2 = nullptr; // second buffer: copies overlap conversions
@@ -819,7 +820,7 @@ template <typename T, int DIR>
 int launch_filter(astr_ctx* c, int do_q2f) {
   prof_begin(c, KC_FILTER);
   const cudaError_t e = astr::launch_filter<T, DIR>(sctx<T>(c), sch_f<T>(c, DIR), ftab<T>(c),
-                                                    c->CH[DIR], do_q2f);
+                                                    c->CHf[DIR], do_q2f);
   prof_end(c);
   return launch_result(c, e, "k_filter");
 }
@@ -1193,9 +1194,14 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
   c->prec = params->precision;
   const int dimv[3] = {dims->im, dims->jm, dims->km};
   for (int d = 0; d < ndims; ++d) {
-    const int nmax = npdc[d] == 4 ? dimv[d] + 1 : dimv[d] + 7;
-    c->CH[d] = pick_ch(nmax);
-    if (c->CH[d] < 0) {
+    // rows of the filter system (dim+7 periodic) and the derivative system
+    // (dim+3); x derivative sweeps hold a line in one warp (32 chunks), the
+    // filters and y/z sweeps in a block (NCH_B chunks)
+    const int nf = npdc[d] == 4 ? dimv[d] + 1 : dimv[d] + 7;
+    const int nd = npdc[d] == 4 ? dimv[d] + 1 : dimv[d] + 3;
+    c->CHf[d] = pick_ch(nf, NCH_B);
+    c->CH[d] = pick_ch(nd, d == 0 ? NCH : NCH_B);
+    if (c->CH[d] < 0 || c->CHf[d] < 0 || nf > NCH * 33) {
       delete c;
       return fail(nullptr, ASTR_ERR_UNSUPPORTED, "line longer than 1049 nodes");
     }
@@ -1288,9 +1294,9 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
   // schemes: per direction derivative + filter, in both precisions
   std::vector<HostScheme> hs;
   for (int dd = 0; dd < 3; ++dd) {
-    const int CH = dd < ndims ? c->CH[dd] : 3;
-    hs.push_back(make_deriv(npdc[dd], std::max(dimv[dd], 1), CH, hft));
-    hs.push_back(make_filter(npdc[dd], std::max(dimv[dd], 1), params->alfa_filter, CH, hft));
+    const int CHd = dd < ndims ? c->CH[dd] : 3, CHf = dd < ndims ? c->CHf[dd] : 3;
+    hs.push_back(make_deriv(npdc[dd], std::max(dimv[dd], 1), CHd, hft));
+    hs.push_back(make_filter(npdc[dd], std::max(dimv[dd], 1), params->alfa_filter, CHf, hft));
   }
   size_t tot = 0;
   for (auto& s : hs) tot += 6 * (size_t)s.n + s.K.size() + s.KD.size();

@@ -47,7 +47,12 @@ constexpr int HMD = 5;       // halo width (src/commvar.F90:184)
 #ifndef ASTR_MINB_X
 #define ASTR_MINB_X 6
 #endif
-constexpr int NCH = 32;                // chunks per line
+#ifndef ASTR_NCH_B
+#define ASTR_NCH_B 32
+#endif
+constexpr int NCH = 32;                // chunks per line, one-warp-per-line layout
+constexpr int NCH_B = ASTR_NCH_B;      // chunks per line, block layouts (32 or 64)
+static_assert(NCH_B == 32 || NCH_B == 64, "block layouts take 32 or 64 chunks per line");
 constexpr int YZ_LINES = ASTR_YZ_LINES;  // lines per block for y/z sweeps
 constexpr int X_LINES = ASTR_X_LINES;    // lines (warps) per block for x sweeps
 constexpr int MINB_YZ = ASTR_MINB_YZ;    // resident blocks per SM asked of the compiler
@@ -245,14 +250,16 @@ __device__ __forceinline__ T scan_bwd_warp(T M, T L, int lane) {
 }
 
 constexpr int SM_PITCH = YZ_LINES + 1;
-constexpr int SCAN_SMEM_WORDS = 2 * NCH * SM_PITCH;
+constexpr int SCAN_SMEM_WORDS = 2 * NCH_B * SM_PITCH;
 
-// y/z sweeps: (M,L) of chunk c = threadIdx.y for line threadIdx.x.
-// Warp w scans line w with lane = chunk.
+// Block layouts: (M,L) of chunk c = threadIdx.y for line threadIdx.x.  Warp
+// w scans line w; each lane takes NCH_B/32 consecutive chunks, composes them
+// in scan order, joins the warp-wide affine scan, and writes each chunk's
+// inclusive carry back.
 template <bool FWD, typename T>
 __device__ __forceinline__ T scan_block(T M, T L, T* sm) {
   T* sM = sm;
-  T* sL = sm + NCH * SM_PITCH;
+  T* sL = sm + NCH_B * SM_PITCH;
   const int tx = threadIdx.x, ty = threadIdx.y;
   sM[ty * SM_PITCH + tx] = M;
   sL[ty * SM_PITCH + tx] = L;
@@ -260,8 +267,22 @@ __device__ __forceinline__ T scan_block(T M, T L, T* sm) {
   const int tid = tx + YZ_LINES * ty;
   const int w = tid >> 5, lane = tid & 31;
   if (w < YZ_LINES) {
-    T m = sM[lane * SM_PITCH + w];
-    T l = sL[lane * SM_PITCH + w];
+    constexpr int CPL = NCH_B / 32;
+    T ml[CPL], ll[CPL];
+#pragma unroll
+    for (int e = 0; e < CPL; ++e) {
+      ml[e] = sM[(lane * CPL + e) * SM_PITCH + w];
+      ll[e] = sL[(lane * CPL + e) * SM_PITCH + w];
+    }
+    // the lane's chunks composed in scan order
+    T m = FWD ? ml[0] : ml[CPL - 1];
+    T l = FWD ? ll[0] : ll[CPL - 1];
+#pragma unroll
+    for (int k = 1; k < CPL; ++k) {
+      const int e = FWD ? k : CPL - 1 - k;
+      l = ll[e] + ml[e] * l;
+      m = ml[e] * m;
+    }
 #pragma unroll
     for (int off = 1; off < 32; off <<= 1) {
       const T Mo = FWD ? __shfl_up_sync(0xffffffffu, m, off) : __shfl_down_sync(0xffffffffu, m, off);
@@ -272,12 +293,24 @@ __device__ __forceinline__ T scan_block(T M, T L, T* sm) {
         m = m * Mo;
       }
     }
-    sL[lane * SM_PITCH + w] = l;
+    if (CPL == 1) {
+      sL[lane * SM_PITCH + w] = l;
+    } else {
+      // carry entering this lane's chunks, then each chunk's inclusive value
+      const T prev = FWD ? __shfl_up_sync(0xffffffffu, l, 1) : __shfl_down_sync(0xffffffffu, l, 1);
+      T carry = FWD ? (lane == 0 ? T(0) : prev) : (lane == 31 ? T(0) : prev);
+#pragma unroll
+      for (int k = 0; k < CPL; ++k) {
+        const int e = FWD ? k : CPL - 1 - k;
+        carry = ll[e] + ml[e] * carry;
+        sL[(lane * CPL + e) * SM_PITCH + w] = carry;
+      }
+    }
   }
   __syncthreads();
   T r;
   if (FWD) r = ty == 0 ? T(0) : sL[(ty - 1) * SM_PITCH + tx];
-  else r = ty == NCH - 1 ? T(0) : sL[(ty + 1) * SM_PITCH + tx];
+  else r = ty == NCH_B - 1 ? T(0) : sL[(ty + 1) * SM_PITCH + tx];
   __syncthreads();
   return r;
 }

@@ -7,7 +7,7 @@
 namespace astr {
 
 template <int DIR, bool XB = false>
-inline dim3 sweep_block() { return warp_lines<DIR, XB>() ? dim3(NCH, X_LINES) : dim3(YZ_LINES, NCH); }
+inline dim3 sweep_block() { return warp_lines<DIR, XB>() ? dim3(NCH, X_LINES) : dim3(YZ_LINES, NCH_B); }
 
 template <int DIR, bool XB = false>
 inline dim3 sweep_grid(const Geo& g) {

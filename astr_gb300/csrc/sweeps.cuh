@@ -8,7 +8,7 @@
 namespace astr {
 
 template <int DIR, bool XB = false>
-constexpr int block_threads() { return warp_lines<DIR, XB>() ? NCH * X_LINES : NCH * YZ_LINES; }
+constexpr int block_threads() { return warp_lines<DIR, XB>() ? NCH * X_LINES : NCH_B * YZ_LINES; }
 template <int DIR, bool XB = false>
 constexpr int min_blocks() { return warp_lines<DIR, XB>() ? MINB_X : MINB_YZ; }
 
