@@ -416,6 +416,128 @@ def channel_state(ia, ja, ka, y, mach=0.5, prandtl=0.72, gamma=1.4, seed=2026120
     return _pack_state(ia, ja, ka, rho, u, v, w, p, T, q5)
 
 
+def grid1d(ia, ja, xmin=-5.0, xmax=5.0):
+    """grid1d (src/gridgeneration.F90:143-173) with a second direction:
+    x = (xmax - xmin)/ia * i + xmin, y = j/ja, z = 0."""
+    x = (xmax - xmin) / float(ia) * np.arange(ia + 1, dtype=np.float64) + xmin
+    y = 1.0 / float(ja) * np.arange(ja + 1, dtype=np.float64)
+    return x, y, np.zeros(1)
+
+
+def shock_tube_fields(kind, x):
+    """rho, u, p of sodini / shuosherini (src/initialisation.F90:283-331
+    and the Sod set-up after it) on the nodes x."""
+    x = np.asarray(x, dtype=np.float64)
+    if kind == "sod":
+        left = x < 0.0
+        rho = np.where(left, 1.0, 0.125)
+        p = np.where(left, 1.0, 0.1)
+        u = np.zeros_like(x)
+    elif kind == "shuosher":
+        left = x < -4.0
+        rho = np.where(left, 3.857143, 1.0 + 0.2 * np.sin(5.0 * x))
+        u = np.where(left, 2.629369, 0.0)
+        p = np.where(left, 10.33333, 1.0)
+    else:
+        raise ValueError(kind)
+    return rho, u, p
+
+
+def shock_tube_state(kind, im, jm, mach=3.0, amp=0.0, gamma=1.4):
+    """Halo-layout 2-D state (km = 0) of the Sod or Shu-Osher tube along x
+    on grid1d nodes, uniform in y unless amp > 0, which multiplies the
+    density by 1 + amp sin(2 pi y) (pressure unchanged) so that the y
+    fluxes do work.  T = p/rho * gamma M^2 (thermal), q5 = p/(gamma-1) +
+    rho |u|^2 / 2."""
+    x, y, _ = grid1d(im, jm)
+    rho1, u1, p1 = shock_tube_fields(kind, x)
+    Y = y.reshape(1, -1, 1)
+    rho = rho1.reshape(-1, 1, 1) * (1.0 + amp * np.sin(2.0 * PI * Y))
+    u = u1.reshape(-1, 1, 1) * np.ones_like(rho)
+    p = p1.reshape(-1, 1, 1) * np.ones_like(rho)
+    v = np.zeros_like(rho)
+    w = np.zeros_like(rho)
+    c = refcal(mach, 1.0, gamma=gamma)
+    T = p / rho * c["const2"]
+    q5 = rho * (T * c["const1"] + 0.5 * (u * u + v * v + w * w))
+    return _pack_state(im, jm, 0, rho, u, v, w, p, T, q5)
+
+
+def riemann_exact(left, right, x, t, x0=0.0, gamma=1.4):
+    """Exact solution of the 1-D Riemann problem for the Euler equations
+    (ideal gas), states (rho, u, p): star pressure by Newton iteration on
+    the pressure function and sampling of the wave fan (Toro, Riemann
+    Solvers and Numerical Methods for Fluid Dynamics, 3rd ed., ch. 4).
+    Returns rho, u, p at x and time t > 0."""
+    rl, ul, pl = left
+    rr, ur, pr = right
+    g = gamma
+    cl, cr = np.sqrt(g * pl / rl), np.sqrt(g * pr / rr)
+
+    def fk(p, rk, pk, ck):
+        if p > pk:  # shock
+            A, B = 2.0 / ((g + 1.0) * rk), (g - 1.0) / (g + 1.0) * pk
+            s = np.sqrt(A / (p + B))
+            return (p - pk) * s, s * (1.0 - 0.5 * (p - pk) / (B + p))
+        r = p / pk  # rarefaction
+        return (2.0 * ck / (g - 1.0) * (r ** ((g - 1.0) / (2.0 * g)) - 1.0),
+                1.0 / (rk * ck) * r ** (-(g + 1.0) / (2.0 * g)))
+
+    p = max(1e-8, 0.5 * (pl + pr))
+    for _ in range(100):
+        f1, d1 = fk(p, rl, pl, cl)
+        f2, d2 = fk(p, rr, pr, cr)
+        dp = (f1 + f2 + ur - ul) / (d1 + d2)
+        p_new = max(1e-12, p - dp)
+        if abs(p_new - p) < 1e-14 * p:
+            p = p_new
+            break
+        p = p_new
+    f1, _ = fk(p, rl, pl, cl)
+    f2, _ = fk(p, rr, pr, cr)
+    us = 0.5 * (ul + ur) + 0.5 * (f2 - f1)
+    S = (np.asarray(x, dtype=np.float64) - x0) / t
+    rho = np.empty_like(S)
+    uu = np.empty_like(S)
+    pp = np.empty_like(S)
+    gm = (g - 1.0) / (g + 1.0)
+    for n, s in enumerate(S.ravel()):
+        if s <= us:  # left of the contact
+            if p > pl:
+                sl = ul - cl * np.sqrt((g + 1.0) / (2.0 * g) * p / pl + (g - 1.0) / (2.0 * g))
+                st = (rl * ((p / pl + gm) / (gm * p / pl + 1.0)), us, p) if s >= sl else (rl, ul, pl)
+            else:
+                shl = ul - cl
+                cls = cl * (p / pl) ** ((g - 1.0) / (2.0 * g))
+                stl = us - cls
+                if s <= shl:
+                    st = (rl, ul, pl)
+                elif s >= stl:
+                    st = (rl * (p / pl) ** (1.0 / g), us, p)
+                else:
+                    c = 2.0 / (g + 1.0) * (cl + (g - 1.0) / 2.0 * (ul - s))
+                    uf = 2.0 / (g + 1.0) * (cl + (g - 1.0) / 2.0 * ul + s)
+                    st = (rl * (c / cl) ** (2.0 / (g - 1.0)), uf, pl * (c / cl) ** (2.0 * g / (g - 1.0)))
+        else:
+            if p > pr:
+                sr = ur + cr * np.sqrt((g + 1.0) / (2.0 * g) * p / pr + (g - 1.0) / (2.0 * g))
+                st = (rr * ((p / pr + gm) / (gm * p / pr + 1.0)), us, p) if s <= sr else (rr, ur, pr)
+            else:
+                shr = ur + cr
+                crs = cr * (p / pr) ** ((g - 1.0) / (2.0 * g))
+                str_ = us + crs
+                if s >= shr:
+                    st = (rr, ur, pr)
+                elif s <= str_:
+                    st = (rr * (p / pr) ** (1.0 / g), us, p)
+                else:
+                    c = 2.0 / (g + 1.0) * (cr - (g - 1.0) / 2.0 * (ur - s))
+                    uf = 2.0 / (g + 1.0) * (-cr + (g - 1.0) / 2.0 * ur + s)
+                    st = (rr * (c / cr) ** (2.0 / (g - 1.0)), uf, pr * (c / cr) ** (2.0 * g / (g - 1.0)))
+        rho.flat[n], uu.flat[n], pp.flat[n] = st
+    return rho, uu, pp
+
+
 def _pack_state(im, jm, km, rho, u, v, w, p, T, q5):
     full = (im + 2 * HM + 1, jm + 2 * HM + 1, km + 2 * HM + 1)
     sl = (slice(HM, HM + im + 1), slice(HM, HM + jm + 1), slice(HM, HM + km + 1))

@@ -71,11 +71,15 @@ struct orc_ctx {
   double tempconst, tempconst1, pinf, roinf, uinf, tinf;
   double dxm, dym, dzm;  // mini-app uniform spacings
   Scheme fd[3], flt[3];
+  Scheme fuw[3], fdw[3];  // compact upwind / downwind interface-flux schemes
   FilterTables ft;
   // halo arrays
   std::vector<double> q, rho, vel, prs, tmp, x, dxi, jacob, sigma, qflux;
   // interior arrays
   std::vector<double> qrhs, qsave, dvel, dtmp;
+  std::vector<double> ssf;              // shock-sensor function (halo array)
+  std::vector<unsigned char> lshock;    // lshock(0:im,0:jm,0:km)
+  bool sson = false;                    // allocated(lshock)
   double force[3] = {0, 0, 0};
   double massflux_target = 0.0;
   double massflux = 0.0, fbcx = 0.0;  // last statcal values (channel)
@@ -478,6 +482,304 @@ inline void fvar2q_prs_node(orc_ctx& c, long p) {
   c.q[p + 4 * nh] = c.prs[p] * c.const6 + ro * var1;
 }
 
+
+// ---------------------------------------------------------------------------
+// Compact MP convective scheme (conschm 543c)
+// ---------------------------------------------------------------------------
+const double GAMMA = 1.4;  // src/commvar.F90 (ideal gas, no species)
+const double NUM1D6 = 1.0 / 6.0, NUM1D18 = 1.0 / 18.0, NUM19D18 = 19.0 / 18.0;
+const double NUM5D9 = 5.0 / 9.0, NUM9D36 = 9.0 / 36.0, NUM2D15 = 2.0 / 15.0;
+const double NUM37D60 = 37.0 / 60.0;  // src/constdef.F90:15-26
+
+// compact_flux_initiate, src/flux.F90:32-112 (scheme 543)
+void compact_flux_initiate(Scheme& s, int ntype, int dim, int wind, double b) {
+  int i0 = -2, imx = dim + 1;
+  switch (ntype) {
+    case 1: i0 = -1; imx = dim + 1; break;
+    case 2: i0 = -2; imx = dim; break;
+    case 3: i0 = -2; imx = dim + 1; break;
+    default: i0 = -1; imx = dim; break;
+  }
+  s.first = i0; s.last = imx; s.dim = dim; s.ntype = ntype;
+  s.alloc();
+  const double lo = 0.5 - NUM1D6 * b, hi = NUM1D6 + NUM1D6 * b;
+  for (int i = 0; i < s.n(); ++i) {
+    s.a[i] = wind > 0 ? lo : hi;
+    s.c[i] = wind > 0 ? hi : lo;
+  }
+  s.a[0] = 0.0; s.c[0] = 0.0;
+  s.a[imx - i0] = 0.0; s.c[imx - i0] = 0.0;
+  if (ntype == 1 || ntype == 4) {
+    s.a[0] = 2.0; s.c[0] = 2.0;
+    s.a[1] = 0.25; s.c[1] = 0.25;
+  }
+  if (ntype == 2 || ntype == 4) {
+    s.a[imx - i0] = 2.0; s.c[imx - i0] = 2.0;
+    s.a[imx - 1 - i0] = 0.25; s.c[imx - 1 - i0] = 0.25;
+  }
+  s.preprocess();
+}
+
+// compact_flux_rhs, src/flux.F90:163-256 ; flux_compact 125-150.
+// f points at node 0 (valid -HM..dim+HM); fh receives interfaces -1..dim.
+void flux_compact(const Scheme& s, int wind, double b, const double* f, double* fh, double* d,
+                  double* xx) {
+  const int i0 = s.first, imx = s.last, nt = s.ntype;
+  auto D = [&](int j) -> double& { return d[j - i0]; };
+  int is_ = i0 + 1, ie_ = imx - 1;
+  if (nt == 1 || nt == 4) {
+    int j = i0;
+    D(j) = 2.5 * f[j + 1] + 0.5 * f[j + 2];
+    j = i0 + 1;
+    D(j) = 0.75 * f[j] + 0.75 * f[j + 1];
+    is_ = i0 + 2;
+  } else {
+    int j = i0;
+    double v1 = f[j] + f[j + 1], v2 = f[j - 1] + f[j + 2], v3 = f[j - 2] + f[j + 3];
+    D(j) = NUM37D60 * v1 - NUM2D15 * v2 + NUM1D60 * v3;
+  }
+  if (nt == 2 || nt == 4) {
+    int j = imx - 1;
+    D(j) = 0.75 * f[j + 1] + 0.75 * f[j];
+    j = imx;
+    D(j) = 2.5 * f[j] + 0.5 * f[j - 1];
+    ie_ = imx - 2;
+  } else {
+    int j = imx;
+    double v1 = f[j] + f[j + 1], v2 = f[j - 1] + f[j + 2], v3 = f[j - 2] + f[j + 3];
+    D(j) = NUM37D60 * v1 - NUM2D15 * v2 + NUM1D60 * v3;
+  }
+  const double w0 = NUM1D18 - NUM1D36 * b, w1 = NUM19D18 - NUM9D36 * b;
+  const double w2 = NUM5D9 + NUM9D36 * b, w3 = NUM1D36 * b;
+  if (wind > 0) {
+    for (int j = is_; j <= ie_; ++j) D(j) = w0 * f[j - 1] + w1 * f[j] + w2 * f[j + 1] + w3 * f[j + 2];
+  } else {
+    for (int j = is_; j <= ie_; ++j) D(j) = w0 * f[j + 2] + w1 * f[j + 1] + w2 * f[j] + w3 * f[j - 1];
+  }
+  s.solve(d, xx);
+  for (int j = -1; j <= s.dim; ++j) fh[j + 1] = xx[j - i0];
+}
+
+// flux_steger_warming, src/riemann.F90:23-160 (nondimensional, no species)
+void steger_warming(double mach, double rho, const double* vel, double prs, double tmp,
+                    const double* q, const double* dxi, double jac, double* fp, double* fm) {
+  const double eps = 0.04;
+  const double uu = dxi[0] * vel[0] + dxi[1] * vel[1] + dxi[2] * vel[2];
+  const double var0 = 1.0 / std::sqrt(dxi[0] * dxi[0] + dxi[1] * dxi[1] + dxi[2] * dxi[2]);
+  const double gpd[3] = {dxi[0] * var0, dxi[1] * var0, dxi[2] * var0};
+  const double gm2 = 0.5 / GAMMA;
+  const double css = std::sqrt(tmp) / mach;  // sos, src/fludyna.F90:832-859
+  const double csa = css / var0;
+  const double lmach = uu / csa;
+  if (lmach >= 1.0) {
+    fp[0] = jac * q[0] * uu;
+    fp[1] = jac * (q[1] * uu + dxi[0] * prs);
+    fp[2] = jac * (q[2] * uu + dxi[1] * prs);
+    fp[3] = jac * (q[3] * uu + dxi[2] * prs);
+    fp[4] = jac * (q[4] + prs) * uu;
+    for (int n = 0; n < 5; ++n) fm[n] = 0.0;
+    return;
+  }
+  if (lmach <= -1.0) {
+    for (int n = 0; n < 5; ++n) fp[n] = 0.0;
+    fm[0] = jac * q[0] * uu;
+    fm[1] = jac * (q[1] * uu + dxi[0] * prs);
+    fm[2] = jac * (q[2] * uu + dxi[1] * prs);
+    fm[3] = jac * (q[3] * uu + dxi[2] * prs);
+    fm[4] = jac * (q[4] + prs) * uu;
+    return;
+  }
+  const double lmda[3] = {uu, uu + csa, uu - csa};  // lmda(1)=lmda(2)=lmda(3), (4), (5)
+  double lp[3], lm[3];
+  for (int n = 0; n < 3; ++n) {
+    lp[n] = 0.5 * (lmda[n] + std::sqrt(lmda[n] * lmda[n] + eps * eps));
+    lm[n] = lmda[n] - lp[n];
+  }
+  const double fhi = 0.5 * (GAMMA - 1.0) * (vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]);
+  const double jro = jac * rho;
+  for (int s = 0; s < 2; ++s) {
+    const double* L = s == 0 ? lp : lm;
+    double* F = s == 0 ? fp : fm;
+    const double var1 = L[0];
+    const double var2 = L[1] - L[2];
+    const double var3 = 2.0 * L[0] - L[1] - L[2];
+    const double var4 = var1 - var3 * gm2;
+    F[0] = jro * var4;
+    F[1] = jro * (var4 * vel[0] + var2 * css * gpd[0] * gm2);
+    F[2] = jro * (var4 * vel[1] + var2 * css * gpd[1] * gm2);
+    F[3] = jro * (var4 * vel[2] + var2 * css * gpd[2] * gm2);
+    F[4] = jac * (var1 * q[4] + rho * (var2 * uu * var0 * css * gm2 -
+                                       var3 * (fhi + css * css) * gm2 / (GAMMA - 1.0)));
+  }
+}
+
+// chardecomp, src/solver.F90:1958-2162 (no species).  st = {T, rho, p, E,
+// u, v, w, dxi1, dxi2, dxi3}.  R, L column-major 5x5: R[(m-1)+5(n-1)] = REV(m,n).
+void chardecomp(const double* stl, const double* str, double* R, double* L) {
+  auto rv = [&](int m, int n) -> double& { return R[(m - 1) + 5 * (n - 1)]; };
+  auto lv = [&](int m, int n) -> double& { return L[(m - 1) + 5 * (n - 1)]; };
+  const double ro_l = stl[1], p_l = stl[2], E_l = stl[3];
+  const double ro_r = str[1], p_r = str[2], E_r = str[3];
+  const double* vl = stl + 4;
+  const double* vr = str + 4;
+  const double rero = 1.e-12;
+  const double WRoe = std::sqrt(ro_l) / (std::sqrt(ro_l) + std::sqrt(ro_r));
+  const double WRoe1 = 1.0 - WRoe;
+  const double u1 = WRoe * vl[0] + WRoe1 * vr[0];
+  const double u2 = WRoe * vl[1] + WRoe1 * vr[1];
+  const double u3 = WRoe * vl[2] + WRoe1 * vr[2];
+  const double KRoe = 0.5 * (u1 * u1 + u2 * u2 + u3 * u3);
+  const double HL = (E_l + p_l) / ro_l;
+  const double HR = (E_r + p_r) / ro_r;
+  const double HRoe = WRoe * HL + WRoe1 * HR;
+  const double Css = std::sqrt((GAMMA - 1.0) * (HRoe - KRoe));
+  const double rcs = 1.0 / Css;
+  const double var1 = 0.5 * (stl[7] + str[7]);
+  const double var2 = 0.5 * (stl[8] + str[8]);
+  const double var3 = 0.5 * (stl[9] + str[9]);
+  const double var4 = 1.0 / std::sqrt(var1 * var1 + var2 * var2 + var3 * var3);
+  const double g1 = var1 * var4, g2 = var2 * var4, g3 = var3 * var4;
+  const double ugp = u1 * g1 + u2 * g2 + u3 * g3;
+  const double b1 = (GAMMA - 1.0) / (Css * Css);
+  const double b2 = 1.0 + 2.0 * b1 * KRoe - b1 * HRoe;
+  lv(1, 1) = 0.5 * (b2 + ugp * rcs);
+  lv(1, 2) = -0.5 * (b1 * u1 + g1 * rcs);
+  lv(1, 3) = -0.5 * (b1 * u2 + g2 * rcs);
+  lv(1, 4) = -0.5 * (b1 * u3 + g3 * rcs);
+  lv(1, 5) = 0.5 * b1;
+  rv(1, 1) = 1.0;
+  rv(2, 1) = u1 - Css * g1;
+  rv(3, 1) = u2 - Css * g2;
+  rv(4, 1) = u3 - Css * g3;
+  rv(5, 1) = HRoe - ugp * Css;
+  lv(2, 1) = 1.0 - b2;
+  lv(2, 2) = b1 * u1;
+  lv(2, 3) = b1 * u2;
+  lv(2, 4) = b1 * u3;
+  lv(2, 5) = -b1;
+  rv(1, 2) = 1.0;
+  rv(2, 2) = u1;
+  rv(3, 2) = u2;
+  rv(4, 2) = u3;
+  rv(5, 2) = HRoe - 1.0 / b1;
+  if (std::fabs(var1) > rero) {
+    const double rgp = 1.0 / g1;
+    lv(3, 1) = (ugp * g2 - u2) * rgp;
+    lv(3, 2) = -g2;
+    lv(3, 3) = (1.0 - g2 * g2) * rgp;
+    lv(3, 4) = -g2 * g3 * rgp;
+    lv(3, 5) = 0.0;
+    lv(4, 1) = (ugp * g3 - u3) * rgp;
+    lv(4, 2) = -g3;
+    lv(4, 3) = -g2 * g3 * rgp;
+    lv(4, 4) = (1.0 - g3 * g3) * rgp;
+    lv(4, 5) = 0.0;
+    rv(1, 3) = 0.0; rv(2, 3) = -g2; rv(3, 3) = g1; rv(4, 3) = 0.0; rv(5, 3) = u2 * g1 - u1 * g2;
+    rv(1, 4) = 0.0; rv(2, 4) = -g3; rv(3, 4) = 0.0; rv(4, 4) = g1; rv(5, 4) = u3 * g1 - u1 * g3;
+  } else if (std::fabs(var2) > rero) {
+    const double rgp = 1.0 / g2;
+    lv(3, 1) = (ugp * g1 - u1) * rgp;
+    lv(3, 2) = (1.0 - g1 * g1) * rgp;
+    lv(3, 3) = -g1;
+    lv(3, 4) = -g1 * g3 * rgp;
+    lv(3, 5) = 0.0;
+    lv(4, 1) = (ugp * g3 - u3) * rgp;
+    lv(4, 2) = -g1 * g3 * rgp;
+    lv(4, 3) = -g3;
+    lv(4, 4) = (1.0 - g3 * g3) * rgp;
+    lv(4, 5) = 0.0;
+    rv(1, 3) = 0.0; rv(2, 3) = g2; rv(3, 3) = -g1; rv(4, 3) = 0.0; rv(5, 3) = u1 * g2 - u2 * g1;
+    rv(1, 4) = 0.0; rv(2, 4) = 0.0; rv(3, 4) = -g3; rv(4, 4) = g2; rv(5, 4) = u3 * g2 - u2 * g3;
+  } else {
+    // the reference stops when all three components are below rero
+    const double rgp = 1.0 / g3;
+    lv(3, 1) = (ugp * g1 - u1) * rgp;
+    lv(3, 2) = (1.0 - g1 * g1) * rgp;
+    lv(3, 3) = -g1 * g2 * rgp;
+    lv(3, 4) = -g1;
+    lv(3, 5) = 0.0;
+    lv(4, 1) = (ugp * g2 - u2) * rgp;
+    lv(4, 2) = -g1 * g2 * rgp;
+    lv(4, 3) = (1.0 - g2 * g2) * rgp;
+    lv(4, 4) = -g2;
+    lv(4, 5) = 0.0;
+    rv(1, 3) = 0.0; rv(2, 3) = g3; rv(3, 3) = 0.0; rv(4, 3) = -g1; rv(5, 3) = u1 * g3 - u3 * g1;
+    rv(1, 4) = 0.0; rv(2, 4) = 0.0; rv(3, 4) = g3; rv(4, 4) = -g2; rv(5, 4) = u2 * g3 - u3 * g2;
+  }
+  lv(5, 1) = 0.5 * (b2 - ugp * rcs);
+  lv(5, 2) = -0.5 * (b1 * u1 - g1 * rcs);
+  lv(5, 3) = -0.5 * (b1 * u2 - g2 * rcs);
+  lv(5, 4) = -0.5 * (b1 * u3 - g3 * rcs);
+  lv(5, 5) = 0.5 * b1;
+  rv(1, 5) = 1.0;
+  rv(2, 5) = u1 + Css * g1;
+  rv(3, 5) = u2 + Css * g2;
+  rv(4, 5) = u3 + Css * g3;
+  rv(5, 5) = HRoe + ugp * Css;
+}
+
+// minmod2, minmod4: src/commfunc.F90:699-738
+inline double minmod2(double a, double b) {
+  if (a > 0.0 && b > 0.0) return std::min(std::fabs(a), std::fabs(b));
+  if (a < 0.0 && b < 0.0) return -1.0 * std::min(std::fabs(a), std::fabs(b));
+  return 0.0;
+}
+inline double minmod4(double a, double b, double c, double d) {
+  if (a > 0.0 && b > 0.0 && c > 0.0 && d > 0.0)
+    return std::min(std::min(std::fabs(a), std::fabs(b)), std::min(std::fabs(c), std::fabs(d)));
+  if (a < 0.0 && b < 0.0 && c < 0.0 && d < 0.0)
+    return -1.0 * std::min(std::min(std::fabs(a), std::fabs(b)), std::min(std::fabs(c), std::fabs(d)));
+  return 0.0;
+}
+
+// MP5 with a supplied linear value, src/flux.F90:434-496 (Suresh & Huynh 1997)
+double mp5(const double* u, double ulinear, bool lskt) {
+  const double u1 = u[0], u2 = u[1], u3 = u[2], u4 = u[3], u5 = u[4];
+  double var1 = u4 - u3;
+  double var2 = 4.0 * (u3 - u2);
+  const double uMP = u3 + minmod2(var1, var2);
+  var1 = (ulinear - u3) * (ulinear - uMP);
+  if (lskt && var1 >= 1.e-10) {
+    const double dm1 = u1 - 2.0 * u2 + u3;
+    const double d0 = u2 - 2.0 * u3 + u4;
+    const double d1 = u3 - 2.0 * u4 + u5;
+    const double dhm1 = minmod4(4.0 * dm1 - d0, 4.0 * d0 - dm1, dm1, d0);
+    const double dh0 = minmod4(4.0 * d0 - d1, 4.0 * d1 - d0, d0, d1);
+    const double uUL = u3 + 4.0 * (u3 - u2);
+    const double uAV = 0.5 * (u3 + u4);
+    const double uMD = uAV - 0.5 * dh0;
+    const double uLC = u3 + 0.5 * (u3 - u2) + 1.333333333333333 * dhm1;
+    const double uMIN = std::max(std::min(std::min(u3, u4), uMD), std::min(std::min(u3, uUL), uLC));
+    const double uMAX = std::min(std::max(std::max(u3, u4), uMD), std::max(std::max(u3, uUL), uLC));
+    return ulinear + minmod2(uMIN - ulinear, uMAX - ulinear);
+  }
+  return ulinear;
+}
+
+// mplimiter, src/flux.F90:363-379
+inline double mplimiter(const double* f, double fl, bool shock, int inode, int dim, int ntype) {
+  if ((ntype == 1 && inode == 0) || (ntype == 2 && inode == dim - 1) || (ntype == 1 && inode == 1) ||
+      (ntype == 2 && inode == dim - 2))
+    return fl;
+  return mp5(f, fl, shock);
+}
+
+// iwind6, src/solver.F90:1236-1257
+inline int iwind6(int i, int n, int imin, int imax, int dir) {
+  int w = dir > 0 ? i + n - 3 : i + 4 - n;
+  if (w < imin) w = imin;
+  if (w > imax) w = imax;
+  return w;
+}
+
+// node range of the flux split (iss..iee), src/solver.F90:1318-1332
+inline void split_range(int npdc, int dim, int& a, int& b) {
+  if (npdc == 1) { a = 0; b = dim + HM; }
+  else if (npdc == 2) { a = -HM; b = dim; }
+  else if (npdc == 3) { a = -HM; b = dim + HM; }
+  else { a = 0; b = dim; }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -524,6 +826,14 @@ orc_ctx* orc_create(const orc_config* cfg) {
   compact_filter_initiate(c->flt[0], cfg->npdci, c->im, cfg->alfa_filter);
   compact_filter_initiate(c->flt[1], cfg->npdcj, c->jm, cfg->alfa_filter);
   compact_filter_initiate(c->flt[2], cfg->npdck, c->km, cfg->alfa_filter);
+  if (cfg->conschm_mp) {
+    const int np[3] = {cfg->npdci, cfg->npdcj, cfg->npdck};
+    const int dm[3] = {c->im, c->jm, c->km};
+    for (int d = 0; d < 3; ++d) {
+      compact_flux_initiate(c->fuw[d], np[d], dm[d], +1, cfg->bfacmpld);
+      compact_flux_initiate(c->fdw[d], np[d], dm[d], -1, cfg->bfacmpld);
+    }
+  }
   // commarray allocation (src/commarray.F90:56-108)
   c->q.assign(5 * c->nh, 0.0);
   c->rho.assign(c->nh, 0.0); c->prs.assign(c->nh, 0.0); c->tmp.assign(c->nh, 0.0);
@@ -537,6 +847,11 @@ orc_ctx* orc_create(const orc_config* cfg) {
   c->qsave.assign(5 * c->n0, 0.0);
   c->dvel.assign(9 * c->n0, 0.0);
   c->dtmp.assign(3 * c->n0, 0.0);
+  // the sensor's work array: halos of directions without a periodic copy
+  // are never written by the reference (it reads them as allocated); here
+  // they hold zero
+  c->ssf.assign(c->nh, 0.0);
+  c->lshock.assign(c->n0, 0);
   return c;
 }
 
@@ -554,6 +869,7 @@ double* orc_field(orc_ctx* c, const char* name) {
   if (s == "jacob") return c->jacob.data();
   if (s == "sigma") return c->sigma.data();
   if (s == "qflux") return c->qflux.data();
+  if (s == "ssf") return c->ssf.data();
   if (s == "qrhs") return c->qrhs.data();
   if (s == "qsave") return c->qsave.data();
   if (s == "dvel") return c->dvel.data();
@@ -1276,9 +1592,209 @@ void orc_diffrsdcal6(orc_ctx* c) {
   }
 }
 
+
+// ducrossensor, src/commcal.F90:196-353
+void orc_ducrossensor(orc_ctx* c) {
+  const int im = c->im, jm = c->jm, km = c->km;
+  const long n0 = c->n0;
+  const int npi = c->cfg.npdci, npj = c->cfg.npdcj, npk = c->cfg.npdck;
+#pragma omp parallel for collapse(2)
+  for (int k = 0; k <= km; ++k)
+    for (int j = 0; j <= jm; ++j)
+      for (int i = 0; i <= im; ++i) {
+        const long zp = c->z(i, j, k);
+        auto dv = [&](int n, int m) { return c->dvel[zp + ((n - 1) + 3 * (m - 1)) * n0]; };
+        const double dsum = dv(1, 1) + dv(2, 2) + dv(3, 3);
+        const double div2 = dsum * dsum;
+        const double vortx = dv(3, 2) - dv(2, 3);
+        const double vorty = dv(1, 3) - dv(3, 1);
+        const double vortz = dv(2, 1) - dv(1, 2);
+        const double vort = vortx * vortx + vorty * vorty + vortz * vortz;
+        int ip1 = i + 1, im1 = i - 1, jp1 = j + 1, jm1 = j - 1, kp1 = k + 1, km1 = k - 1;
+        if (npi == 1 && im1 < 0) im1 = 0;
+        if (npj == 1 && jm1 < 0) jm1 = 0;
+        if (npk == 1 && km1 < 0) km1 = 0;
+        if (npi == 2 && ip1 > im) ip1 = im;
+        if (npj == 2 && jp1 > jm) jp1 = jm;
+        if (npk == 2 && kp1 > km) kp1 = km;
+        const double* P = c->prs.data();
+        const double p0 = P[c->h(i, j, k)];
+        auto dp = [&](double pm, double pp) {
+          return std::fabs(pp - 2.0 * p0 + pm) / (pp + 2.0 * p0 + pm);
+        };
+        const double dpdi = dp(P[c->h(im1, j, k)], P[c->h(ip1, j, k)]);
+        const double dpdj = dp(P[c->h(i, jm1, k)], P[c->h(i, jp1, k)]);
+        const double dpdk = dp(P[c->h(i, j, km1)], P[c->h(i, j, kp1)]);
+        c->ssf[c->h(i, j, k)] = div2 / (div2 + vort + 1.e-30) * std::max(std::max(dpdi, dpdj), dpdk);
+      }
+  dataswap(*c, c->ssf.data(), 1, 0);
+#pragma omp parallel for collapse(2)
+  for (int k = 0; k <= km; ++k)
+    for (int j = 0; j <= jm; ++j)
+      for (int i = 0; i <= im; ++i) {
+        double mx = 0.0;
+        for (int i1 = -HM + 1; i1 <= HM; ++i1) {
+          int ii = i + i1;
+          if (npi == 1 && ii < 0) ii = 0;
+          if (npi == 2 && ii > im) ii = im;
+          mx = std::max(mx, c->ssf[c->h(ii, j, k)]);
+        }
+        for (int j1 = -HM + 1; j1 <= HM; ++j1) {
+          int jj = j + j1;
+          if (npj == 1 && jj < 0) jj = 0;
+          if (npj == 2 && jj > jm) jj = jm;
+          mx = std::max(mx, c->ssf[c->h(i, jj, k)]);
+        }
+        for (int k1 = -HM + 1; k1 <= HM; ++k1) {
+          int kk = k + k1;
+          if (npk == 1 && kk < 0) kk = 0;
+          if (npk == 2 && kk > km) kk = km;
+          mx = std::max(mx, c->ssf[c->h(i, j, kk)]);
+        }
+        c->lshock[c->z(i, j, k)] = mx > c->cfg.shkcrt ? 1 : 0;
+      }
+  c->sson = true;
+}
+
+int orc_lshock(orc_ctx* c, unsigned char* out) {
+  if (!c->sson) return 0;
+  std::memcpy(out, c->lshock.data(), c->lshock.size());
+  return 1;
+}
+
+// convrsdcmp, src/solver.F90:1271-1937 (no species, crinod all false: the
+// reference sets it only in crash recovery, src/mainloop.F90:81, 738)
+void orc_convrsdcmp(orc_ctx* c) {
+  const long nh = c->nh, n0 = c->n0;
+  const int mx = std::max(c->im, std::max(c->jm, c->km));
+  const bool chard = c->cfg.lchardecomp != 0;
+  const double mach = c->cfg.mach, bf = c->cfg.bfacmpld;
+  for (int d = 0; d < c->ndims; ++d) {
+    const int dim = c->dimof(d), npdc = c->npdc(d);
+    const long hs = c->hstride(d), sz = c->zstride(d);
+    int a0, a1, b0, b1, l0, l1;
+    if (d == 0) { a0 = c->js; a1 = c->je; b0 = c->ks; b1 = c->ke; l0 = c->is; l1 = c->ie; }
+    else if (d == 1) { a0 = c->is; a1 = c->ie; b0 = c->ks; b1 = c->ke; l0 = c->js; l1 = c->je; }
+    else { a0 = c->is; a1 = c->ie; b0 = c->js; b1 = c->je; l0 = c->ks; l1 = c->ke; }
+    int iss, iee;
+    split_range(npdc, dim, iss, iee);
+    for_lines(*c, d, a0, a1, b0, b1, [&](int a, int b) {
+      thread_local std::vector<double> fsw, fhc, Fh, dd, xx;
+      const int L = mx + 2 * HM + 1;
+      if (a < 0) {
+        fsw.assign(10 * L, 0.0); fhc.assign(10 * (mx + 2), 0.0); Fh.assign(5 * (mx + 2), 0.0);
+        dd.assign(mx + 16, 0.0); xx.assign(mx + 16, 0.0);
+        return;
+      }
+      const long h0 = hpos(*c, d, 0, a, b), z0 = zpos(*c, d, 0, a, b);
+      auto FP = [&](int n, int l) -> double& { return fsw[n * L + l + HM]; };
+      auto FM = [&](int n, int l) -> double& { return fsw[(5 + n) * L + l + HM]; };
+      for (int l = iss; l <= iee; ++l) {
+        const long p = h0 + hs * l;
+        const double vel[3] = {c->vel[p], c->vel[p + nh], c->vel[p + 2 * nh]};
+        const double q[5] = {c->q[p], c->q[p + nh], c->q[p + 2 * nh], c->q[p + 3 * nh], c->q[p + 4 * nh]};
+        const double xr[3] = {c->dxi[p + (d + 0) * nh], c->dxi[p + (d + 3) * nh], c->dxi[p + (d + 6) * nh]};
+        double fp[5], fm[5];
+        steger_warming(mach, c->rho[p], vel, c->prs[p], c->tmp[p], q, xr, c->jacob[p], fp, fm);
+        for (int n = 0; n < 5; ++n) { FP(n, l) = fp[n]; FM(n, l) = fm[n]; }
+      }
+      for (int n = 0; n < 5; ++n) {
+        flux_compact(c->fuw[d], +1, bf, &FP(n, 0), fhc.data() + n * (mx + 2), dd.data(), xx.data());
+        flux_compact(c->fdw[d], -1, bf, &FM(n, 0), fhc.data() + (5 + n) * (mx + 2), dd.data(), xx.data());
+      }
+      auto HCP = [&](int n, int i) { return fhc[n * (mx + 2) + i + 1]; };
+      auto HCM = [&](int n, int i) { return fhc[(5 + n) * (mx + 2) + i + 1]; };
+      auto state = [&](int l, double* st) {
+        const long p = h0 + hs * l;
+        st[0] = c->tmp[p]; st[1] = c->rho[p]; st[2] = c->prs[p]; st[3] = c->q[p + 4 * nh];
+        st[4] = c->vel[p]; st[5] = c->vel[p + nh]; st[6] = c->vel[p + 2 * nh];
+        st[7] = c->dxi[p + (d + 0) * nh]; st[8] = c->dxi[p + (d + 3) * nh]; st[9] = c->dxi[p + (d + 6) * nh];
+      };
+      auto lsh_at = [&](int l) { return c->lshock[z0 + sz * l] != 0; };
+      for (int i = l0 - 1; i <= l1; ++i) {
+        double R[25], Lv[25], flcp[5][5], flcm[5][5], fhcpc[5], fhcmc[5];
+        if (chard) {
+          double sl[10], sr[10];
+          state(i, sl);
+          state(i + 1, sr);
+          chardecomp(sl, sr, R, Lv);
+          auto lev = [&](int m, int k) { return Lv[m + 5 * k]; };
+          for (int m = 0; m < 5; ++m) {
+            for (int n = 1; n <= 5; ++n) {
+              int w = iwind6(i, n, iss, iee, +1);
+              flcp[m][n - 1] = lev(m, 0) * FP(0, w) + lev(m, 1) * FP(1, w) + lev(m, 2) * FP(2, w) +
+                               lev(m, 3) * FP(3, w) + lev(m, 4) * FP(4, w);
+              w = iwind6(i, n, iss, iee, -1);
+              flcm[m][n - 1] = lev(m, 0) * FM(0, w) + lev(m, 1) * FM(1, w) + lev(m, 2) * FM(2, w) +
+                               lev(m, 3) * FM(3, w) + lev(m, 4) * FM(4, w);
+            }
+            fhcpc[m] = lev(m, 0) * HCP(0, i) + lev(m, 1) * HCP(1, i) + lev(m, 2) * HCP(2, i) +
+                       lev(m, 3) * HCP(3, i) + lev(m, 4) * HCP(4, i);
+            fhcmc[m] = lev(m, 0) * HCM(0, i) + lev(m, 1) * HCM(1, i) + lev(m, 2) * HCM(2, i) +
+                       lev(m, 3) * HCM(3, i) + lev(m, 4) * HCM(4, i);
+          }
+        } else {
+          for (int n = 1; n <= 5; ++n) {
+            const int wp = iwind6(i, n, iss, iee, +1), wm = iwind6(i, n, iss, iee, -1);
+            for (int m = 0; m < 5; ++m) { flcp[m][n - 1] = FP(m, wp); flcm[m][n - 1] = FM(m, wm); }
+          }
+          for (int m = 0; m < 5; ++m) { fhcpc[m] = HCP(m, i); fhcmc[m] = HCM(m, i); }
+        }
+        bool lsh = true;
+        if (c->sson) {
+          if (i < 0) lsh = lsh_at(i + 1);
+          else if (i + 1 > dim) lsh = lsh_at(i);
+          else lsh = lsh_at(i) || lsh_at(i + 1);
+        }
+        double Fhc[5];
+        for (int m = 0; m < 5; ++m) {
+          const double v1 = mplimiter(flcp[m], fhcpc[m], lsh, i, dim, npdc);
+          const double v2 = mplimiter(flcm[m], fhcmc[m], lsh, i, dim, npdc);
+          Fhc[m] = v1 + v2;
+        }
+        for (int m = 0; m < 5; ++m) {
+          double v = Fhc[m];
+          if (chard)
+            v = R[m] * Fhc[0] + R[m + 5] * Fhc[1] + R[m + 10] * Fhc[2] + R[m + 15] * Fhc[3] +
+                R[m + 20] * Fhc[4];
+          Fh[m * (mx + 2) + i + 1] = v;
+        }
+      }
+      for (int l = l0; l <= l1; ++l)
+        for (int m = 0; m < 5; ++m) {
+          double& r = c->qrhs[z0 + sz * l + m * n0];
+          r = r + Fh[m * (mx + 2) + l + 1] - Fh[m * (mx + 2) + l];
+        }
+    });
+  }
+}
+
+void orc_line_flux(orc_ctx* c, int dir, int wind, const double* f, double* fh) {
+  const int dim = c->dimof(dir);
+  std::vector<double> d(dim + 16), xx(dim + 16);
+  const Scheme& s = wind > 0 ? c->fuw[dir] : c->fdw[dir];
+  flux_compact(s, wind, c->cfg.bfacmpld, f + HM, fh, d.data(), xx.data());
+}
+
+double orc_mp5(const double* u5, double ul, int discont) { return mp5(u5, ul, discont != 0); }
+
+void orc_steger_warming(orc_ctx* c, const double* prim, const double* q5, const double* dxi3,
+                        double jac, double* fp, double* fm) {
+  steger_warming(c->cfg.mach, prim[0], prim + 1, prim[4], prim[5], q5, dxi3, jac, fp, fm);
+}
+
+void orc_chardecomp(const double* stl, const double* str, double* rev, double* lev) {
+  chardecomp(stl, str, rev, lev);
+}
+
 // rhscal, src/solver.F90:185-282 (main) ; tgvsolver.F90:962-992 (mini-app)
 void orc_rhscal(orc_ctx* c) {
-  orc_convrsdcal6(c);
+  if (c->cfg.conschm_mp && c->cfg.mode == ORC_MODE_MAIN) {
+    if (c->cfg.lchardecomp) orc_ducrossensor(c);
+    orc_convrsdcmp(c);
+  } else {
+    orc_convrsdcal6(c);
+  }
   for (auto& r : c->qrhs) r = -r;
   if (c->cfg.diffterm) orc_diffrsdcal6(c);
   if (c->cfg.channel) src_chan(*c);

@@ -48,6 +48,12 @@ typedef struct {
   double mach, reynolds, prandtl, ref_tem, suth_const; /* 110.3 main, 110.4 mini-app */
   double deltat;
   double twall;            /* isothermal wall temperature (channel) */
+  /* convective scheme: 0 = central 643c (convrsdcal6), 1 = compact MP
+   * 543c (convrsdcmp, src/solver.F90:1271-1937) */
+  int conschm_mp;
+  int lchardecomp;         /* characteristic projection + Ducros sensor */
+  double bfacmpld;         /* b factor of the compact upwind scheme */
+  double shkcrt;           /* shock-sensor threshold */
 } orc_config;
 
 orc_ctx* orc_create(const orc_config* cfg);
@@ -55,7 +61,7 @@ void orc_destroy(orc_ctx* c);
 
 /* Direct access to internal arrays (Fortran layout). Names:
  * "q","rho","vel","prs","tmp","x","dxi","jacob" (halo arrays),
- * "qrhs","qsave","dvel","dtmp" (0:im arrays), "sigma","qflux" (halo). */
+ * "qrhs","qsave","dvel","dtmp" (0:im arrays), "sigma","qflux","ssf" (halo). */
 double* orc_field(orc_ctx* c, const char* name);
 /* Scheme coefficients: dir 0..2, kind 0 = derivative, 1 = filter.
  * Copies a,c,ac1,ac2,ac3 for nodes first..last into out (5*n doubles);
@@ -94,6 +100,23 @@ void orc_rk3_steps(orc_ctx* c, int nsteps, double* stats /* 2*nsteps or NULL */)
 /* Stand-alone line kernels (used by the known-answer tests). */
 void orc_line_derivative(orc_ctx* c, int dir, const double* f /* -5..dim+5 */, double* df /* 0..dim */);
 void orc_line_filter(orc_ctx* c, int dir, const double* f, double* ff);
+
+/* Compact MP convective path (conschm 543c). */
+void orc_ducrossensor(orc_ctx* c);  /* ssf, lshock from dvel and prs */
+void orc_convrsdcmp(orc_ctx* c);    /* qrhs += interface-flux differences */
+/* lshock(0:im,0:jm,0:km) as bytes (0/1); returns 0 before the first sensor call */
+int orc_lshock(orc_ctx* c, unsigned char* out);
+/* Line kernels of the MP path: the compact upwind (wind=+1) or downwind
+ * (wind=-1) interface flux fh(-1..dim) of f(-5..dim+5) along dir. */
+void orc_line_flux(orc_ctx* c, int dir, int wind, const double* f, double* fh);
+double orc_mp5(const double* u5, double ul, int discont);
+/* Steger-Warming split at one node: prim = {rho,u,v,w,p,T}, q5, dxi row
+ * (3), jacob -> fplus(5), fminus(5). */
+void orc_steger_warming(orc_ctx* c, const double* prim, const double* q5, const double* dxi3,
+                        double jac, double* fp, double* fm);
+/* Roe-averaged eigenvectors between two nodes: st = {T,rho,p,E,u,v,w,dxi1,dxi2,dxi3}
+ * of the left and right node; REV, LEV (5x5, column-major). */
+void orc_chardecomp(const double* stl, const double* str, double* rev, double* lev);
 
 /* Diagnostics. */
 double orc_kenergy(orc_ctx* c);

@@ -55,6 +55,8 @@ class OrcConfig(ctypes.Structure):
         ("prandtl", ctypes.c_double), ("ref_tem", ctypes.c_double),
         ("suth_const", ctypes.c_double), ("deltat", ctypes.c_double),
         ("twall", ctypes.c_double),
+        ("conschm_mp", ctypes.c_int), ("lchardecomp", ctypes.c_int),
+        ("bfacmpld", ctypes.c_double), ("shkcrt", ctypes.c_double),
     ]
 
 
@@ -90,6 +92,15 @@ def lib():
         L.orc_kenergy.argtypes = [vp]
         L.orc_enstrophy.restype = ctypes.c_double
         L.orc_enstrophy.argtypes = [vp]
+        for name in ("orc_ducrossensor", "orc_convrsdcmp"):
+            getattr(L, name).argtypes = [vp]
+        L.orc_lshock.argtypes = [vp, ctypes.c_void_p]
+        L.orc_lshock.restype = ctypes.c_int
+        L.orc_line_flux.argtypes = [vp, ctypes.c_int, ctypes.c_int, dp, dp]
+        L.orc_mp5.argtypes = [dp, ctypes.c_double, ctypes.c_int]
+        L.orc_mp5.restype = ctypes.c_double
+        L.orc_steger_warming.argtypes = [vp, dp, dp, dp, ctypes.c_double, dp, dp]
+        L.orc_chardecomp.argtypes = [dp, dp, dp, dp]
         L.orc_set_threads.argtypes = [ctypes.c_int]
         L.orc_get_threads.restype = ctypes.c_int
         _lib = L
@@ -102,7 +113,7 @@ def _dptr(a: np.ndarray):
 
 
 HALO_FIELDS = {"q": 5, "rho": 0, "vel": 3, "prs": 0, "tmp": 0, "x": 3, "dxi": 9,
-               "jacob": 0, "sigma": 6, "qflux": 3}
+               "jacob": 0, "sigma": 6, "qflux": 3, "ssf": 0}
 INTERIOR_FIELDS = {"qrhs": 5, "qsave": 5, "dvel": 9, "dtmp": 3}
 
 
@@ -113,14 +124,17 @@ class Oracle:
                  diffterm=True, alfa_filter=0.49, beter_halo=1.11, beter_bound=0.98,
                  mach=0.1, reynolds=1600.0, prandtl=0.72, ref_tem=273.15,
                  suth_const=None, deltat=1e-3, ia=None, ja=None, ka=None, channel=False,
-                 twall=1.0):
+                 twall=1.0, conschm="643c", lchardecomp=True, bfacmpld=0.3, shkcrt=0.01):
         if suth_const is None:
             suth_const = 110.4 if mode == MODE_MINIAPP else 110.3
         self.cfg = OrcConfig(im, jm, km, im if ia is None else ia, jm if ja is None else ja,
                              km if ka is None else ka, npdc[0], npdc[1], npdc[2], mode,
                              int(lfilter), int(diffterm), int(channel), alfa_filter,
                              beter_halo, beter_bound, mach, reynolds, prandtl, ref_tem,
-                             suth_const, deltat, twall)
+                             suth_const, deltat, twall, int(conschm == "543c"),
+                             int(lchardecomp), bfacmpld, shkcrt)
+        if conschm not in ("643c", "543c"):
+            raise ValueError(f"conschm {conschm!r}: 643c (central) or 543c (compact MP)")
         self.L = lib()
         self.h = self.L.orc_create(ctypes.byref(self.cfg))
         self.im, self.jm, self.km = im, jm, km
@@ -219,6 +233,47 @@ class Oracle:
         out = np.zeros(dim + 1)
         self.L.orc_line_filter(self.h, d, _dptr(f), _dptr(out))
         return out
+
+    # -- compact MP path ----------------------------------------------------
+    def lshock(self):
+        """lshock(0:im,0:jm,0:km) as a bool array, None before the sensor ran."""
+        out = np.zeros((self.im + 1) * (self.jm + 1) * (self.km + 1), dtype=np.uint8)
+        ok = self.L.orc_lshock(self.h, out.ctypes.data_as(ctypes.c_void_p))
+        if not ok:
+            return None
+        return out.reshape((self.im + 1, self.jm + 1, self.km + 1), order="F").astype(bool)
+
+    def line_flux(self, d: int, wind: int, f: np.ndarray) -> np.ndarray:
+        """Compact upwind (wind=+1) / downwind (-1) interface flux fh(-1..dim)."""
+        dim = (self.im, self.jm, self.km)[d]
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        assert f.size == dim + 2 * HM + 1
+        out = np.zeros(dim + 2)
+        self.L.orc_line_flux(self.h, d, int(wind), _dptr(f), _dptr(out))
+        return out
+
+    def steger_warming(self, prim, q5, dxi3, jac):
+        prim = np.ascontiguousarray(prim, dtype=np.float64)
+        q5 = np.ascontiguousarray(q5, dtype=np.float64)
+        dxi3 = np.ascontiguousarray(dxi3, dtype=np.float64)
+        fp, fm = np.zeros(5), np.zeros(5)
+        self.L.orc_steger_warming(self.h, _dptr(prim), _dptr(q5), _dptr(dxi3), float(jac),
+                                  _dptr(fp), _dptr(fm))
+        return fp, fm
+
+
+def mp5(u5, ul, discont=True) -> float:
+    u5 = np.ascontiguousarray(u5, dtype=np.float64)
+    return lib().orc_mp5(_dptr(u5), float(ul), int(bool(discont)))
+
+
+def chardecomp(stl, str_):
+    """REV, LEV (5x5) between two node states {T,rho,p,E,u,v,w,dxi1..3}."""
+    a = np.ascontiguousarray(stl, dtype=np.float64)
+    b = np.ascontiguousarray(str_, dtype=np.float64)
+    R, L = np.zeros(25), np.zeros(25)
+    lib().orc_chardecomp(_dptr(a), _dptr(b), _dptr(R), _dptr(L))
+    return R.reshape(5, 5, order="F"), L.reshape(5, 5, order="F")
 
 
 def set_threads(n: int):
