@@ -27,6 +27,8 @@ ORDER_MAIN = 0
 ORDER_MINIAPP = 1
 FP64 = 0
 FP32_STORAGE = 1
+CONSCHM_CENTRAL = 0
+CONSCHM_MP = 1
 
 # Every symbol the header declares (checked by the CPU test suite).
 EXPORTS = [
@@ -42,7 +44,7 @@ EXPORTS = [
     "astr_gpu_cflcal",
 ]
 NOALLOC_STATS_MAX_BLOCKS = 65536
-KERNEL_CLASSES = ["filter", "halo", "convgrad", "visc", "pointwise", "stats"]
+KERNEL_CLASSES = ["filter", "halo", "convgrad", "visc", "pointwise", "stats", "mp"]
 
 
 class AstrDims(ctypes.Structure):
@@ -59,7 +61,9 @@ class AstrParams(ctypes.Structure):
                 ("reynolds", ctypes.c_double), ("prandtl", ctypes.c_double),
                 ("ref_tem", ctypes.c_double), ("suth_const", ctypes.c_double),
                 ("deltat", ctypes.c_double), ("channel", ctypes.c_int),
-                ("twall", ctypes.c_double)]
+                ("twall", ctypes.c_double), ("conschm", ctypes.c_int),
+                ("lchardecomp", ctypes.c_int), ("bfacmpld", ctypes.c_double),
+                ("shkcrt", ctypes.c_double)]
 
 
 class AstrStatus(ctypes.Structure):

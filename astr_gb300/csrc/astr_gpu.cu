@@ -18,6 +18,7 @@
 // Two precision forms share the kernels: plain FP64 (T = double), and FP32
 // storage (T = float) with the RK3 base and a master copy of q in FP64.
 #include "launch.cuh"
+#include "mp.cuh"
 #include "../../include/astr_gpu.h"
 
 #include <algorithm>
@@ -588,6 +589,29 @@ HostScheme make_filter(int ntype, int dim, double alfa, int CH, const HostFTab& 
   return s;
 }
 
+// compact_flux_initiate, src/flux.F90:32-112 (scheme 543): rows -2..dim+1
+// with explicit central end rows (periodic), or -1..dim with the
+// third-order boundary rows (physical boundaries at both ends).
+HostScheme make_flux(int ntype, int dim, int wind, double b, int CH, const HostFTab& t) {
+  HostScheme s;
+  const int i0 = ntype == 4 ? -1 : -2, imx = ntype == 4 ? dim : dim + 1;
+  s.first = i0; s.n = imx - i0 + 1; s.ntype = ntype; s.dim = dim;
+  const double lo = 0.5 - (1.0 / 6.0) * b, hi = (1.0 / 6.0) + (1.0 / 6.0) * b;
+  s.a.assign(s.n, wind > 0 ? lo : hi);
+  s.c.assign(s.n, wind > 0 ? hi : lo);
+  s.a[0] = s.c[0] = 0.0;
+  s.a[s.n - 1] = s.c[s.n - 1] = 0.0;
+  if (ntype == 4) {
+    s.a[0] = s.c[0] = 2.0;
+    s.a[1] = s.c[1] = 0.25;
+    s.a[s.n - 1] = s.c[s.n - 1] = 2.0;
+    s.a[s.n - 2] = s.c[s.n - 2] = 0.25;
+  }
+  s.finish(CH, t);
+  s.ulo = 1; s.uhi = 0;  // no uniform chunks (FP64 solves)
+  return s;
+}
+
 HostFTab make_ftab(double alfa, double bh, double bb) {
   HostFTab t;
   std::memset(&t, 0, sizeof(t));
@@ -717,6 +741,10 @@ struct astr_ctx {
   // first non-diagonal set arrives
   bool gen = false;
   void* xg = nullptr;
+  // compact MP convective scheme (conschm 543c): scratch and schemes
+  bool mp = false;
+  MPDev mpd{};
+  MPSchemes mps{};
   // one RK3 step captured as a CUDA graph (asynchronous stepping)
   cudaGraphExec_t step_graph = nullptr;
   long long graph_kernels = 0;  // kernel launches in one captured step
@@ -774,7 +802,7 @@ int after_launch(astr_ctx* c, const char* what) {
   return ASTR_OK;
 }
 
-enum { KC_FILTER = 0, KC_HALO, KC_CONVGRAD, KC_VISC, KC_POINT, KC_STATS, KC_N };
+enum { KC_FILTER = 0, KC_HALO, KC_CONVGRAD, KC_VISC, KC_POINT, KC_STATS, KC_MP, KC_N };
 
 void prof_begin(astr_ctx* c, int cls) {
   if (!c->prof) return;
@@ -1009,6 +1037,52 @@ int run_chan(astr_ctx* c, bool stage1) {
   return ASTR_OK;
 }
 
+// Compact MP convective residual (convrsdcmp, src/solver.F90:1271-1937),
+// with the Ducros sensor first when the characteristic decomposition is on
+// (rhscal, src/solver.F90:226-230) and rhscal's negation folded into the
+// last direction.  qrhs starts from zero (time_integration_rk,
+// src/mainloop.F90:408).
+int run_mpconv(astr_ctx* c) {
+  const Geo& g = c->g;
+  const DevT<double>& d = c->d64;
+  const MPDev& m = c->mpd;
+  CK(cudaMemsetAsync(d.qrhs, 0, 5 * (size_t)g.n0 * sizeof(double), c->st));
+  if (m.chard) {
+    for (int part = 0; part < 3; ++part) {
+      prof_begin(c, KC_MP);
+      const cudaError_t e = launch_mp_sensor(g, d, m, c->st, part);
+      prof_end(c);
+      RC(launch_result(c, e, "k_mp_sensor"));
+    }
+  }
+  const int nd = g.ndims;
+  for (int dir = 0; dir < nd; ++dir) {
+    cudaError_t e;
+    prof_begin(c, KC_MP);
+    e = dir == 0 ? launch_mp_split<0>(g, d, m, c->st)
+                 : (dir == 1 ? launch_mp_split<1>(g, d, m, c->st) : launch_mp_split<2>(g, d, m, c->st));
+    prof_end(c);
+    RC(launch_result(c, e, "k_mp_split"));
+    prof_begin(c, KC_MP);
+    e = dir == 0 ? launch_mp_cflux<0>(g, m, c->mps, c->st)
+                 : (dir == 1 ? launch_mp_cflux<1>(g, m, c->mps, c->st) : launch_mp_cflux<2>(g, m, c->mps, c->st));
+    prof_end(c);
+    RC(launch_result(c, e, "k_mp_cflux"));
+    prof_begin(c, KC_MP);
+    e = dir == 0 ? launch_mp_face<0>(g, d, m, c->st)
+                 : (dir == 1 ? launch_mp_face<1>(g, d, m, c->st) : launch_mp_face<2>(g, d, m, c->st));
+    prof_end(c);
+    RC(launch_result(c, e, "k_mp_face"));
+    const int last = dir == nd - 1;
+    prof_begin(c, KC_MP);
+    e = dir == 0 ? launch_mp_diff<0>(g, d, m, c->st, last)
+                 : (dir == 1 ? launch_mp_diff<1>(g, d, m, c->st, last) : launch_mp_diff<2>(g, d, m, c->st, last));
+    prof_end(c);
+    RC(launch_result(c, e, "k_mp_diff"));
+  }
+  return ASTR_OK;
+}
+
 template <typename T>
 int one_step(astr_ctx* c, double* stats) {
   const bool mini = c->pm.order == ASTR_ORDER_MINIAPP;
@@ -1028,7 +1102,9 @@ int one_step(astr_ctx* c, double* stats) {
       if (c->pm.lfilter) RC(run_filter<T>(c, false));
       if (c->channel) RC(run_noslip<T>(c));
       RC(run_qswap<T>(c));
-      RC(run_convgrad<T>(c, true, true, visc && !split_sig, st1 && stats && !c->gen, st1));
+      // compact MP: the sweeps give the gradients (and the RK3 base), the
+      // convective residual comes from the MP kernels
+      RC(run_convgrad<T>(c, !c->mp, true, visc && !split_sig, st1 && stats && !c->gen, st1));
       if (c->gen) {
         // general metrics: gradients contracted with the metrics, then the
         // statistics from them
@@ -1036,6 +1112,7 @@ int one_step(astr_ctx* c, double* stats) {
         if (st1 && stats) RC(stats_pointwise<T>(c));
       }
       if (split_sig) RC(sigma_pointwise<T>(c));
+      if (c->mp) RC(run_mpconv(c));
       if (c->channel) RC(run_chan<T>(c, st1));
       if (visc) RC(run_visc<T>(c, !split_rk, !split_rk));
       if (!visc || split_rk) RC(rk_pointwise<T>(c, 1));
@@ -1131,7 +1208,8 @@ int download_array(astr_ctx* c, double* dst, const void* src, size_t n) {
 
 template <typename T>
 int rhscal_t(astr_ctx* c) {
-  RC(run_convgrad<T>(c, true, false, false, false, false));
+  if (c->mp) RC(run_mpconv(c));
+  else RC(run_convgrad<T>(c, true, false, false, false, false));
   if (c->pm.diffterm) {
     prof_begin(c, KC_POINT);
     k_sigma<T><<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, dev<T>(c), c->ph);
@@ -1167,6 +1245,9 @@ size_t astr_gpu_footprint(const astr_dims* dims, const astr_params* params) {
   size_t b = w * (15 * nh + 26 * n0) + 8 * (nh + 5 * n0);
   if (f32) b += 8 * (3 * nh + 5 * n0);
   if (params && params->channel) b += 8 * nh;  // y coordinates
+  // compact MP: split fluxes 10, compact interface values 10, interface
+  // flux 5, sensor 1 (halo arrays, FP64) and the shock flags (bytes)
+  if (params && params->conschm == ASTR_CONSCHM_MP) b += 8 * 26 * nh + n0;
   return b;
 }
 
@@ -1187,6 +1268,11 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
   if (ndims == 2 && npdc[2] != 3) return fail(nullptr, ASTR_ERR_ARG, "2-D cases need npdck = 3");
   if (params->channel && (npdc[1] != 4 || params->order != ASTR_ORDER_MAIN || !(params->twall > 0.0)))
     return fail(nullptr, ASTR_ERR_ARG, "a channel needs npdcj = 4, the main ordering and twall > 0");
+  if (params->conschm != ASTR_CONSCHM_CENTRAL && params->conschm != ASTR_CONSCHM_MP)
+    return fail(nullptr, ASTR_ERR_ARG, "conschm must be ASTR_CONSCHM_CENTRAL or ASTR_CONSCHM_MP");
+  if (params->conschm == ASTR_CONSCHM_MP &&
+      (params->precision != ASTR_FP64 || params->order != ASTR_ORDER_MAIN))
+    return fail(nullptr, ASTR_ERR_UNSUPPORTED, "the compact MP scheme runs in FP64 and the main ordering");
 
   c = new astr_ctx();
   c->dm = *dims;
@@ -1359,6 +1445,65 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
   };
   fill(c->d64, (double*)nullptr);
   fill(c->d32, (float*)nullptr);
+  if (params->conschm == ASTR_CONSCHM_MP) {
+    // compact MP: scratch, and the upwind / downwind interface schemes of
+    // each direction (compact_flux_initiate, src/flux.F90:32-112)
+    MPDev& m = c->mpd;
+    m.fsw = (double*)alloc(10 * nh * 8);
+    m.fhc = (double*)alloc(10 * nh * 8);
+    m.fh = (double*)alloc(5 * nh * 8);
+    m.ssf = (double*)alloc(nh * 8);
+    m.lshock = (unsigned char*)alloc(n0);
+    m.chard = params->lchardecomp != 0;
+    for (int d = 0; d < 3; ++d) m.npdc[d] = npdc[d];
+    m.mach = params->mach;
+    m.bfac = params->bfacmpld;
+    m.shkcrt = params->shkcrt;
+    std::vector<HostScheme> fs;
+    for (int d = 0; d < 3; ++d) {
+      const int dim = std::max(dimv[d], 1);
+      const int rows = npdc[d] == 4 ? dim + 2 : dim + 4;
+      c->mps.CH[d] = d < ndims ? pick_ch(rows, NCH_B) : 3;
+      if (c->mps.CH[d] < 0) ok = false;
+      fs.push_back(make_flux(npdc[d], dim, +1, params->bfacmpld, std::max(c->mps.CH[d], 3), hft));
+      fs.push_back(make_flux(npdc[d], dim, -1, params->bfacmpld, std::max(c->mps.CH[d], 3), hft));
+    }
+    size_t ftot = 0;
+    for (auto& f : fs) ftot += 5 * (size_t)f.n;
+    double* fcoef = ok ? (double*)alloc(ftot * 8) : nullptr;
+    if (!ok) {
+      astr_gpu_destroy(c);
+      return fail(nullptr, ASTR_ERR_OOM, "device allocation failed (compact MP scratch or line length)");
+    }
+    std::vector<double> fb(ftot);
+    size_t fo = 0;
+    for (int idx = 0; idx < 6; ++idx) {
+      const HostScheme& f = fs[idx];
+      const size_t n = f.n;
+      const std::vector<double>* arr[5] = {&f.ac1, &f.ac3, &f.G, &f.H, &f.ac2};
+      for (int a = 0; a < 5; ++a) std::memcpy(&fb[fo + a * n], arr[a]->data(), n * 8);
+      DScheme<double> d8{};
+      d8.ac1 = fcoef + fo; d8.ac3 = fcoef + fo + n; d8.G = fcoef + fo + 2 * n;
+      d8.H = fcoef + fo + 3 * n; d8.ac2 = fcoef + fo + 4 * n;
+      d8.n = f.n; d8.first = f.first; d8.ntype = f.ntype; d8.dim = f.dim;
+      d8.ulo = 1; d8.uhi = 0;
+      if (idx % 2 == 0) c->mps.uw[idx / 2] = d8;
+      else c->mps.dw[idx / 2] = d8;
+      fo += 5 * n;
+    }
+    e = cudaMemcpy(fcoef, fb.data(), ftot * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(m.fsw, 0, 10 * nh * 8);
+    if (e == cudaSuccess) e = cudaMemset(m.fhc, 0, 10 * nh * 8);
+    if (e == cudaSuccess) e = cudaMemset(m.fh, 0, 5 * nh * 8);
+    if (e == cudaSuccess) e = cudaMemset(m.ssf, 0, nh * 8);
+    if (e == cudaSuccess) e = cudaMemset(m.lshock, 0, n0);
+    if (e != cudaSuccess) {
+      std::string msg = std::string("compact MP initialisation: ") + cudaGetErrorString(e);
+      astr_gpu_destroy(c);
+      return fail(nullptr, ASTR_ERR_CUDA, msg);
+    }
+    c->mp = true;
+  }
   *out = c;
   return ASTR_OK;
 }

@@ -45,8 +45,11 @@ class GpuSolver:
                  npdc=(3, 3, 3), lfilter=True, diffterm=True, alfa_filter=0.49,
                  beter_halo=1.11, beter_bound=0.98, mach=0.1, reynolds=1600.0, prandtl=0.72,
                  ref_tem=273.15, suth_const=None, deltat=1e-3, ia=None, ja=None, ka=None,
-                 channel=False, twall=1.0):
+                 channel=False, twall=1.0, conschm="643c", lchardecomp=True, bfacmpld=0.3,
+                 shkcrt=0.01):
         L = capi.load()
+        if conschm not in ("643c", "543c"):
+            raise ValueError(f"conschm {conschm!r}: 643c (central) or 543c (compact MP)")
         if suth_const is None:
             suth_const = 110.4 if order == capi.ORDER_MINIAPP else 110.3
         self.im, self.jm, self.km = im, jm, km
@@ -54,7 +57,9 @@ class GpuSolver:
                                   km if ka is None else ka, *npdc)
         self.params = capi.AstrParams(order, precision, int(lfilter), int(diffterm), alfa_filter,
                                       beter_halo, beter_bound, mach, reynolds, prandtl, ref_tem,
-                                      suth_const, deltat, int(channel), twall)
+                                      suth_const, deltat, int(channel), twall,
+                                      capi.CONSCHM_MP if conschm == "543c" else capi.CONSCHM_CENTRAL,
+                                      int(lchardecomp), bfacmpld, shkcrt)
         h = ctypes.c_void_p()
         rc = L.astr_gpu_create(ctypes.byref(self.dims), ctypes.byref(self.params), ctypes.byref(h))
         if rc != capi.ASTR_OK:

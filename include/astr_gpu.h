@@ -70,7 +70,25 @@ typedef struct {
                               controller (src/statistic.F90:641-657, 1494-1533);
                               needs npdcj = 4 and the grid (astr_gpu_set_grid) */
   double twall;            /* isothermal wall temperature (twall, bctype 41) */
+  int conschm;             /* ASTR_CONSCHM_*: convective scheme (conschm,
+                              src/commvar.F90; dispatch in rhscal,
+                              src/solver.F90:208-236)                        */
+  int lchardecomp;         /* compact MP: characteristic decomposition and
+                              the Ducros shock sensor (ducrossensor,
+                              src/commcal.F90:196-353)                      */
+  double bfacmpld;         /* compact MP: b factor of the compact upwind
+                              interface scheme (src/flux.F90:72-82; 0.3)    */
+  double shkcrt;           /* compact MP: shock-sensor threshold (0.01)     */
 } astr_params;
+
+/* Convective schemes.  CENTRAL is '643c' (convrsdcal6,
+ * src/solver.F90:2173-2341).  MP is '543c' (convrsdcmp,
+ * src/solver.F90:1271-1937): Steger-Warming flux splitting
+ * (src/riemann.F90:23-160), fifth-order compact upwind interface fluxes
+ * (src/flux.F90:32-256), MP5 limiting (src/flux.F90:363-496) and, with
+ * lchardecomp, Roe-averaged characteristic projection
+ * (src/solver.F90:1958-2162).  MP needs ASTR_FP64 and the main ordering. */
+enum { ASTR_CONSCHM_CENTRAL = 0, ASTR_CONSCHM_MP = 1 };
 
 typedef struct {
   double kenergy;          /* kenergycal, src/statistic.F90:938-992         */
