@@ -416,6 +416,24 @@ def channel_state(ia, ja, ka, y, mach=0.5, prandtl=0.72, gamma=1.4, seed=2026120
     return _pack_state(ia, ja, ka, rho, u, v, w, p, T, q5)
 
 
+def shock_box_state(n, mach=0.3, jump=0.5):
+    """Periodic 3-D shock box for the compact MP scheme: the TGV fields of
+    tgvini at the given Mach number with the pressure raised by the factor
+    1 + jump in z < pi, so that two plane pressure jumps steepen into shocks
+    and rarefactions inside the vortex field (T = p/rho gamma M^2)."""
+    L = 2.0 * PI
+    x, y, z = gridcube(n, n, n, L, L, L)
+    st = tgv_state(n, n, n, mach=mach, x=x, y=y, z=z)
+    c = refcal(mach, 1600.0)
+    sl = (slice(HM, HM + n + 1),) * 3
+    rho = st["rho"][sl]
+    u, v, w = (st["vel"][sl + (m,)] for m in range(3))
+    p = st["prs"][sl] * (1.0 + jump * (z.reshape(1, 1, -1) < PI))
+    T = p / rho * c["const2"]
+    q5 = rho * (T * c["const1"] + 0.5 * (u * u + v * v + w * w))
+    return _pack_state(n, n, n, rho, u, v, w, p, T, q5)
+
+
 def grid1d(ia, ja, xmin=-5.0, xmax=5.0):
     """grid1d (src/gridgeneration.F90:143-173) with a second direction:
     x = (xmax - xmin)/ia * i + xmin, y = j/ja, z = 0."""

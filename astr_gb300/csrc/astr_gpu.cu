@@ -1457,6 +1457,7 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
     m.chard = params->lchardecomp != 0;
     for (int d = 0; d < 3; ++d) m.npdc[d] = npdc[d];
     m.mach = params->mach;
+    m.rmach = 1.0 / params->mach;
     m.bfac = params->bfacmpld;
     m.shkcrt = params->shkcrt;
     std::vector<HostScheme> fs;

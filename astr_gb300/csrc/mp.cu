@@ -11,46 +11,76 @@ constexpr double N37D60 = 37.0 / 60.0, N2D15 = 2.0 / 15.0, N1D60 = 1.0 / 60.0;  
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
+// The limiter's comparisons, minima and maxima run on the integer pipe (the
+// FP64 pipe is the bound of these kernels): for doubles that are not NaN,
+// x > 0 is bits(x) > 0, x < 0 is bits(-x) > 0, magnitudes order as
+// bits & ~sign, and the order of two values is the order of their sortable
+// keys (negative values with the magnitude bits flipped).  Results are
+// bit-identical to the floating-point forms (a zero may come out as -0.0
+// where those give +0.0, which no later sum can tell apart).
+constexpr long long SIGN = (long long)0x8000000000000000ULL;
+__device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
+__device__ __forceinline__ double dval(long long b) { return __longlong_as_double(b); }
+__device__ __forceinline__ long long dkey(double x) {
+  const long long b = dbits(x);
+  return b >= 0 ? b : b ^ 0x7fffffffffffffffLL;
+}
+__device__ __forceinline__ double dmin(double a, double b) { return dkey(a) <= dkey(b) ? a : b; }
+__device__ __forceinline__ double dmax(double a, double b) { return dkey(a) >= dkey(b) ? a : b; }
+
 // minmod2, minmod4: src/commfunc.F90:699-738
 __device__ __forceinline__ double minmod2(double a, double b) {
-  if (a > 0.0 && b > 0.0) return fmin(fabs(a), fabs(b));
-  if (a < 0.0 && b < 0.0) return -fmin(fabs(a), fabs(b));
+  const long long ia = dbits(a), ib = dbits(b);
+  if (ia > 0 && ib > 0) return ia <= ib ? a : b;
+  const long long na = ia ^ SIGN, nb = ib ^ SIGN;
+  if (na > 0 && nb > 0) return na <= nb ? a : b;
   return 0.0;
 }
 __device__ __forceinline__ double minmod4(double a, double b, double c, double d) {
-  if (a > 0.0 && b > 0.0 && c > 0.0 && d > 0.0) return fmin(fmin(fabs(a), fabs(b)), fmin(fabs(c), fabs(d)));
-  if (a < 0.0 && b < 0.0 && c < 0.0 && d < 0.0) return -fmin(fmin(fabs(a), fabs(b)), fmin(fabs(c), fabs(d)));
+  const long long ia = dbits(a), ib = dbits(b), ic = dbits(c), id = dbits(d);
+  if (ia > 0 && ib > 0 && ic > 0 && id > 0) return dval(min(min(ia, ib), min(ic, id)));
+  const long long na = ia ^ SIGN, nb = ib ^ SIGN, nc = ic ^ SIGN, nd = id ^ SIGN;
+  if (na > 0 && nb > 0 && nc > 0 && nd > 0) return dval(min(min(na, nb), min(nc, nd)) ^ SIGN);
   return 0.0;
 }
 
 // MP5 with the compact value as the linear one (src/flux.F90:434-496;
-// Suresh & Huynh, JCP 136, 1997)
-__device__ __forceinline__ double mp5(const double (&u)[5], double ulinear, bool lskt) {
-  const double uMP = u[2] + minmod2(u[3] - u[2], 4.0 * (u[2] - u[1]));
-  const double var1 = (ulinear - u[2]) * (ulinear - uMP);
-  if (lskt && var1 >= 1.e-10) {
-    const double dm1 = u[0] - 2.0 * u[1] + u[2];
-    const double d0 = u[1] - 2.0 * u[2] + u[3];
-    const double d1 = u[2] - 2.0 * u[3] + u[4];
-    const double dhm1 = minmod4(4.0 * dm1 - d0, 4.0 * d0 - dm1, dm1, d0);
-    const double dh0 = minmod4(4.0 * d0 - d1, 4.0 * d1 - d0, d0, d1);
-    const double uUL = u[2] + 4.0 * (u[2] - u[1]);
-    const double uAV = 0.5 * (u[2] + u[3]);
-    const double uMD = uAV - 0.5 * dh0;
-    const double uLC = u[2] + 0.5 * (u[2] - u[1]) + 1.333333333333333 * dhm1;
-    const double uMIN = fmax(fmin(fmin(u[2], u[3]), uMD), fmin(fmin(u[2], uUL), uLC));
-    const double uMAX = fmin(fmax(fmax(u[2], u[3]), uMD), fmax(fmax(u[2], uUL), uLC));
-    return ulinear + minmod2(uMIN - ulinear, uMAX - ulinear);
-  }
-  return ulinear;
+// Suresh & Huynh, JCP 136, 1997), in two parts: the test whether the
+// linear value needs limiting uses the three centre points only; the
+// limiter itself needs all five.
+__device__ __forceinline__ bool mp5_needs(double u1, double u2, double u3, double ulinear) {
+  const double uMP = u2 + minmod2(u3 - u2, 4.0 * (u2 - u1));
+  const double var1 = (ulinear - u2) * (ulinear - uMP);
+  return dbits(var1) >= dbits(1.e-10);  // var1 >= 1e-10
+}
+__device__ __forceinline__ double mp5_limit(double u0, double u1, double u2, double u3, double u4,
+                                            double ulinear) {
+  const double dm1 = u0 - 2.0 * u1 + u2;
+  const double d0 = u1 - 2.0 * u2 + u3;
+  const double d1 = u2 - 2.0 * u3 + u4;
+  const double dhm1 = minmod4(4.0 * dm1 - d0, 4.0 * d0 - dm1, dm1, d0);
+  const double dh0 = minmod4(4.0 * d0 - d1, 4.0 * d1 - d0, d0, d1);
+  const double uUL = u2 + 4.0 * (u2 - u1);
+  const double uAV = 0.5 * (u2 + u3);
+  const double uMD = uAV - 0.5 * dh0;
+  const double uLC = u2 + 0.5 * (u2 - u1) + 1.333333333333333 * dhm1;
+  const double uMIN = dmax(dmin(dmin(u2, u3), uMD), dmin(dmin(u2, uUL), uLC));
+  const double uMAX = dmin(dmax(dmax(u2, u3), uMD), dmax(dmax(u2, uUL), uLC));
+  return ulinear + minmod2(uMIN - ulinear, uMAX - ulinear);
 }
 
-// mplimiter, src/flux.F90:363-379
-__device__ __forceinline__ double mplimiter(const double (&f)[5], double fl, bool shock, int inode,
-                                            int dim, int ntype) {
+// mplimiter (src/flux.F90:363-379) on a five-point stencil fetched by
+// point index (0..4): the two outer points are fetched only when MP5
+// limits.  shock false: MP5 returns the linear value.
+template <class Fetch>
+__device__ __forceinline__ double mplimiter(const Fetch& u, double fl, bool shock, int inode, int dim,
+                                            int ntype) {
   if ((ntype == 1 && (inode == 0 || inode == 1)) || (ntype == 2 && (inode == dim - 1 || inode == dim - 2)))
     return fl;
-  return mp5(f, fl, shock);
+  if (!shock) return fl;
+  const double u1 = u(1), u2 = u(2), u3 = u(3);
+  if (!mp5_needs(u1, u2, u3, fl)) return fl;
+  return mp5_limit(u(0), u1, u2, u3, u(4), fl);
 }
 
 __device__ __forceinline__ void metric_row(const Geo& g, const DevT<double>& d, int DIR, long long p,
@@ -191,16 +221,21 @@ __global__ void __launch_bounds__(256) k_mp_split(Geo g, DevT<double> d, MPDev m
   metric_row(g, d, DIR, p, x0, x1, x2);
   const double J = d.jac[p];
   double* F = m.fsw + p;
+  // The divisions of the reference that only scale by constants or by
+  // var0 are multiplications here (sos uses 1/M, csa = css |grad xi|, the
+  // energy term 1/(gamma-1)), and the sonic test compares uu with csa
+  // instead of uu/csa with 1: rounding-level differences.
   const double eps = 0.04;
   const double uu = x0 * u + x1 * v + x2 * w;
-  const double var0 = 1.0 / sqrt(x0 * x0 + x1 * x1 + x2 * x2);
+  const double sg = sqrt(x0 * x0 + x1 * x1 + x2 * x2);
+  const double var0 = 1.0 / sg;
   const double g0 = x0 * var0, g1 = x1 * var0, g2 = x2 * var0;
   const double gm2 = 0.5 / GAM;
-  const double css = sqrt(tmp) / m.mach;
-  const double csa = css / var0;
-  const double lmach = uu / csa;
-  if (lmach >= 1.0 || lmach <= -1.0) {
-    const int on = lmach >= 1.0 ? 0 : 5, off = lmach >= 1.0 ? 5 : 0;
+  const double css = sqrt(tmp) * m.rmach;
+  const double csa = css * sg;
+  const bool sup = uu >= csa, sdn = uu <= -csa;
+  if (sup || sdn) {
+    const int on = sup ? 0 : 5, off = sup ? 5 : 0;
     F[(on + 0) * nh] = J * q0 * uu;
     F[(on + 1) * nh] = J * (q1 * uu + x0 * prs);
     F[(on + 2) * nh] = J * (q2 * uu + x1 * prs);
@@ -231,7 +266,7 @@ __global__ void __launch_bounds__(256) k_mp_split(Geo g, DevT<double> d, MPDev m
     Fs[2 * nh] = jro * (var4 * v + var2 * css * g1 * gm2);
     Fs[3 * nh] = jro * (var4 * w + var2 * css * g2 * gm2);
     Fs[4 * nh] = J * (var1 * q4 + rho * (var2 * uu * var0 * css * gm2 -
-                                         var3 * (fhi + css * css) * gm2 / (GAM - 1.0)));
+                                         var3 * (fhi + css * css) * gm2 * (1.0 / (GAM - 1.0))));
   }
 }
 
@@ -345,16 +380,23 @@ __global__ void __launch_bounds__(128) k_mp_face(Geo g, DevT<double> d, MPDev m,
   if (!m.chard) {
 #pragma unroll 1
     for (int c = 0; c < 5; ++c) {
-      double up[5], dn[5];
-#pragma unroll
-      for (int n = 0; n < 5; ++n) {
-        up[n] = __ldg(FP + c * nh + hs * wp[n]);
-        dn[n] = __ldg(FM + c * nh + hs * wm[n]);
-      }
+      const double* a = FP + c * nh;
+      const double* z = FM + c * nh;
+      auto up = [&](int n) { return __ldg(a + hs * wp[n]); };
+      auto dn = [&](int n) { return __ldg(z + hs * wm[n]); };
       const double v1 = mplimiter(up, HC[c * nh], lsh, f, dim, npdc);
       const double v2 = mplimiter(dn, HC[(5 + c) * nh], lsh, f, dim, npdc);
       out[c * nh] = v1 + v2;
     }
+    return;
+  }
+  if (!lsh) {
+    // The sensor is off at both nodes: MP5 returns the linear value for
+    // every characteristic field, so the reference forms R L (fhcp + fhcm)
+    // with R L = I.  The projection and its inverse are skipped; the sum
+    // differs from the reference's by rounding (eps * cond(R)).
+#pragma unroll
+    for (int r = 0; r < 5; ++r) out[r * nh] = HC[r * nh] + HC[(5 + r) * nh];
     return;
   }
   // chardecomp, src/solver.F90:1958-2162, between nodes f and f+1
@@ -426,17 +468,14 @@ __global__ void __launch_bounds__(128) k_mp_face(Geo g, DevT<double> d, MPDev m,
         R[0] = 0.0; R[1] = 0.0; R[2] = g3; R[3] = -g2; R[4] = u2 * g3 - u3 * g2;
       }
     }
-    // projections of the stencils and the compact values onto field c
-    double up[5], dn[5];
-#pragma unroll
-    for (int n = 0; n < 5; ++n) {
-      const double* a = FP + hs * wp[n];
-      const double* z = FM + hs * wm[n];
-      up[n] = L[0] * __ldg(a) + L[1] * __ldg(a + nh) + L[2] * __ldg(a + 2 * nh) +
-              L[3] * __ldg(a + 3 * nh) + L[4] * __ldg(a + 4 * nh);
-      dn[n] = L[0] * __ldg(z) + L[1] * __ldg(z + nh) + L[2] * __ldg(z + 2 * nh) +
-              L[3] * __ldg(z + 3 * nh) + L[4] * __ldg(z + 4 * nh);
-    }
+    // projections onto field c of the compact values and, where the
+    // limiter may act, of the stencil points
+    auto proj = [&](const double* a) {
+      return L[0] * __ldg(a) + L[1] * __ldg(a + nh) + L[2] * __ldg(a + 2 * nh) +
+             L[3] * __ldg(a + 3 * nh) + L[4] * __ldg(a + 4 * nh);
+    };
+    auto up = [&](int n) { return proj(FP + hs * wp[n]); };
+    auto dn = [&](int n) { return proj(FM + hs * wm[n]); };
     const double hp = L[0] * HC[0] + L[1] * HC[nh] + L[2] * HC[2 * nh] + L[3] * HC[3 * nh] + L[4] * HC[4 * nh];
     const double hm = L[0] * HC[5 * nh] + L[1] * HC[6 * nh] + L[2] * HC[7 * nh] + L[3] * HC[8 * nh] +
                       L[4] * HC[9 * nh];

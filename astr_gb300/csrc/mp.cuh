@@ -28,7 +28,7 @@ struct MPDev {
   unsigned char* lshock;  // interior array
   int chard;              // lchardecomp: characteristic projection and sensor
   int npdc[3];
-  double mach, bfac, shkcrt;
+  double mach, rmach, bfac, shkcrt;  // rmach = 1/mach
 };
 
 struct MPSchemes {

@@ -693,6 +693,96 @@ def run_serve(args, rank, world, dist):
     return 0
 
 
+def run_mp(args, rank, world, dist):
+    """Compact MP convective scheme (conschm 543c: Steger-Warming split,
+    compact upwind interface fluxes, Roe characteristic projection, MP5
+    limiting, Ducros sensor; FP64) on the periodic 3-D shock box (TGV at
+    Mach 0.3 with a pressure jump, Re 1600, viscous, no filter, CFL 0.5),
+    beside the same case with the central scheme; the oracle on the host
+    cores on a bounded sample; the Sod tube against the exact Riemann
+    solution."""
+    from astr_gb300 import capi, cases
+    from astr_gb300.solver import GpuSolver
+    if rank != 0:
+        return 0
+    n, mach = args.mp_n, 0.3
+    L = 2.0 * np.pi
+    x, y, z = cases.gridcube(n, n, n, L, L, L)
+    (d11, d22, d33), J = cases.rect_metrics(x, y, z, diag_only=True)
+    st = cases.shock_box_state(n, mach=mach, jump=0.5)
+    dt = cases.cfl_deltat(st, (d11, d22, d33), mach, CFL)
+    pts = float(n) ** 3
+    forms = {}
+    for scheme in ("543c", "643c"):
+        g = GpuSolver(n, n, n, mach=mach, reynolds=1600.0, deltat=dt, lfilter=False,
+                      conschm=scheme)
+        g.set_metrics_diag(d11, d22, d33, J)
+        g.upload_state(st["q"], st["rho"], st["vel"], st["prs"], st["tmp"])
+        g.time_integration_rk(1)
+        g.timed_steps(args.warmup - 1)
+        clocks = ClockSampler(env_int("LOCAL_RANK", 0))
+        clocks.start()
+        l0 = g.launches
+        ms = g.timed_steps(args.steps)
+        launches = (g.launches - l0) // args.steps
+        clk = clocks.stop()
+        g.set_profiling(True)
+        g.timed_steps(1)
+        kt = {k: round(v[0], 3) for k, v in g.kernel_times().items() if v[1]}
+        g.set_profiling(False)
+        q = g.download_state()["q"]
+        g.close()
+        forms[scheme] = {"value": round(pts * 3 * args.steps / (ms / 1e3) / 1e6, 3),
+                         "ms_per_step": round(ms / args.steps, 3),
+                         "kernel_ms_one_step": kt, "launches_per_step": launches,
+                         "finite": bool(np.isfinite(q).all()), "clocks": clk}
+    # oracle (C++ restatement, all host cores) on a 64^3 sample of the case
+    from oracle import pyoracle as po
+    po.set_threads(os.cpu_count())
+    ns = 64
+    sts = cases.shock_box_state(ns, mach=mach, jump=0.5)
+    xs, ys, zs = cases.gridcube(ns, ns, ns, L, L, L)
+    ds, _ = cases.rect_metrics(xs, ys, zs, diag_only=True)
+    o = po.from_state(sts, (ns, ns, ns), lx=L, ly=L, lz=L, mach=mach, reynolds=1600.0,
+                      lfilter=False, conschm="543c",
+                      deltat=cases.cfl_deltat(sts, ds, mach, CFL))
+    o.rk3_steps(1)
+    t0 = time.perf_counter()
+    o.rk3_steps(2)
+    tc = time.perf_counter() - t0
+    cpu = ns ** 3 * 3 * 2 / tc / 1e6
+    # Sod tube, 400 points, t = 1.5, against the exact Riemann solution
+    im, jm, sdt = 400, 8, 0.004
+    ss = cases.shock_tube_state("sod", im, jm)
+    xg, yg, zg = cases.grid1d(im, jm)
+    dxi, Jg = cases.rect_metrics(xg, yg, zg, npdc=(4, 3, 3))
+    g = GpuSolver(im, jm, 0, npdc=(4, 3, 3), mach=3.0, deltat=sdt, lfilter=False,
+                  diffterm=False, conschm="543c")
+    g.set_metrics(dxi, Jg)
+    g.upload_state(ss["q"], ss["rho"], ss["vel"], ss["prs"], ss["tmp"])
+    g.time_integration_rk(int(round(1.5 / sdt)))
+    rho = g.download_state()["rho"][5:5 + im + 1, 5, 5]
+    g.close()
+    re_, _, _ = cases.riemann_exact((1.0, 0.0, 1.0), (0.125, 0.0, 0.1), xg, 1.5)
+    line = {
+        "case": "mp",
+        "workload": f"periodic shock box {n}^3: TGV at Mach {mach}, pressure x1.5 in z < pi, "
+                    f"Re 1600, viscous, no filter, CFL {CFL} (dt {dt:.4e}); conschm 543c "
+                    "(lchardecomp, bfacmpld 0.3, shkcrt 0.01) against 643c on the same case",
+        "unit": UNIT, "dtype": "f64", "forms": forms,
+        "mp_over_central_time": round(forms["543c"]["ms_per_step"] / forms["643c"]["ms_per_step"], 3),
+        "cpu_baseline": {"value": round(cpu, 3), "unit": UNIT, "cores": po.get_threads(),
+                         "kind": "port",
+                         "sample": f"oracle, the same case at {ns}^3, conschm 543c, 2 RK3 steps in "
+                                   f"{tc:.2f} s"},
+        "sod_400_t1.5": {"rho_l1_vs_exact": round(float(np.mean(np.abs(rho - re_))), 6)},
+        "note": "device time of the stepping loop (CUDA events), state resident in HBM; "
+                "kernel_ms_one_step from a separate profiled step",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def ctypes_peak():
     import ctypes
     from astr_gb300 import capi
@@ -711,7 +801,8 @@ def main():
     ap.add_argument("--n", type=int, default=512)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--form", default="both", choices=["both", "fp64", "fp32_storage"])
-    ap.add_argument("--case", default="tgv", choices=["tgv", "vortex2d", "channel", "serve"])
+    ap.add_argument("--case", default="tgv", choices=["tgv", "vortex2d", "channel", "serve", "mp"])
+    ap.add_argument("--mp-n", type=int, default=256)
     ap.add_argument("--serve-cases", type=int, default=100)
     ap.add_argument("--serve-rate", type=float, default=50.0)
     ap.add_argument("--serve-slots", type=int, default=32)
@@ -733,6 +824,8 @@ def main():
         return run_channel(args, rank, world, dist)
     if args.case == "serve":
         return run_serve(args, rank, world, dist)
+    if args.case == "mp":
+        return run_mp(args, rank, world, dist)
     if args.history:
         return run_history(args, rank, world, dist)
     return run_gpu(args, rank, world, dist)

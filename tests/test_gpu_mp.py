@@ -75,20 +75,11 @@ def test_mp_sod_matches_oracle(gpu_lib, chard):
 
 
 def _jump3d(n, mach=0.3, **kw):
-    """TGV fields at Mach 0.3 with the pressure raised by half in z < pi (two
-    plane discontinuities in the periodic box)."""
+    """The periodic shock box: TGV fields at Mach 0.3 with the pressure
+    raised by half in z < pi (two plane discontinuities)."""
     from oracle import pyoracle as po
     L = 2.0 * np.pi
-    x, y, z = cases.gridcube(n, n, n, L, L, L)
-    st = cases.tgv_state(n, n, n, mach=mach, x=x, y=y, z=z)
-    c = cases.refcal(mach, 1600.0)
-    sl = (slice(H, H + n + 1),) * 3
-    rho = st["rho"][sl]
-    u, v, w = (st["vel"][sl + (m,)] for m in range(3))
-    p = st["prs"][sl] * (1.0 + 0.5 * (z.reshape(1, 1, -1) < np.pi))
-    T = p / rho * c["const2"]
-    q5 = rho * (T * c["const1"] + 0.5 * (u * u + v * v + w * w))
-    st = cases._pack_state(n, n, n, rho, u, v, w, p, T, q5)
+    st = cases.shock_box_state(n, mach=mach, jump=0.5)
     o = po.from_state(st, (n, n, n), lx=L, ly=L, lz=L, mach=mach, conschm="543c", **kw)
     _zero_offdiag(o)
     return o
