@@ -41,7 +41,7 @@ EXPORTS = [
     "astr_gpu_set_profiling", "astr_gpu_kernel_times", "astr_gpu_measure_fp64_peak",
     "astr_gpu_stats_noalloc", "astr_gpu_set_grid", "astr_gpu_channel_state",
     "astr_gpu_boucon", "astr_gpu_step_async", "astr_gpu_poll", "astr_gpu_crashcheck",
-    "astr_gpu_cflcal",
+    "astr_gpu_cflcal", "astr_gpu_upload_q",
 ]
 NOALLOC_STATS_MAX_BLOCKS = 65536
 KERNEL_CLASSES = ["filter", "halo", "convgrad", "visc", "pointwise", "stats", "mp"]
@@ -97,6 +97,8 @@ def load(path: str = LIB_PATH):
     L.astr_gpu_destroy.restype = None
     L.astr_gpu_set_metrics.argtypes = [vp, dp, dp]
     L.astr_gpu_upload_state.argtypes = [vp, dp, dp, dp, dp, dp]
+    L.astr_gpu_upload_q.argtypes = [vp, dp]
+    L.astr_gpu_upload_q.restype = ip
     L.astr_gpu_download_state.argtypes = [vp, dp, dp, dp, dp, dp]
     L.astr_gpu_download_rhs.argtypes = [vp, dp, dp, dp]
     L.astr_gpu_rk3_step.argtypes = [vp, ip, dp, ctypes.POINTER(AstrStatus)]

@@ -1721,6 +1721,38 @@ int astr_gpu_upload_state(astr_ctx* c, const double* q, const double* rho, const
   return ASTR_OK;
 }
 
+int astr_gpu_upload_q(astr_ctx* c, const double* q) {
+  if (!c || !q) return fail(c, ASTR_ERR_ARG, "null argument");
+  const size_t nh = (size_t)c->g.nh, w = wsize(c);
+  char* dq = (char*)c->d64.q;
+  RC(xfer_begin(c));
+  for (int m = 0; m < 5; ++m) {
+    if (c->prec == ASTR_FP64) {
+      RC(upload_array(c, dq + m * nh * w, q + m * nh, nh));
+    } else {
+      double* buf = nullptr;
+      RC(xfer_in(c, q + m * nh, nh, &buf));
+      k_to_float<<<point_grid((long long)nh), 256, 0, c->st>>>(buf, (float*)(dq + m * nh * w),
+                                                                 (long long)nh);
+      RC(after_launch(c, "k_to_float"));
+      k_halo_to_interior<<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, buf, c->d32.qm + m * c->g.n0);
+      RC(after_launch(c, "k_halo_to_interior"));
+      RC(xfer_used(c, buf));
+    }
+  }
+  // primitives of the interior nodes from q (updatefvar); halo primitives are
+  // rebuilt by qswap at the start of each stage (periodic directions) or
+  // keep what the last full upload put there (physical ends)
+  if (c->prec == ASTR_FP64)
+    k_updatefvar<double><<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, c->d64, c->ph);
+  else
+    k_updatefvar<float><<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, c->d32, c->ph);
+  RC(after_launch(c, "k_updatefvar"));
+  RC(xfer_sync(c));
+  c->state_set = true;
+  return ASTR_OK;
+}
+
 int astr_gpu_download_state(astr_ctx* c, double* q, double* rho, double* vel, double* prs, double* tmp) {
   if (!c) return fail(c, ASTR_ERR_ARG, "null context");
   const size_t nh = (size_t)c->g.nh, w = wsize(c);

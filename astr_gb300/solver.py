@@ -126,6 +126,12 @@ class GpuSolver:
         self._c(self.L.astr_gpu_upload_state(self.h, capi.dptr(q), capi.dptr(rho), capi.dptr(vel),
                                              capi.dptr(prs), capi.dptr(tmp)))
 
+    def upload_q(self, q):
+        """Upload q alone; the interior primitives are recomputed on the
+        device (updatefvar)."""
+        q = _f(q, halo_shape(self.im, self.jm, self.km, 5))
+        self._c(self.L.astr_gpu_upload_q(self.h, capi.dptr(q)))
+
     def download_state(self):
         im, jm, km = self.im, self.jm, self.km
         out = {

@@ -152,6 +152,13 @@ int astr_gpu_boucon(astr_ctx* ctx);
  * completed time steps.  ASTR_ERR_STATE unless the context is a channel. */
 int astr_gpu_channel_state(astr_ctx* ctx, double* out5);
 
+/* Upload the conserved variables q(-hm:..,1:5) (halo layout) alone: the
+ * primitives of the interior nodes are recomputed from them on the device
+ * (updatefvar, src/fludyna.F90:191-242), the halo primitives are rebuilt by
+ * qswap at the start of each stage in periodic directions.  The state of a
+ * step is q; this is the per-step input when the host owns the state. */
+int astr_gpu_upload_q(astr_ctx* ctx, const double* q);
+
 /* Upload the conserved variables q(-hm:..,1:5) (halo layout) and the
  * primitive arrays rho, vel(..,1:3), prs, tmp (halo layout).  The
  * primitives are part of the solver state: interior primitives are the
