@@ -63,7 +63,8 @@ class AstrParams(ctypes.Structure):
                 ("deltat", ctypes.c_double), ("channel", ctypes.c_int),
                 ("twall", ctypes.c_double), ("conschm", ctypes.c_int),
                 ("lchardecomp", ctypes.c_int), ("bfacmpld", ctypes.c_double),
-                ("shkcrt", ctypes.c_double)]
+                ("shkcrt", ctypes.c_double), ("bctype", ctypes.c_int * 6),
+                ("twall_face", ctypes.c_double * 6)]
 
 
 class AstrStatus(ctypes.Structure):

@@ -148,43 +148,121 @@ __global__ void k_rkupdate(Geo g, DevT<T> d, Phys ph, int q2f) {
   if (q2f) q2fvar_store(g, d, ph, p);
 }
 
-// noslip isothermal wall at j = 0 and j = jm (src/bc.F90:6423-6611): u = 0,
-// T = T_w, p = (4 p(1) - p(2))/3, rho = p/T*const2, q = fvar2q with
-// pressure (src/fludyna.F90:312-376).  The FP32 form also sets the FP64
-// master at the wall nodes.
+// Boundary routines of boucon (src/bc.F90:327-409) on face n (0-based:
+// xmin, xmax, ymin, ymax, zmin, zmax), one thread per face node, in FP64
+// from the stored fields; nondimensional, no species.  Each branch restates
+// the face branch of its routine as the reference writes it, including
+// where the faces differ:
+//   41 noslip (6306-6712): u = 0, T = T_w, p extrapolated, rho = p/T*const2,
+//      q with pressure;
+//   42 noslip_adibatic (6728-7036, x and y faces): p and T extrapolated;
+//   50 zeroextrap (2356-2652): x faces extrapolate T, the others rho; q with
+//      temperature on ymax only;
+//   60 symmetry (2664-2996): x faces and zmax remove the velocity along the
+//      metric row's unit vector, y faces and zmin zero the normal component;
+//      q with temperature on the x faces, ymax and zmax.
+// extrapolate(v1, v2, 0) is (4 v1 - v2)/3 (extrapolate_2o,
+// src/commfunc.F90:277-285).
+__device__ __forceinline__ double bc_ex2(double v1, double v2) {
+  return (1.0 / 3.0) * (4.0 * v1 - v2 - 2.0 * 0.0);
+}
+
 template <typename T>
-__global__ void k_noslip(Geo g, DevT<T> d, Phys ph, double tw, double const6) {
+__global__ void k_face_bc(Geo g, DevT<T> d, Phys ph, int n, int type, double tw, double const1,
+                          double const6) {
+  const int dir = n / 2, side = n % 2;
+  const int na = (dir == 0 ? g.jm : g.im) + 1;
+  const int nb = (dir == 2 ? g.jm : g.km) + 1;
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long long ncol = (long long)g.I * (g.km + 1);
-  if (idx >= 2 * ncol) return;
-  const int side = idx >= ncol ? 1 : 0;
-  const long long col = idx - side * ncol;
-  const int i = (int)(col % g.I), k = (int)(col / g.I);
-  const int j = side ? g.jm : 0, j1 = side ? g.jm - 1 : 1, j2 = side ? g.jm - 2 : 2;
+  if (idx >= (long long)na * nb) return;
+  const int a = (int)(idx % na), b = (int)(idx / na);
+  const int dim = dir == 0 ? g.im : (dir == 1 ? g.jm : g.km);
+  auto node = [&](int l, int& i, int& j, int& k) {
+    const int x = side ? dim - l : l;
+    i = dir == 0 ? x : a;
+    j = dir == 0 ? a : (dir == 1 ? x : b);
+    k = dir == 2 ? x : b;
+  };
+  int i, j, k, i1, j1, k1, i2, j2, k2;
+  node(0, i, j, k);
+  node(1, i1, j1, k1);
+  node(2, i2, j2, k2);
   const long long nh = g.nh;
-  const long long p = hidx(g, i, j, k);
-  const double p1 = (double)d.pr[hidx(g, i, j1, k) + 4 * nh];
-  const double p2 = (double)d.pr[hidx(g, i, j2, k) + 4 * nh];
-  const double pe = (4.0 * p1 - p2) / 3.0;
-  const double ro = pe / tw * ph.const2;
-  const double e = pe * const6;
+  const long long p = hidx(g, i, j, k), p1 = hidx(g, i1, j1, k1), p2 = hidx(g, i2, j2, k2);
+  const double c2 = ph.const2, c6 = const6;
+  auto prim = [&](long long q, int m) { return (double)d.pr[q + m * nh]; };
+  double ro, u, v, w, pe, te;
+  bool tform = false;  // q with temperature (else with pressure)
+  if (type == 41) {
+    pe = (1.0 / 3.0) * (4.0 * prim(p1, 4) - prim(p2, 4));
+    u = v = w = 0.0;
+    te = tw;
+    ro = pe / te * c2;
+  } else if (type == 42) {
+    pe = (1.0 / 3.0) * (4.0 * prim(p1, 4) - prim(p2, 4));
+    te = (1.0 / 3.0) * (4.0 * prim(p1, 5) - prim(p2, 5));
+    u = v = w = 0.0;
+    ro = pe / te * c2;
+  } else {
+    u = bc_ex2(prim(p1, 1), prim(p2, 1));
+    v = bc_ex2(prim(p1, 2), prim(p2, 2));
+    w = bc_ex2(prim(p1, 3), prim(p2, 3));
+    pe = bc_ex2(prim(p1, 4), prim(p2, 4));
+    const bool rho_extrap = type == 50 ? dir != 0 : n == 5;
+    if (rho_extrap) {
+      ro = bc_ex2(prim(p1, 0), prim(p2, 0));
+      te = pe / ro * c2;
+    } else {
+      te = bc_ex2(prim(p1, 5), prim(p2, 5));
+      ro = pe / te * c2;
+    }
+    if (type == 50) {
+      tform = n == 3;
+    } else if (n <= 1 || n == 5) {
+      // unit vector along the metric row (gridgeom's bnorm, src/geom.F90:700-830)
+      double x0, x1, x2;
+      if (d.xg) {
+        x0 = (double)d.xg[(3 * dir + 0) * nh + p];
+        x1 = (double)d.xg[(3 * dir + 1) * nh + p];
+        x2 = (double)d.xg[(3 * dir + 2) * nh + p];
+      } else {
+        const double xv = (double)d.xd[dir * nh + p];
+        x0 = dir == 0 ? xv : 0.0;
+        x1 = dir == 1 ? xv : 0.0;
+        x2 = dir == 2 ? xv : 0.0;
+      }
+      const double var1 = sqrt(x0 * x0 + x1 * x1 + x2 * x2);
+      const double n0 = x0 / var1, n1 = x1 / var1, n2 = x2 / var1;
+      const double vne = u * n0 + v * n1 + w * n2;
+      u = u - vne * n0;
+      v = v - vne * n1;
+      w = w - vne * n2;
+      tform = true;
+    } else {
+      if (dir == 1) v = 0.0;
+      else w = 0.0;
+      tform = n == 3;
+    }
+  }
+  const double var1 = 0.5 * (u * u + v * v + w * w);
+  const double e = tform ? ro * (te * const1 + var1) : pe * c6 + ro * var1;
   d.pr[p] = (T)ro;
-  d.pr[p + nh] = T(0);
-  d.pr[p + 2 * nh] = T(0);
-  d.pr[p + 3 * nh] = T(0);
+  d.pr[p + nh] = (T)u;
+  d.pr[p + 2 * nh] = (T)v;
+  d.pr[p + 3 * nh] = (T)w;
   d.pr[p + 4 * nh] = (T)pe;
-  d.pr[p + 5 * nh] = (T)tw;
+  d.pr[p + 5 * nh] = (T)te;
   d.q[p] = (T)ro;
-  d.q[p + nh] = T(0);
-  d.q[p + 2 * nh] = T(0);
-  d.q[p + 3 * nh] = T(0);
+  d.q[p + nh] = (T)(ro * u);
+  d.q[p + 2 * nh] = (T)(ro * v);
+  d.q[p + 3 * nh] = (T)(ro * w);
   d.q[p + 4 * nh] = (T)e;
   if (d.qm) {
     const long long z = zidx(g, i, j, k), n0 = g.n0;
     d.qm[z] = ro;
-    d.qm[z + n0] = 0.0;
-    d.qm[z + 2 * n0] = 0.0;
-    d.qm[z + 3 * n0] = 0.0;
+    d.qm[z + n0] = ro * u;
+    d.qm[z + 2 * n0] = ro * v;
+    d.qm[z + 3 * n0] = ro * w;
     d.qm[z + 4 * n0] = e;
   }
 }
@@ -741,6 +819,10 @@ struct astr_ctx {
   // first non-diagonal set arrives
   bool gen = false;
   void* xg = nullptr;
+  // boundary routine and wall temperature of each face (boucon)
+  int bct[6] = {0, 0, 0, 0, 0, 0};
+  double btw[6] = {0, 0, 0, 0, 0, 0};
+  bool has_bc = false;
   // compact MP convective scheme (conschm 543c): scratch and schemes
   bool mp = false;
   MPDev mpd{};
@@ -1009,14 +1091,26 @@ int rk_pointwise(astr_ctx* c, int q2f) {
 
 constexpr int CHAN_THREADS = 256;
 
+// boucon (src/bc.F90:327-409): the faces' boundary routines in face order.
 template <typename T>
-int run_noslip(astr_ctx* c) {
-  const long long n = 2LL * c->g.I * (c->g.km + 1);
-  prof_begin(c, KC_HALO);
-  k_noslip<T><<<point_grid(n), 256, 0, c->st>>>(c->g, dev<T>(c), c->ph, c->pm.twall,
-                                                  1.0 / c->ph.rconst6);
-  prof_end(c);
-  return after_launch(c, "k_noslip");
+int run_boucon(astr_ctx* c) {
+  const Geo& g = c->g;
+  // refcal (src/solver.F90:102-128): const1 = 1/(gamma (gamma-1) M^2), const6 = 1/(gamma-1)
+  const double gamma = 1.4, mach = c->pm.mach;
+  const double const1 = 1.0 / (gamma * (gamma - 1.0) * (mach * mach));
+  const double const6 = 1.0 / (gamma - 1.0);
+  for (int n = 0; n < 2 * g.ndims; ++n) {
+    const int type = c->bct[n];
+    if (type != 41 && type != 42 && type != 50 && type != 60) continue;
+    const int dir = n / 2;
+    const long long cnt = (long long)((dir == 0 ? g.jm : g.im) + 1) * ((dir == 2 ? g.jm : g.km) + 1);
+    prof_begin(c, KC_HALO);
+    k_face_bc<T><<<point_grid(cnt), 256, 0, c->st>>>(g, dev<T>(c), c->ph, n, type, c->btw[n], const1,
+                                                     const6);
+    prof_end(c);
+    RC(after_launch(c, "k_face_bc"));
+  }
+  return ASTR_OK;
 }
 
 // Channel bulk sums and controller for one stage; statcal at stage 1 from
@@ -1100,7 +1194,7 @@ int one_step(astr_ctx* c, double* stats) {
       const bool split_sig = visc && ((c->split_last & 1) || c->gen);
       const bool split_rk = visc && (c->split_last & 2);
       if (c->pm.lfilter) RC(run_filter<T>(c, false));
-      if (c->channel) RC(run_noslip<T>(c));
+      if (c->has_bc) RC(run_boucon<T>(c));
       RC(run_qswap<T>(c));
       // compact MP: the sweeps give the gradients (and the RK3 base), the
       // convective residual comes from the MP kernels
@@ -1268,6 +1362,20 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
   if (ndims == 2 && npdc[2] != 3) return fail(nullptr, ASTR_ERR_ARG, "2-D cases need npdck = 3");
   if (params->channel && (npdc[1] != 4 || params->order != ASTR_ORDER_MAIN || !(params->twall > 0.0)))
     return fail(nullptr, ASTR_ERR_ARG, "a channel needs npdcj = 4, the main ordering and twall > 0");
+  int bct[6];
+  for (int n = 0; n < 6; ++n) {
+    bct[n] = params->bctype[n];
+    if (params->channel && (n == 2 || n == 3) && (bct[n] == 0 || bct[n] == 1)) bct[n] = 41;
+    if (bct[n] == 0 || bct[n] == 1) continue;
+    if (bct[n] != 41 && bct[n] != 42 && bct[n] != 50 && bct[n] != 60)
+      return fail(nullptr, ASTR_ERR_UNSUPPORTED, "bctype: 41, 42, 50 and 60 are built (0/1: none)");
+    if (bct[n] == 42 && n >= 4)
+      return fail(nullptr, ASTR_ERR_UNSUPPORTED, "bctype 42 exists for the x and y faces only");
+    if (n / 2 >= ndims || npdc[n / 2] != 4)
+      return fail(nullptr, ASTR_ERR_ARG, "a boundary routine needs npdc = 4 in its direction");
+    const double tw = params->twall_face[n] != 0.0 ? params->twall_face[n] : params->twall;
+    if (bct[n] == 41 && !(tw > 0.0)) return fail(nullptr, ASTR_ERR_ARG, "bctype 41 needs a wall temperature > 0");
+  }
   if (params->conschm != ASTR_CONSCHM_CENTRAL && params->conschm != ASTR_CONSCHM_MP)
     return fail(nullptr, ASTR_ERR_ARG, "conschm must be ASTR_CONSCHM_CENTRAL or ASTR_CONSCHM_MP");
   if (params->conschm == ASTR_CONSCHM_MP &&
@@ -1369,6 +1477,11 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
   int* flag = (int*)alloc(64);
   c->stats_dev = (double*)alloc(64);
   c->channel = params->channel != 0;
+  for (int n = 0; n < 6; ++n) {
+    c->bct[n] = bct[n];
+    c->btw[n] = params->twall_face[n] != 0.0 ? params->twall_face[n] : params->twall;
+    if (bct[n] >= 41) c->has_bc = true;
+  }
   if (const char* e = std::getenv("ASTR_SPLIT_LAST")) c->split_last = std::atoi(e) & 3;
   if (c->channel) {
     const long long ncol = (long long)g.im * (ndims == 3 ? g.km : 1);
@@ -1671,8 +1784,8 @@ int astr_gpu_cflcal(astr_ctx* c, double deltat, double* cfl, double* delta3) {
 
 int astr_gpu_boucon(astr_ctx* c) {
   if (!c) return fail(c, ASTR_ERR_ARG, "null context");
-  if (!c->channel) return ASTR_OK;
-  return c->prec == ASTR_FP64 ? run_noslip<double>(c) : run_noslip<float>(c);
+  if (!c->has_bc) return ASTR_OK;
+  return c->prec == ASTR_FP64 ? run_boucon<double>(c) : run_boucon<float>(c);
 }
 
 int astr_gpu_set_metrics_diag(astr_ctx* c, const double* x11, const double* x22, const double* x33,

@@ -79,6 +79,16 @@ typedef struct {
   double bfacmpld;         /* compact MP: b factor of the compact upwind
                               interface scheme (src/flux.F90:72-82; 0.3)    */
   double shkcrt;           /* compact MP: shock-sensor threshold (0.01)     */
+  int bctype[6];           /* boundary routine of each face (xmin, xmax, ymin,
+                              ymax, zmin, zmax), bctype of boucon
+                              (src/bc.F90:327-409): 41 isothermal no-slip
+                              (6306-6712), 42 adiabatic no-slip (6728-7036,
+                              x and y faces), 50 zero-gradient extrapolation
+                              (2356-2652), 60 symmetry (2664-2996); 0 or 1:
+                              none.  A face with a routine needs npdc = 4 in
+                              its direction.  A channel has 41 on the y
+                              faces unless set otherwise.                    */
+  double twall_face[6];    /* wall temperature of each 41 face (0: twall)   */
 } astr_params;
 
 /* Convective schemes.  CENTRAL is '643c' (convrsdcal6,

@@ -1267,28 +1267,151 @@ void orc_qswap(orc_ctx* c) {
   }
 }
 
-// boucon (src/bc.F90:327-409): for the channel, noslip isothermal walls
-// at j = 0 and j = jm (bctype 41; noslip, src/bc.F90:6423-6611): u = 0,
-// T = T_w, p extrapolated (4 p(1) - p(2))/3, rho = p/T*const2 (thermal,
-// src/fludyna.F90:45-110), q = fvar2q with pressure (312-376).
+// Boundary routines of boucon (src/bc.F90:327-409), single rank, no
+// species, nondimensional.  Face n (0-based: xmin, xmax, ymin, ymax, zmin,
+// zmax), applied in face order (faces share their edge nodes; the later
+// face's values stay).  Each restates the face branch of its routine as the
+// reference writes it, including where the faces differ.
+namespace {
+
+// extrapolate(v1, v2, dv=0): extrapolate_2o, src/commfunc.F90:277-285
+inline double ex2(double v1, double v2) { return NUM1D3 * (4.0 * v1 - v2 - 2.0 * 0.0); }
+
+// fvar2q_sca with temperature (src/fludyna.F90:312-370)
+inline void fvar2q_tmp_node(orc_ctx& c, long p) {
+  const long nh = c.nh;
+  double ro = c.rho[p], u = c.vel[p], v = c.vel[p + nh], w = c.vel[p + 2 * nh];
+  c.q[p] = ro;
+  c.q[p + nh] = ro * u;
+  c.q[p + 2 * nh] = ro * v;
+  c.q[p + 3 * nh] = ro * w;
+  double var1 = 0.5 * (u * u + v * v + w * w);
+  c.q[p + 4 * nh] = ro * (c.tmp[p] * c.const1 + var1);
+}
+
+int face_bctype(const orc_ctx& c, int n) {
+  int t = c.cfg.bctype[n];
+  if (c.cfg.channel && (n == 2 || n == 3) && (t == 0 || t == 1)) t = 41;
+  return t;
+}
+
+double face_twall(const orc_ctx& c, int n) {
+  return c.cfg.twall6[n] != 0.0 ? c.cfg.twall6[n] : c.cfg.twall;
+}
+
+// unit vector along the metric row d at node p (gridgeom's bnorm,
+// src/geom.F90:700-830; its sign does not enter the symmetry condition)
+inline void bnorm(const orc_ctx& c, int d, long p, double* nv) {
+  const double* X = c.dxi.data() + p;
+  const long nh = c.nh;
+  double a = X[(d + 0) * nh], b = X[(d + 3) * nh], e = X[(d + 6) * nh];
+  double var1 = std::sqrt(a * a + b * b + e * e);
+  nv[0] = a / var1; nv[1] = b / var1; nv[2] = e / var1;
+}
+
+void face_node(orc_ctx& c, int n, int type, double tw, int i, int j, int k) {
+  const int d = n / 2, side = n % 2;
+  const int dim = c.dimof(d);
+  const long nh = c.nh;
+  auto at = [&](int l) {
+    int ii = i, jj = j, kk = k;
+    const int node = side ? dim - l : l;
+    if (d == 0) ii = node; else if (d == 1) jj = node; else kk = node;
+    return c.h(ii, jj, kk);
+  };
+  const long p = at(0), p1 = at(1), p2 = at(2);
+  double* R = c.rho.data(); double* P = c.prs.data(); double* T = c.tmp.data();
+  double* V = c.vel.data();
+  if (type == 41) {  // noslip, src/bc.F90:6306-6712 (all faces)
+    const double pe = NUM1D3 * (4.0 * P[p1] - P[p2]);
+    V[p] = 0.0; V[p + nh] = 0.0; V[p + 2 * nh] = 0.0;
+    P[p] = pe;
+    T[p] = tw;
+    R[p] = P[p] / T[p] * c.const2;
+    fvar2q_prs_node(c, p);
+  } else if (type == 42) {  // noslip_adibatic, src/bc.F90:6728-7036 (x, y faces)
+    const double pe = NUM1D3 * (4.0 * P[p1] - P[p2]);
+    const double te = NUM1D3 * (4.0 * T[p1] - T[p2]);
+    V[p] = 0.0; V[p + nh] = 0.0; V[p + 2 * nh] = 0.0;
+    P[p] = pe;
+    T[p] = te;
+    R[p] = P[p] / T[p] * c.const2;
+    fvar2q_prs_node(c, p);
+  } else if (type == 50) {  // zeroextrap, src/bc.F90:2356-2652
+    const double ue = ex2(V[p1], V[p2]), ve = ex2(V[p1 + nh], V[p2 + nh]);
+    const double we = ex2(V[p1 + 2 * nh], V[p2 + 2 * nh]);
+    const double pe = ex2(P[p1], P[p2]);
+    if (d == 0) {
+      const double te = ex2(T[p1], T[p2]);
+      P[p] = pe;
+      T[p] = te;
+      V[p] = ue; V[p + nh] = ve; V[p + 2 * nh] = we;
+      R[p] = P[p] / T[p] * c.const2;
+      fvar2q_prs_node(c, p);
+    } else {
+      const double roe = ex2(R[p1], R[p2]);
+      P[p] = pe;
+      R[p] = roe;
+      V[p] = ue; V[p + nh] = ve; V[p + 2 * nh] = we;
+      T[p] = P[p] / R[p] * c.const2;
+      if (n == 3) fvar2q_tmp_node(c, p);
+      else fvar2q_prs_node(c, p);
+    }
+  } else if (type == 60) {  // symmetry, src/bc.F90:2664-2996
+    const double ue = ex2(V[p1], V[p2]), ve = ex2(V[p1 + nh], V[p2 + nh]);
+    const double we = ex2(V[p1 + 2 * nh], V[p2 + 2 * nh]);
+    const double pe = ex2(P[p1], P[p2]);
+    if (n <= 1) {  // x faces: tangential projection, temperature form
+      const double te = ex2(T[p1], T[p2]);
+      double nv[3];
+      bnorm(c, 0, p, nv);
+      double vec[3] = {ue, ve, we};
+      const double vne = vec[0] * nv[0] + vec[1] * nv[1] + vec[2] * nv[2];
+      for (int m = 0; m < 3; ++m) vec[m] = vec[m] - vne * nv[m];
+      P[p] = pe;
+      T[p] = te;
+      V[p] = vec[0]; V[p + nh] = vec[1]; V[p + 2 * nh] = vec[2];
+      R[p] = P[p] / T[p] * c.const2;
+      fvar2q_tmp_node(c, p);
+    } else if (n <= 4) {  // y faces and zmin: the normal component set to 0
+      const double te = ex2(T[p1], T[p2]);
+      V[p] = ue; V[p + nh] = ve; V[p + 2 * nh] = we;
+      V[p + (d == 1 ? 1 : 2) * nh] = 0.0;
+      P[p] = pe;
+      T[p] = te;
+      R[p] = P[p] / T[p] * c.const2;
+      if (n == 3) fvar2q_tmp_node(c, p);
+      else fvar2q_prs_node(c, p);
+    } else {  // zmax: density extrapolated, tangential projection
+      const double roe = ex2(R[p1], R[p2]);
+      P[p] = pe;
+      R[p] = roe;
+      double nv[3];
+      bnorm(c, 2, p, nv);
+      double vec[3] = {ue, ve, we};
+      const double vne = vec[0] * nv[0] + vec[1] * nv[1] + vec[2] * nv[2];
+      for (int m = 0; m < 3; ++m) vec[m] = vec[m] - vne * nv[m];
+      V[p] = vec[0]; V[p + nh] = vec[1]; V[p + 2 * nh] = vec[2];
+      T[p] = P[p] / R[p] * c.const2;
+      fvar2q_tmp_node(c, p);
+    }
+  }
+}
+
+}  // namespace
+
 void orc_boucon(orc_ctx* c) {
-  if (!c->cfg.channel || c->cfg.npdcj != 4) return;
-  const long nh = c->nh;
-  const double tw = c->cfg.twall;
-  for (int side = 0; side < 2; ++side) {
-    const int j = side == 0 ? 0 : c->jm;
-    const int j1 = side == 0 ? 1 : c->jm - 1, j2 = side == 0 ? 2 : c->jm - 2;
-    for (int k = 0; k <= c->km; ++k)
-      for (int i = 0; i <= c->im; ++i) {
-        const long p = c->h(i, j, k);
-        const double pe = NUM1D3 * (4.0 * c->prs[c->h(i, j1, k)] - c->prs[c->h(i, j2, k)]);
-        c->vel[p] = 0.0;
-        c->vel[p + nh] = 0.0;
-        c->vel[p + 2 * nh] = 0.0;
-        c->prs[p] = pe;
-        c->tmp[p] = tw;
-        c->rho[p] = c->prs[p] / c->tmp[p] * c->const2;
-        fvar2q_prs_node(*c, p);
+  for (int n = 0; n < 2 * c->ndims; ++n) {
+    const int type = face_bctype(*c, n);
+    if (type != 41 && type != 42 && type != 50 && type != 60) continue;
+    const int d = n / 2;
+    if (c->npdc(d) != 4) continue;
+    const double tw = face_twall(*c, n);
+    const int a1 = d == 0 ? c->jm : c->im, b1 = d == 2 ? c->jm : c->km;
+    for (int b = 0; b <= b1; ++b)
+      for (int a = 0; a <= a1; ++a) {
+        const int i = d == 0 ? 0 : a, j = d == 0 ? a : (d == 1 ? 0 : b), k = d == 2 ? 0 : b;
+        face_node(*c, n, type, tw, i, j, k);
       }
   }
 }

@@ -54,6 +54,12 @@ typedef struct {
   int lchardecomp;         /* characteristic projection + Ducros sensor */
   double bfacmpld;         /* b factor of the compact upwind scheme */
   double shkcrt;           /* shock-sensor threshold */
+  /* boundary routine of each face (xmin, xmax, ymin, ymax, zmin, zmax),
+   * bctype of src/bc.F90:327-409: 41 isothermal no-slip, 42 adiabatic
+   * no-slip, 50 zero-gradient extrapolation, 60 symmetry; 0 or 1 none.
+   * A channel (channel = 1) with 0 on the y faces has 41 there. */
+  int bctype[6];
+  double twall6[6];        /* wall temperature of each 41 face (0: twall) */
 } orc_config;
 
 orc_ctx* orc_create(const orc_config* cfg);
@@ -81,7 +87,7 @@ void orc_updateq(orc_ctx* c);       /* q from primitives at 0:im (fvar2q with T)
 /* Hot-path restatements (each acts on the context's arrays). */
 void orc_filterq(orc_ctx* c);
 void orc_qswap(orc_ctx* c);
-void orc_boucon(orc_ctx* c);       /* channel: noslip isothermal j-walls; else no-op */
+void orc_boucon(orc_ctx* c);       /* the faces' boundary routines, in face order */
 /* Channel controller state: force(1), mass flux, its target, wall friction,
  * completed steps (5 doubles). */
 void orc_chan_state(orc_ctx* c, double* out5);

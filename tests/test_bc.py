@@ -1,0 +1,94 @@
+"""Boundary routines of boucon (src/bc.F90:327-409) in the oracle, on CPU:
+the face values each routine sets (41 isothermal no-slip, 42 adiabatic
+no-slip, 50 zero-gradient extrapolation, 60 symmetry), and a closed box
+stepping stably with walls on every face."""
+import numpy as np
+import pytest
+
+from astr_gb300 import cases
+
+H = 5
+MACH = 0.3
+
+
+def box_state(dims, lengths=(2.0 * np.pi, 2.0 * np.pi, 2.0 * np.pi), mach=MACH):
+    """TGV fields at Mach 0.3 on a box whose nodes include both ends of every
+    direction (non-periodic layout), shifted by a quarter period so that the
+    velocity does not vanish on the faces."""
+    im, jm, km = dims
+    x, y, z = cases.gridcube(im, jm, km, *lengths)
+    X = x.reshape(-1, 1, 1) + 0.7
+    Y = y.reshape(1, -1, 1) + 0.4
+    Z = z.reshape(1, 1, -1) + 0.3
+    c = cases.refcal(mach, 1600.0)
+    shape = (im + 1, jm + 1, km + 1)
+    rho = (1.0 + 0.1 * np.sin(X) * np.cos(Y)) * np.ones(shape)
+    u = np.sin(X) * np.cos(Y) * np.cos(Z) * np.ones(shape)
+    v = -np.cos(X) * np.sin(Y) * np.cos(Z) * np.ones(shape)
+    w = (0.2 * np.sin(Z) * np.cos(X) if km > 0 else 0.0) * np.ones(shape)
+    p = c["pinf"] + 1.0 / 16.0 * (np.cos(2 * X) + np.cos(2 * Y)) * (np.cos(2 * Z) + 2.0)
+    T = p / rho * c["const2"]
+    q5 = rho * (T * c["const1"] + 0.5 * (u * u + v * v + w * w))
+    return cases._pack_state(im, jm, km, rho, u, v, w, p, T, q5), (x, y, z)
+
+
+def bc_oracle(dims, npdc, bctype, twall6=(0.0,) * 6, **kw):
+    from oracle import pyoracle as po
+    st, grid = box_state(dims)
+    kw.setdefault("mach", MACH)
+    kw.setdefault("reynolds", 400.0)
+    return po.from_state(st, dims, grid=grid, npdc=npdc, bctype=bctype, twall6=twall6, **kw)
+
+
+def _face(a, n, l=0):
+    """Face n at distance l from it, without its edges (edge nodes belong to
+    two faces; the later face in boucon's order sets them)."""
+    d, side = n // 2, n % 2
+    dim = a.shape[d] - 2 * H - 1
+    idx = [slice(H + 1, H + a.shape[m] - 2 * H - 1) for m in range(3)]
+    idx[d] = H + (dim - l if side else l)
+    return a[tuple(idx)]
+
+
+def test_face_values():
+    dims = (24, 20, 16)
+    o = bc_oracle(dims, (4, 4, 4), (41, 42, 60, 50, 60, 41), twall6=(1.3, 0, 0, 0, 0, 0.9),
+                  twall=1.0)
+    before = {k: o.field(k).copy() for k in ("vel", "prs", "tmp", "rho")}
+    o.call("boucon")
+    vel, prs, tmp, rho, q = (o.field(k) for k in ("vel", "prs", "tmp", "rho", "q"))
+    ex = lambda a, n: (4.0 * _face(a, n, 1) - _face(a, n, 2)) / 3.0
+    # 41 on xmin (T_w 1.3) and zmax (0.9): u = 0, T = T_w, p extrapolated
+    for n, tw in ((0, 1.3), (5, 0.9)):
+        assert np.all(_face(vel, n) == 0.0) and np.all(_face(tmp, n) == tw)
+        np.testing.assert_allclose(_face(prs, n), ex(before["prs"], n), rtol=1e-14)
+    # 42 on xmax: p and T extrapolated, u = 0
+    assert np.all(_face(vel, 1) == 0.0)
+    np.testing.assert_allclose(_face(tmp, 1), ex(before["tmp"], 1), rtol=1e-14)
+    # 60 on ymin: v = 0, u and w extrapolated; 60 on zmin: w = 0
+    assert np.all(_face(vel[..., 1], 2) == 0.0)
+    assert np.all(_face(vel[..., 2], 4) == 0.0)
+    # 50 on ymax: every primitive extrapolated (T from p and the extrapolated rho)
+    np.testing.assert_allclose(_face(vel, 3), ex(before["vel"], 3), rtol=1e-13, atol=1e-14)
+    np.testing.assert_allclose(_face(rho, 3), ex(before["rho"], 3), rtol=1e-14)
+    # q consistent with the primitives on every face
+    for n in range(6):
+        np.testing.assert_allclose(_face(q[..., 1], n), _face(rho, n) * _face(vel[..., 0], n), rtol=1e-14,
+                                   atol=1e-15)
+        e = _face(prs, n) * 2.5 + 0.5 * _face(rho, n) * (_face(vel, n) ** 2).sum(axis=-1)
+        np.testing.assert_allclose(_face(q[..., 4], n), e, rtol=1e-12)
+
+
+def test_closed_box_steps():
+    """A 2-D box with walls on all four faces (isothermal, adiabatic and a
+    symmetry plane) and the viscous terms steps stably."""
+    o = bc_oracle((32, 24, 0), (4, 4, 3), (41, 42, 41, 60, 0, 0), twall=1.0, deltat=2e-3,
+                  lfilter=True)
+    o.rk3_steps(10)
+    q = o.field("q")
+    assert np.isfinite(q).all()
+    # boucon runs at the start of each stage: apply it to see the faces
+    o.call("boucon")
+    vel = o.field("vel")
+    assert np.all(_face(vel, 0) == 0.0) and np.all(_face(vel, 1) == 0.0)
+    assert np.all(_face(vel[..., 1], 3) == 0.0)

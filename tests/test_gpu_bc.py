@@ -1,0 +1,108 @@
+"""Boundary routines of boucon on the GPU against the oracle (FP64, 1e-12):
+a 3-D box with a different routine on each face (isothermal and adiabatic
+no-slip, symmetry, zero-gradient extrapolation), the viscous terms and the
+filter; a skewed curvilinear box where the symmetry faces project on the
+metric normal; and the FP32-storage form against FP64."""
+import numpy as np
+import pytest
+
+from astr_gb300 import capi
+from test_bc import H, MACH, bc_oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _gpu_from(o, precision=capi.FP64):
+    from astr_gb300.solver import GpuSolver
+    c = o.cfg
+    g = GpuSolver(o.im, o.jm, o.km, precision=precision, npdc=(c.npdci, c.npdcj, c.npdck),
+                  mach=c.mach, reynolds=c.reynolds, deltat=c.deltat, lfilter=bool(c.lfilter),
+                  diffterm=bool(c.diffterm), twall=c.twall, bctype=tuple(c.bctype),
+                  twall_face=tuple(c.twall6))
+    g.set_metrics(o.field("dxi").copy(order="F"), o.field("jacob").copy(order="F"))
+    g.upload_state(o.field("q"), o.field("rho"), o.field("vel"), o.field("prs"), o.field("tmp"))
+    return g
+
+
+def _cmp(o, s, tol=1e-12):
+    sl = (slice(H, H + o.im + 1), slice(H, H + o.jm + 1), slice(H, H + o.km + 1))
+    qo = o.field("q")[sl]
+    mom = np.abs(qo[..., 1:4]).max()
+    errs = {}
+    for m in range(5):
+        ref = qo[..., m]
+        scale = mom if 1 <= m <= 3 else np.abs(ref).max()
+        errs[f"q{m + 1}"] = float(np.abs(s["q"][sl + (m,)] - ref).max() / scale)
+    for name in ("prs", "tmp", "rho"):
+        ref = o.field(name)[sl]
+        errs[name] = float(np.abs(s[name][sl] - ref).max() / np.abs(ref).max())
+    print(" ".join(f"{k} {v:.1e}" for k, v in errs.items()))
+    assert max(errs.values()) <= tol, errs
+
+
+def _mixed_box():
+    return bc_oracle((24, 20, 16), (4, 4, 4), (41, 42, 60, 50, 60, 41),
+                     twall6=(1.3, 0, 0, 0, 0, 0.9), twall=1.0, deltat=2e-3, lfilter=True)
+
+
+def test_mixed_faces_match_oracle(gpu_lib):
+    o = _mixed_box()
+    g = _gpu_from(o)
+    o.rk3_steps(4)
+    g.time_integration_rk(4)
+    s = g.download_state()
+    g.close()
+    _cmp(o, s)
+
+
+def test_skewed_symmetry_faces_match_oracle(gpu_lib):
+    from oracle import pyoracle as po
+    from test_bc import box_state
+    n = 16
+    L = 2.0 * np.pi
+    st, _ = box_state((n, n, n))
+    xi = L / n * np.arange(n + 1)
+    Xi, Et, Ze = np.meshgrid(xi, xi, xi, indexing="ij")
+    o = po.Oracle(n, n, n, npdc=(4, 3, 4), bctype=(60, 60, 0, 0, 50, 60), mach=MACH,
+                  reynolds=400.0, deltat=2e-3)
+    x = o.field("x")
+    sl = (slice(H, H + n + 1),) * 3
+    x[sl + (0,)] = Xi + 0.15 * np.sin(Et) * np.sin(Ze)
+    x[sl + (1,)] = Et + 0.15 * np.sin(Ze)
+    x[sl + (2,)] = Ze
+    o.call("gridgeom")
+    for name in ("q", "rho", "vel", "prs", "tmp"):
+        o.field(name)[...] = st[name]
+    D = o.field("dxi")
+    assert np.abs(D[..., 0 + 3 * 1]).max() > 0.1  # x faces: the metric row is skewed
+    g = _gpu_from(o)
+    o.rk3_steps(3)
+    g.time_integration_rk(3)
+    s = g.download_state()
+    g.close()
+    _cmp(o, s)
+
+
+def test_mixed_faces_fp32_storage(gpu_lib):
+    o = _mixed_box()
+    out = {}
+    for name, prec in (("fp64", capi.FP64), ("fp32", capi.FP32_STORAGE)):
+        g = _gpu_from(o, prec)
+        g.time_integration_rk(10)
+        out[name] = g.download_state()
+        g.close()
+    sl = (slice(H, H + o.im + 1), slice(H, H + o.jm + 1), slice(H, H + o.km + 1))
+    a, b = out["fp32"]["q"][sl], out["fp64"]["q"][sl]
+    e = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    print(f"mixed faces, 10 steps: FP32-storage vs FP64 rel L2 {e:.2e}")
+    assert e <= 1e-5
+
+
+def test_boundary_routine_checks(gpu_lib):
+    from astr_gb300.solver import GpuSolver
+    with pytest.raises(capi.AstrError):   # a routine on a periodic direction
+        GpuSolver(16, 16, 16, bctype=(41, 0, 0, 0, 0, 0))
+    with pytest.raises(capi.AstrError):   # adiabatic no-slip exists for x and y faces only
+        GpuSolver(16, 16, 16, npdc=(3, 3, 4), bctype=(0, 0, 0, 0, 42, 0))
+    with pytest.raises(capi.AstrError):   # not built
+        GpuSolver(16, 16, 16, npdc=(4, 3, 3), bctype=(11, 21, 0, 0, 0, 0))
