@@ -1167,6 +1167,7 @@ int run_mpconv(astr_ctx* c) {
                  : (dir == 1 ? launch_mp_face<1>(g, d, m, c->st) : launch_mp_face<2>(g, d, m, c->st));
     prof_end(c);
     RC(launch_result(c, e, "k_mp_face"));
+    if (m.chard) ++c->launches;  // k_mp_face_split before it
     const int last = dir == nd - 1;
     prof_begin(c, KC_MP);
     e = dir == 0 ? launch_mp_diff<0>(g, d, m, c->st, last)
@@ -1567,6 +1568,15 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
     m.fh = (double*)alloc(5 * nh * 8);
     m.ssf = (double*)alloc(nh * 8);
     m.lshock = (unsigned char*)alloc(n0);
+    long long nif = 0;  // interfaces of the largest direction box
+    for (int d = 0; d < ndims; ++d) {
+      long long c1 = dimv[d] + 2;
+      for (int t = 0; t < ndims; ++t)
+        if (t != d) c1 *= dimv[t] + 1;
+      nif = std::max(nif, c1);
+    }
+    m.flist = (int*)alloc((size_t)nif * sizeof(int));
+    m.fcount = (int*)alloc(64);
     m.chard = params->lchardecomp != 0;
     for (int d = 0; d < 3; ++d) m.npdc[d] = npdc[d];
     m.mach = params->mach;

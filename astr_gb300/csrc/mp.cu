@@ -277,9 +277,14 @@ __global__ void __launch_bounds__(256) k_mp_split(Geo g, DevT<double> d, MPDev m
 // threadIdx.y).  Rows first..last = -2..dim+1 (periodic) or -1..dim
 // (physical boundaries); interface i is stored at node i.
 // ---------------------------------------------------------------------------
+// Interior-row weights of the compact upwind right-hand side (bfacmpld folded in).
+struct UpwindWeights {
+  double x, y, z, w;
+};
+
 template <int DIR, int CH>
 __global__ void __launch_bounds__(YZ_LINES * NCH_B, 1)
-k_mp_cflux(Geo g, MPDev m, DScheme<double> SU, DScheme<double> SD, double4 wt) {
+k_mp_cflux(Geo g, MPDev m, DScheme<double> SU, DScheme<double> SD, UpwindWeights wt) {
   __shared__ double sm[SCAN_SMEM_WORDS];
   LineMap<DIR, true> lm(g);
   const long long hs = hstride<DIR>(g), nh = g.nh;
@@ -346,10 +351,63 @@ k_mp_cflux(Geo g, MPDev m, DScheme<double> SU, DScheme<double> SD, double4 wt) {
 // Interface flux, src/solver.F90:1363-1497 (and the j, k copies): one
 // thread per interface i (between nodes i and i+1) of a line.
 // ---------------------------------------------------------------------------
+// The sensor flag of interface f (between nodes f and f+1) of the line
+// through (i, j, k).
 template <int DIR>
-__global__ void __launch_bounds__(128) k_mp_face(Geo g, DevT<double> d, MPDev m, Box b) {
+__device__ __forceinline__ bool iface_shock(const Geo& g, const MPDev& m, int i, int j, int k, int f,
+                                            int dim) {
+  const long long zs = zstride<DIR>(g);
+  const long long zb = zidx(g, i, j, k) - zs * f;
+  auto ls = [&](int l) { return m.lshock[zb + zs * l] != 0; };
+  if (f < 0) return ls(f + 1);
+  if (f + 1 > dim) return ls(f);
+  return ls(f) || ls(f + 1);
+}
+
+// Characteristic form, every interface: where the sensor is off at both
+// nodes MP5 returns the linear value for every characteristic field, so the
+// reference forms R L (fhcp + fhcm) with R L = I; the sum is written here
+// (a rounding-level difference, eps * cond(R)).  Flagged interfaces are
+// listed (warp-aggregated append) for k_mp_face, which then runs densely
+// over them.
+template <int DIR>
+__global__ void __launch_bounds__(256) k_mp_face_split(Geo g, MPDev m, Box b) {
   int i, j, k;
-  if (!box_node(b, (long long)blockIdx.x * blockDim.x + threadIdx.x, i, j, k)) return;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool in = box_node(b, t, i, j, k);
+  bool flagged = false;
+  if (in) {
+    const int f = along<DIR>(i, j, k);
+    const int dim = DIR == 0 ? g.im : (DIR == 1 ? g.jm : g.km);
+    flagged = iface_shock<DIR>(g, m, i, j, k, f, dim);
+    if (!flagged) {
+      const long long nh = g.nh, p = hidx(g, i, j, k);
+      const double* HC = m.fhc + p;
+#pragma unroll
+      for (int r = 0; r < 5; ++r) m.fh[r * nh + p] = HC[r * nh] + HC[(5 + r) * nh];
+    }
+  }
+  const unsigned mask = __ballot_sync(0xffffffffu, flagged);
+  if (mask == 0u) return;
+  const int lane = threadIdx.x & 31, leader = __ffs(mask) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(m.fcount, __popc(mask));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (flagged) m.flist[base + __popc(mask & ((1u << lane) - 1u))] = (int)t;
+}
+
+// Interface flux with the limiter: every interface of the box (no
+// characteristic decomposition: the MP5 test runs everywhere), or the
+// listed ones (characteristic form: the flagged interfaces).
+template <int DIR>
+__global__ void __launch_bounds__(128) k_mp_face(Geo g, DevT<double> d, MPDev m, Box b, int listed) {
+  int i, j, k;
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (listed) {
+    if (t >= *m.fcount) return;
+    t = m.flist[t];
+  }
+  if (!box_node(b, t, i, j, k)) return;
   const int f = along<DIR>(i, j, k);  // interface index
   const long long nh = g.nh, hs = hstride<DIR>(g), zs = zstride<DIR>(g);
   const long long p = hidx(g, i, j, k);
@@ -365,14 +423,10 @@ __global__ void __launch_bounds__(128) k_mp_face(Geo g, DevT<double> d, MPDev m,
     wp[n] = clampi(f + n - 2, iss, iee);
     wm[n] = clampi(f + 3 - n, iss, iee);
   }
-  bool lsh = true;
-  if (m.chard) {
-    const long long zb = zidx(g, i, j, k) - zs * f;
-    auto ls = [&](int l) { return m.lshock[zb + zs * l] != 0; };
-    if (f < 0) lsh = ls(f + 1);
-    else if (f + 1 > dim) lsh = ls(f);
-    else lsh = ls(f) || ls(f + 1);
-  }
+  // without the characteristic decomposition there is no sensor and MP5
+  // limits everywhere; with it, only flagged interfaces reach this kernel
+  const bool lsh = true;
+  (void)zs;
   const double* FP = m.fsw + base;
   const double* FM = m.fsw + 5 * nh + base;
   const double* HC = m.fhc + p;
@@ -388,15 +442,6 @@ __global__ void __launch_bounds__(128) k_mp_face(Geo g, DevT<double> d, MPDev m,
       const double v2 = mplimiter(dn, HC[(5 + c) * nh], lsh, f, dim, npdc);
       out[c * nh] = v1 + v2;
     }
-    return;
-  }
-  if (!lsh) {
-    // The sensor is off at both nodes: MP5 returns the linear value for
-    // every characteristic field, so the reference forms R L (fhcp + fhcm)
-    // with R L = I.  The projection and its inverse are skipped; the sum
-    // differs from the reference's by rounding (eps * cond(R)).
-#pragma unroll
-    for (int r = 0; r < 5; ++r) out[r * nh] = HC[r * nh] + HC[(5 + r) * nh];
     return;
   }
   // chardecomp, src/solver.F90:1958-2162, between nodes f and f+1
@@ -552,8 +597,8 @@ cudaError_t launch_mp_cflux(const Geo& g, const MPDev& m, const MPSchemes& S, cu
   const dim3 gr = sweep_grid<DIR, true>(g), bl = sweep_block<DIR, true>();
   // compact upwind RHS weights, src/flux.F90:243-253
   const double b = m.bfac;
-  const double4 wt = make_double4(1.0 / 18.0 - 1.0 / 36.0 * b, 19.0 / 18.0 - 9.0 / 36.0 * b,
-                                  5.0 / 9.0 + 9.0 / 36.0 * b, 1.0 / 36.0 * b);
+  const UpwindWeights wt{1.0 / 18.0 - 1.0 / 36.0 * b, 19.0 / 18.0 - 9.0 / 36.0 * b,
+                         5.0 / 9.0 + 9.0 / 36.0 * b, 1.0 / 36.0 * b};
   switch (S.CH[DIR]) {
     case 3: k_mp_cflux<DIR, 3><<<gr, bl, 0, st>>>(g, m, S.uw[DIR], S.dw[DIR], wt); break;
     case 5: k_mp_cflux<DIR, 5><<<gr, bl, 0, st>>>(g, m, S.uw[DIR], S.dw[DIR], wt); break;
@@ -568,7 +613,17 @@ cudaError_t launch_mp_cflux(const Geo& g, const MPDev& m, const MPSchemes& S, cu
 template <int DIR>
 cudaError_t launch_mp_face(const Geo& g, const DevT<double>& d, const MPDev& m, cudaStream_t st) {
   const Box b = dir_box<DIR>(g, g.lo[DIR] - 1, g.hi[DIR]);
-  k_mp_face<DIR><<<grid_of(b.count(), 128), 128, 0, st>>>(g, d, m, b);
+  if (!m.chard) {
+    k_mp_face<DIR><<<grid_of(b.count(), 128), 128, 0, st>>>(g, d, m, b, 0);
+    return cudaGetLastError();
+  }
+  cudaError_t e = cudaMemsetAsync(m.fcount, 0, sizeof(int), st);
+  if (e != cudaSuccess) return e;
+  k_mp_face_split<DIR><<<grid_of(b.count(), 256), 256, 0, st>>>(g, m, b);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  // sized for every interface; threads past the listed count return at once
+  k_mp_face<DIR><<<grid_of(b.count(), 128), 128, 0, st>>>(g, d, m, b, 1);
   return cudaGetLastError();
 }
 

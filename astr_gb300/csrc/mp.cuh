@@ -8,7 +8,10 @@
 //   k_mp_face    per interface: Roe eigenvectors (chardecomp,
 //                src/solver.F90:1958-2162), projection of the five-point
 //                stencils and the compact values, MP5 limiting
-//                (src/flux.F90:363-496), back-projection -> Fh;
+//                (src/flux.F90:363-496), back-projection -> Fh; with the
+//                characteristic decomposition only on the interfaces the
+//                sensor flags, listed by k_mp_face_split, which writes the
+//                others;
 //   k_mp_diff    qrhs = qrhs + Fh(i) - Fh(i-1), negated after the last
 //                direction (rhscal's qrhs = -qrhs, src/solver.F90:242).
 // The Ducros sensor (src/commcal.F90:196-353) runs before the directions
@@ -26,6 +29,8 @@ struct MPDev {
   double* fh;             // 5 halo arrays: limited interface flux Fh(i) at node i
   double* ssf;            // halo array: shock-sensor function
   unsigned char* lshock;  // interior array
+  int* flist;             // flagged interfaces of the current direction (box indices)
+  int* fcount;            // their number
   int chard;              // lchardecomp: characteristic projection and sensor
   int npdc[3];
   double mach, rmach, bfac, shkcrt;  // rmach = 1/mach
