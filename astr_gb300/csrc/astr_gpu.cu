@@ -1341,8 +1341,9 @@ size_t astr_gpu_footprint(const astr_dims* dims, const astr_params* params) {
   if (f32) b += 8 * (3 * nh + 5 * n0);
   if (params && params->channel) b += 8 * nh;  // y coordinates
   // compact MP: split fluxes 10, compact interface values 10, interface
-  // flux 5, sensor 1 (halo arrays, FP64) and the shock flags (bytes)
-  if (params && params->conschm == ASTR_CONSCHM_MP) b += 8 * 26 * nh + n0;
+  // flux 5, sensor 1 (halo arrays, FP64), the shock flags (bytes) and the
+  // list of flagged interfaces (at most nh ints)
+  if (params && params->conschm == ASTR_CONSCHM_MP) b += 8 * 26 * nh + n0 + 4 * nh;
   return b;
 }
 

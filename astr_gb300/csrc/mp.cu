@@ -409,7 +409,7 @@ __global__ void __launch_bounds__(128) k_mp_face(Geo g, DevT<double> d, MPDev m,
   }
   if (!box_node(b, t, i, j, k)) return;
   const int f = along<DIR>(i, j, k);  // interface index
-  const long long nh = g.nh, hs = hstride<DIR>(g), zs = zstride<DIR>(g);
+  const long long nh = g.nh, hs = hstride<DIR>(g);
   const long long p = hidx(g, i, j, k);
   const long long base = p - hs * f;
   const int dim = DIR == 0 ? g.im : (DIR == 1 ? g.jm : g.km);
@@ -426,7 +426,6 @@ __global__ void __launch_bounds__(128) k_mp_face(Geo g, DevT<double> d, MPDev m,
   // without the characteristic decomposition there is no sensor and MP5
   // limits everywhere; with it, only flagged interfaces reach this kernel
   const bool lsh = true;
-  (void)zs;
   const double* FP = m.fsw + base;
   const double* FM = m.fsw + 5 * nh + base;
   const double* HC = m.fhc + p;

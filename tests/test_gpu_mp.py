@@ -204,3 +204,22 @@ def test_mp_needs_fp64_main_order(gpu_lib):
     with pytest.raises(capi.AstrError) as e:
         GpuSolver(16, 16, 16, precision=capi.FP32_STORAGE, conschm="543c")
     assert e.value.code == capi.ASTR_ERR_UNSUPPORTED
+
+
+def test_mp_graph_steps_match_plain_steps(gpu_lib):
+    """The compact MP step captured as a CUDA graph (astr_gpu_step_async):
+    the flagged-interface count lives on the device, so the replayed steps
+    are the plain steps."""
+    o = _sod(96, 12, 0.01, 0.1)
+    out = []
+    for graph in (False, True):
+        g = _gpu_from(o)
+        if graph:
+            g.step_async(6)
+            while not g.poll():
+                pass
+        else:
+            g.time_integration_rk(6, stats=False)
+        out.append(g.download_state()["q"])
+        g.close()
+    assert np.array_equal(out[0], out[1])
