@@ -18,6 +18,7 @@ src/initialisation.F90:621-691) and the analytic isentropic vortex, at CFL
 from __future__ import annotations
 
 import collections
+import concurrent.futures as cf
 import math
 import time
 from dataclasses import dataclass, field
@@ -125,9 +126,14 @@ class GpuBackend:
         p.precision = self.precision
         return int(self.L.astr_gpu_footprint(dims, p))
 
-    def start(self, req: Request):
+    def prepare(self, req: Request):
+        """Host-side inputs of a case (grid metrics, initial state, time
+        step); thread-safe, run ahead of admission by the server."""
+        return case_inputs(req)
+
+    def start(self, req: Request, inputs=None):
         from .solver import GpuSolver
-        dims, kw, diag, J, st = case_inputs(req)
+        dims, kw, diag, J, st = inputs if inputs is not None else case_inputs(req)
         g = GpuSolver(*dims, precision=self.precision, **kw)
         g.set_metrics_diag(diag[0], diag[1], diag[2], J)
         g.upload_state(st["q"], st["rho"], st["vel"], st["prs"], st["tmp"])
@@ -168,9 +174,12 @@ class Record:
 
 
 class Server:
-    """First-come-first-served admission by free slots and HBM budget."""
+    """First-come-first-served admission by free slots and HBM budget.  The
+    host-side inputs of the next `prefetch` queued requests are prepared on
+    worker threads while the admitted cases run, when the backend offers
+    prepare()."""
 
-    def __init__(self, backend, hbm_budget: int, max_active: int = 32):
+    def __init__(self, backend, hbm_budget: int, max_active: int = 32, prefetch: int = 4):
         self.b = backend
         self.budget = int(hbm_budget)
         self.max_active = int(max_active)
@@ -180,6 +189,19 @@ class Server:
         self.peak_used = 0
         self.peak_active = 0
         self.launches = 0
+        self.prefetch = int(prefetch) if hasattr(backend, "prepare") else 0
+        self._pool = cf.ThreadPoolExecutor(max_workers=2) if self.prefetch else None
+        self._prepared: dict = {}
+
+    def close(self):
+        if self._pool:
+            self._pool.shutdown(wait=True)
+            self._pool = None
+
+    def _prefetch(self):
+        for req in list(self.queue)[: self.prefetch]:
+            if req.rid not in self._prepared:
+                self._prepared[req.rid] = self._pool.submit(self.b.prepare, req)
 
     def submit(self, req: Request):
         if self.b.footprint(req) > self.budget:
@@ -207,12 +229,18 @@ class Server:
             if self.used + nb > self.budget:
                 break
             self.queue.popleft()
-            h = self.b.start(req)
+            if self.prefetch:
+                fut = self._prepared.pop(req.rid, None)
+                h = self.b.start(req, fut.result() if fut is not None else self.b.prepare(req))
+            else:
+                h = self.b.start(req)
             self.b.enqueue(h, req.steps)
             self.active[req.rid] = _Slot(req, h, nb, now)
             self.used += nb
             self.peak_used = max(self.peak_used, self.used)
             self.peak_active = max(self.peak_active, len(self.active))
+        if self.prefetch:
+            self._prefetch()
         return done
 
 
@@ -319,7 +347,7 @@ class FakeBackend:
     def footprint(self, req):
         return int(request_points(req) * self.bpp)
 
-    def start(self, req):
+    def start(self, req, inputs=None):
         c = _FakeCase(work=request_points(req) * 3 * req.steps)
         self.dev.cases.append(c)
         self.started.append(req.rid)

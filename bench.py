@@ -665,6 +665,7 @@ def run_serve(args, rank, world, dist):
     srv = serve.Server(be, budget, max_active=args.serve_slots)
     barrier(dist)
     recs = serve.serve(reqs, srv)
+    srv.close()
     batched = serve.summarize(reqs, recs)
     batched["makespan_s"] = round(max_over_ranks(dist, batched["makespan_s"]), 3)
     batched["cases_per_s"] = round(len(allreqs) / batched["makespan_s"], 3)

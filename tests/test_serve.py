@@ -82,3 +82,35 @@ def test_partition_across_gpus():
     parts = [serve.partition(reqs, r, 4) for r in range(4)]
     assert sorted(q.rid for p in parts for q in p) == list(range(50))
     assert all(q.rid % 4 == r for r, p in enumerate(parts) for q in p)
+
+
+class _PreparingBackend(serve.FakeBackend):
+    """A backend with host-side preparation: the server must hand each case
+    the inputs prepared for it."""
+
+    def __init__(self, device):
+        super().__init__(device)
+        self.prepared = []
+
+    def prepare(self, req):
+        self.prepared.append(req.rid)
+        return ("inputs", req.rid)
+
+    def start(self, req, inputs=None):
+        assert inputs == ("inputs", req.rid)
+        return super().start(req)
+
+
+def test_scheduler_prefetches_inputs():
+    reqs = serve.make_requests(40, rate=50.0, seed=11, edge3d=(8, 24), edge2d=(16, 64),
+                               steps=(5, 20))
+    dev = serve.FakeDevice(rate=1e6)
+    be = _PreparingBackend(dev)
+    budget = int(sum(be.footprint(r) for r in reqs) * 0.3)
+    srv = serve.Server(be, budget, max_active=4, prefetch=3)
+    recs = serve.serve(reqs, srv, clock=serve.FakeClock(dev), poll_interval=1e-3)
+    srv.close()
+    assert [r.rid for r in recs] == [q.rid for q in reqs]
+    # first come first served, every case prepared exactly once before it started
+    assert be.started == sorted(be.started)
+    assert sorted(be.prepared) == be.started
