@@ -823,6 +823,9 @@ struct astr_ctx {
   int bct[6] = {0, 0, 0, 0, 0, 0};
   double btw[6] = {0, 0, 0, 0, 0, 0};
   bool has_bc = false;
+  // lines per block: one-warp-per-line x layout (warps), block layout (per direction)
+  int lbw = X_LINES;
+  int lbb[3] = {YZ_LINES, YZ_LINES, YZ_LINES};
   // compact MP convective scheme (conschm 543c): scratch and schemes
   bool mp = false;
   MPDev mpd{};
@@ -907,15 +910,18 @@ void prof_end(astr_ctx* c) {
   c->ev_used += 1;
 }
 
+// Warps of the derivative sweep of direction DIR (one statistics partial
+// sum each).
 template <int DIR>
-long long sweep_warps(const Geo& g) {
-  const dim3 gr = sweep_grid<DIR>(g), bl = sweep_block<DIR>();
+long long sweep_warps(const Geo& g, int lbw, const int* lbb) {
+  const int lb = warp_lines<DIR>() ? lbw : lbb[DIR];
+  const dim3 gr = sweep_grid<DIR>(g, lb), bl = sweep_block<DIR>(lb);
   return (long long)gr.x * gr.y * (bl.x * bl.y / 32);
 }
 
 template <typename T>
 SweepCtx<T> sctx(astr_ctx* c) {
-  return SweepCtx<T>{c->g, dev<T>(c), c->ph, c->st, c->gen};
+  return SweepCtx<T>{c->g, dev<T>(c), c->ph, c->st, c->gen, c->lbw, {c->lbb[0], c->lbb[1], c->lbb[2]}};
 }
 
 int launch_result(astr_ctx* c, cudaError_t e, const char* what) {
@@ -1028,8 +1034,9 @@ int stats_finish(astr_ctx* c, double* out2) {
   // partial sums: one per warp of the last convective sweep, or one per
   // block of the point statistics kernel (general metrics)
   const long long nw = c->gen ? (long long)point_grid(c->g.n0).x
-                              : (last == 2 ? sweep_warps<2>(c->g)
-                                           : (last == 1 ? sweep_warps<1>(c->g) : sweep_warps<0>(c->g)));
+                              : (last == 2 ? sweep_warps<2>(c->g, c->lbw, c->lbb)
+                                           : (last == 1 ? sweep_warps<1>(c->g, c->lbw, c->lbb)
+                                                        : sweep_warps<0>(c->g, c->lbw, c->lbb)));
   prof_begin(c, KC_STATS);
   k_stats_final<<<1, 1024, 0, c->st>>>(c->d64.part, nw, c->stats_dev);
   prof_end(c);
@@ -1473,7 +1480,26 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
   c->staging2 = f32 ? (double*)alloc(nh * 8) : nullptr;
   c->jac64 = f32 ? (double*)alloc(nh * 8) : (double*)jac;
   c->rjac64 = (double*)alloc(nh * 8);
-  long long nw = std::max(sweep_warps<0>(g), std::max(sweep_warps<1>(g), sweep_warps<2>(g)));
+  // lines per block: the largest that still gives every SM blocks (the
+  // one-warp-per-line x layout wants MINB_X blocks per SM, the block layout
+  // two); small grids launch fewer lines per block.  FP64 form only: its
+  // sweeps are FP64-bound and gain from the SMs (vortex 512^2: 224 -> 280
+  // Mpts*stages/s); the FP32-storage sweeps are load-latency bound and lose
+  // a little with the narrower rows of 4-line blocks (443 -> 435).
+  {
+    const bool adapt = !std::getenv("ASTR_FIXED_BLOCKS") && c->prec == ASTR_FP64;
+    const long long nsm = 152;
+    const long long xl = (long long)(g.jm + 1) * (g.km + 1);
+    c->lbw = X_LINES;
+    while (adapt && c->lbw > 1 && (xl + c->lbw - 1) / c->lbw < MINB_X * nsm) c->lbw /= 2;
+    for (int d = 0; d < 3; ++d) {
+      const long long na = (d == 0 ? g.jm : g.im) + 1, nb = (d == 2 ? g.jm : g.km) + 1;
+      c->lbb[d] = YZ_LINES;
+      while (adapt && c->lbb[d] > 4 && ((na + c->lbb[d] - 1) / c->lbb[d]) * nb < 2 * nsm) c->lbb[d] /= 2;
+    }
+  }
+  long long nw = std::max(sweep_warps<0>(g, c->lbw, c->lbb),
+                          std::max(sweep_warps<1>(g, c->lbw, c->lbb), sweep_warps<2>(g, c->lbw, c->lbb)));
   nw = std::max(nw, (long long)((g.n0 + 255) / 256));  // point statistics blocks
   double* part = (double*)alloc(2 * nw * 8);
   int* flag = (int*)alloc(64);
@@ -1589,6 +1615,7 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
       const int dim = std::max(dimv[d], 1);
       const int rows = npdc[d] == 4 ? dim + 2 : dim + 4;
       c->mps.CH[d] = d < ndims ? pick_ch(rows, NCH_B) : 3;
+      c->mps.lbb[d] = c->lbb[d];
       if (c->mps.CH[d] < 0) ok = false;
       fs.push_back(make_flux(npdc[d], dim, +1, params->bfacmpld, std::max(c->mps.CH[d], 3), hft));
       fs.push_back(make_flux(npdc[d], dim, -1, params->bfacmpld, std::max(c->mps.CH[d], 3), hft));

@@ -159,7 +159,9 @@ struct SweepCtx {
   DevT<T> d;
   Phys ph;
   cudaStream_t st;
-  bool gen;  // general (non-diagonal) metrics
+  bool gen;    // general (non-diagonal) metrics
+  int lbw;     // lines (warps) per block of the one-warp-per-line x layout
+  int lbb[3];  // lines per block of the block layout, per direction
 };
 
 __device__ __forceinline__ long long hidx(const Geo& g, int i, int j, int k) {
@@ -184,9 +186,11 @@ __device__ __forceinline__ void line_ijk(int a, int b, int l, int& i, int& j, in
 }
 
 // Line layout.  x sweeps with XB false hold one line per warp (lane = chunk,
-// shuffle scans); every other sweep uses blocks of YZ_LINES lines x 32
-// chunks with shared-memory scans (XB: the x filter, measured faster that
-// way; the x derivative sweeps are faster one line per warp).
+// shuffle scans); every other sweep uses blocks of lines x 32 chunks with
+// shared-memory scans (XB: the x filter, measured faster that way; the x
+// derivative sweeps are faster one line per warp).  The lines (warps) per
+// block are the launch's blockDim.x (blockDim.y), at most YZ_LINES
+// (X_LINES): small grids launch fewer per block to occupy more SMs.
 template <int DIR, bool XB = false>
 constexpr bool warp_lines() { return DIR == 0 && !XB; }
 
@@ -199,7 +203,7 @@ struct LineMap {
   __device__ __forceinline__ LineMap(const Geo& g) {
     if (warp_lines<DIR, XB>()) {
       c = threadIdx.x;
-      const long long line = (long long)blockIdx.x * X_LINES + threadIdx.y;
+      const long long line = (long long)blockIdx.x * blockDim.y + threadIdx.y;
       const long long na = g.jm + 1, nl = na * (g.km + 1);
       active = line < nl;
       const long long L = active ? line : 0;
@@ -208,7 +212,7 @@ struct LineMap {
     } else {
       c = threadIdx.y;
       const int amax = DIR == 0 ? g.jm : g.im;
-      const int ai = blockIdx.x * YZ_LINES + threadIdx.x;
+      const int ai = blockIdx.x * blockDim.x + threadIdx.x;
       active = ai <= amax;
       a = active ? ai : amax;
       b = blockIdx.y;
@@ -264,9 +268,10 @@ __device__ __forceinline__ T scan_block(T M, T L, T* sm) {
   sM[ty * SM_PITCH + tx] = M;
   sL[ty * SM_PITCH + tx] = L;
   __syncthreads();
-  const int tid = tx + YZ_LINES * ty;
+  const int nl = blockDim.x;  // lines in this block (at most YZ_LINES)
+  const int tid = tx + nl * ty;
   const int w = tid >> 5, lane = tid & 31;
-  if (w < YZ_LINES) {
+  if (w < nl) {
     constexpr int CPL = NCH_B / 32;
     T ml[CPL], ll[CPL];
 #pragma unroll

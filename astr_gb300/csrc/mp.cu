@@ -593,7 +593,8 @@ cudaError_t launch_mp_split(const Geo& g, const DevT<double>& d, const MPDev& m,
 
 template <int DIR>
 cudaError_t launch_mp_cflux(const Geo& g, const MPDev& m, const MPSchemes& S, cudaStream_t st) {
-  const dim3 gr = sweep_grid<DIR, true>(g), bl = sweep_block<DIR, true>();
+  const int lb = S.lbb[DIR];
+  const dim3 gr = sweep_grid<DIR, true>(g, lb), bl = sweep_block<DIR, true>(lb);
   // compact upwind RHS weights, src/flux.F90:243-253
   const double b = m.bfac;
   const UpwindWeights wt{1.0 / 18.0 - 1.0 / 36.0 * b, 19.0 / 18.0 - 9.0 / 36.0 * b,

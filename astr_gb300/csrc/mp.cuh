@@ -39,6 +39,7 @@ struct MPDev {
 struct MPSchemes {
   DScheme<double> uw[3], dw[3];
   int CH[3];
+  int lbb[3];  // lines per block of the block layout, per direction
 };
 
 // node range of the flux split (iss..iee), src/solver.F90:1318-1332

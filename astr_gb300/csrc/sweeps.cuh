@@ -83,8 +83,6 @@ k_filter(Geo g, DevT<T> d, DScheme<T> S, FTab<T> Tb, Phys ph, int do_q2f) {
 template <typename T>
 constexpr bool stage_flux() { return sizeof(T) == 4; }
 
-template <typename T, int DIR>
-__host__ __device__ constexpr int flux_lines() { return warp_lines<DIR>() ? X_LINES : YZ_LINES; }
 
 // GEN: general metrics.  The convective flux uses the whole metric row
 // (U = dxi(d,1) u + dxi(d,2) v + dxi(d,3) w, pressure terms dxi(d,m) p, as
@@ -102,7 +100,7 @@ k_convgrad(Geo g, DevT<T> d, DScheme<T> S, Phys ph, CGFlags fl) {
   const bool uni = uniform_chunk<DIR, false>(S, lm.c);
   if (warp_lines<DIR>() && !lm.active) {  // whole warp: x-lines own a warp
     if (fl.stats && threadIdx.x == 0) {
-      const long long wid = (long long)blockIdx.x * X_LINES + threadIdx.y;
+      const long long wid = (long long)blockIdx.x * blockDim.y + threadIdx.y;
       d.part[2 * wid] = 0.0;
       d.part[2 * wid + 1] = 0.0;
     }
@@ -124,7 +122,7 @@ k_convgrad(Geo g, DevT<T> d, DScheme<T> S, Phys ph, CGFlags fl) {
 
   if (fl.conv) {
     constexpr bool stg = stage_flux<T>() && !GEN;
-    constexpr int NL = flux_lines<T, DIR>();
+    const int NL = warp_lines<DIR>() ? (int)blockDim.y : (int)blockDim.x;  // lines in the block
     T* fa = reinterpret_cast<T*>(conv_smem);
     const int np = S.n + 6;  // rows -3 .. n+2
     T* fb = fa + (size_t)np * NL;
@@ -397,17 +395,17 @@ k_visc(Geo g, DevT<T> d, DScheme<T> S, Phys ph, VFlags fl) {
 template <typename T, int DIR>
 cudaError_t launch_filter(const SweepCtx<T>& c, const DScheme<T>& S, const FTab<T>& Tb, int CH,
                           int do_q2f) {
-  const dim3 gr = sweep_grid<DIR, true>(c.g), bl = sweep_block<DIR, true>();
+  const int lb = sweep_lb<DIR, true>(c);
+  const dim3 gr = sweep_grid<DIR, true>(c.g, lb), bl = sweep_block<DIR, true>(lb);
   ASTR_CH_SWITCH(CH, (k_filter<T, DIR, CHC><<<gr, bl, 0, c.st>>>(c.g, c.d, S, Tb, c.ph, do_q2f)));
   return cudaGetLastError();
 }
 
 template <typename T, int DIR, int CH, bool GEN>
 cudaError_t launch_convgrad_gen(const SweepCtx<T>& c, const DScheme<T>& S, CGFlags f) {
-  const dim3 gr = sweep_grid<DIR>(c.g), bl = sweep_block<DIR>();
-  const size_t dyn = (stage_flux<T>() && !GEN && f.conv)
-                         ? 2 * (size_t)(S.n + 6) * flux_lines<T, DIR>() * sizeof(T)
-                         : 0;
+  const int lb = sweep_lb<DIR, false>(c);
+  const dim3 gr = sweep_grid<DIR>(c.g, lb), bl = sweep_block<DIR>(lb);
+  const size_t dyn = (stage_flux<T>() && !GEN && f.conv) ? 2 * (size_t)(S.n + 6) * lb * sizeof(T) : 0;
   static size_t attr_bytes = 48 * 1024;  // dynamic shared memory allowed so far (per instantiation)
   if (dyn > attr_bytes) {
     const cudaError_t ea = cudaFuncSetAttribute(k_convgrad<T, DIR, CH, GEN>,
@@ -443,7 +441,8 @@ cudaError_t launch_convgrad(const SweepCtx<T>& c, const DScheme<T>& S, int CH, C
 
 template <typename T, int DIR>
 cudaError_t launch_visc(const SweepCtx<T>& c, const DScheme<T>& S, int CH, VFlags f) {
-  const dim3 gr = sweep_grid<DIR>(c.g), bl = sweep_block<DIR>();
+  const int lb = sweep_lb<DIR, false>(c);
+  const dim3 gr = sweep_grid<DIR>(c.g, lb), bl = sweep_block<DIR>(lb);
   if (c.gen) {
     ASTR_CH_SWITCH(CH, (k_visc<T, DIR, CHC, true><<<gr, bl, 0, c.st>>>(c.g, c.d, S, c.ph, f)));
   } else {
