@@ -1497,6 +1497,16 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
       c->lbb[d] = YZ_LINES;
       while (adapt && c->lbb[d] > 4 && ((na + c->lbb[d] - 1) / c->lbb[d]) * nb < 2 * nsm) c->lbb[d] /= 2;
     }
+    // launch-shape override for tuning: "warps,x,y,z" (powers of two within the maxima)
+    if (const char* e = std::getenv("ASTR_LINES_PER_BLOCK")) {
+      int v[4];
+      if (std::sscanf(e, "%d,%d,%d,%d", &v[0], &v[1], &v[2], &v[3]) == 4) {
+        auto ok = [](int x, int mx) { return x >= 1 && x <= mx && (x & (x - 1)) == 0; };
+        if (ok(v[0], X_LINES)) c->lbw = v[0];
+        for (int d = 0; d < 3; ++d)
+          if (ok(v[1 + d], YZ_LINES)) c->lbb[d] = v[1 + d];
+      }
+    }
   }
   long long nw = std::max(sweep_warps<0>(g, c->lbw, c->lbb),
                           std::max(sweep_warps<1>(g, c->lbw, c->lbb), sweep_warps<2>(g, c->lbw, c->lbb)));

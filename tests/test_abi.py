@@ -39,3 +39,34 @@ def test_create_rejects_bad_dims(gpu_lib):
     rc = gpu_lib.astr_gpu_create(ctypes.byref(d), ctypes.byref(p), ctypes.byref(h))
     assert rc == capi.ASTR_ERR_ARG
     assert "too small" in capi.last_error(None)
+
+
+def _params(**kw):
+    from astr_gb300 import capi
+    p = capi.AstrParams(0, 0, 1, 1, 0.49, 1.11, 0.98, 0.1, 1600.0, 0.72, 273.15, 110.3, 1e-3)
+    for k, v in kw.items():
+        if k == "bctype":
+            p.bctype = (ctypes.c_int * 6)(*v)
+        else:
+            setattr(p, k, v)
+    return p
+
+
+@pytest.mark.parametrize("npdc, kw, code, text", [
+    ((3, 3, 3), dict(bctype=(41, 0, 0, 0, 0, 0), twall=1.0), "ARG", "npdc = 4"),
+    ((3, 3, 4), dict(bctype=(0, 0, 0, 0, 42, 0)), "UNSUPPORTED", "x and y faces"),
+    ((4, 3, 3), dict(bctype=(11, 21, 0, 0, 0, 0)), "UNSUPPORTED", "bctype"),
+    ((4, 3, 3), dict(bctype=(41, 0, 0, 0, 0, 0), twall=0.0), "ARG", "wall temperature"),
+    ((3, 3, 3), dict(conschm=1, precision=1), "UNSUPPORTED", "FP64"),
+    ((3, 3, 3), dict(conschm=7), "ARG", "conschm"),
+])
+def test_create_checks_without_gpu(gpu_lib, npdc, kw, code, text):
+    """Boundary routines and the convective scheme are checked before any
+    device call: the context is refused on a machine without a GPU too."""
+    from astr_gb300 import capi
+    d = capi.AstrDims(16, 16, 16, 16, 16, 16, *npdc)
+    p = _params(**kw)
+    h = ctypes.c_void_p()
+    rc = gpu_lib.astr_gpu_create(ctypes.byref(d), ctypes.byref(p), ctypes.byref(h))
+    assert rc == getattr(capi, "ASTR_ERR_" + code), (rc, capi.last_error(None))
+    assert text in capi.last_error(None)
