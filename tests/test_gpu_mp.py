@@ -223,3 +223,36 @@ def test_mp_graph_steps_match_plain_steps(gpu_lib):
         out.append(g.download_state()["q"])
         g.close()
     assert np.array_equal(out[0], out[1])
+
+
+def test_mp_with_walls_matches_oracle(gpu_lib):
+    """The compact MP scheme with boundary routines: a 2-D box with
+    adiabatic no-slip x-walls and symmetry y-planes, the viscous terms and a
+    pressure jump in x (a shock running between the walls)."""
+    from oracle import pyoracle as po
+    from test_bc import box_state
+    im, jm = 64, 32
+    st, grid = box_state((im, jm, 0))
+    sl = (slice(H, H + im + 1), slice(H, H + jm + 1), H)
+    x = grid[0]
+    st["prs"][sl] *= (1.0 + 0.8 * (x < np.pi)).reshape(-1, 1)
+    c = cases.refcal(0.3, 1600.0)
+    rho, p = st["rho"][sl], st["prs"][sl]
+    u, v = st["vel"][sl + (0,)], st["vel"][sl + (1,)]
+    st["tmp"][sl] = p / rho * c["const2"]
+    st["q"][sl + (4,)] = rho * (st["tmp"][sl] * c["const1"] + 0.5 * (u * u + v * v))
+    o = po.from_state(st, (im, jm, 0), grid=grid, npdc=(4, 4, 3), mach=0.3, reynolds=400.0,
+                      deltat=2e-3, conschm="543c", lfilter=False, bctype=(42, 42, 60, 60, 0, 0))
+    _zero_offdiag(o)
+    from astr_gb300.solver import GpuSolver
+    g = GpuSolver(im, jm, 0, npdc=(4, 4, 3), mach=0.3, reynolds=400.0, deltat=2e-3,
+                  lfilter=False, conschm="543c", bctype=(42, 42, 60, 60, 0, 0))
+    g.set_metrics(o.field("dxi").copy(order="F"), o.field("jacob").copy(order="F"))
+    g.upload_state(o.field("q"), o.field("rho"), o.field("vel"), o.field("prs"), o.field("tmp"))
+    o.rk3_steps(8)
+    g.time_integration_rk(8)
+    s = g.download_state()
+    g.close()
+    ls = o.lshock()
+    assert ls.any() and not ls.all()
+    _cmp(o, s)
