@@ -826,6 +826,9 @@ struct astr_ctx {
   // lines per block: one-warp-per-line x layout (warps), block layout (per direction)
   int lbw = X_LINES;
   int lbb[3] = {YZ_LINES, YZ_LINES, YZ_LINES};
+  // small grids: the variables of a line spread over blocks (gridDim.z) and
+  // the stress, RK3 update and statistics run as point kernels
+  bool vsplit = false;
   // compact MP convective scheme (conschm 543c): scratch and schemes
   bool mp = false;
   MPDev mpd{};
@@ -921,7 +924,8 @@ long long sweep_warps(const Geo& g, int lbw, const int* lbb) {
 
 template <typename T>
 SweepCtx<T> sctx(astr_ctx* c) {
-  return SweepCtx<T>{c->g, dev<T>(c), c->ph, c->st, c->gen, c->lbw, {c->lbb[0], c->lbb[1], c->lbb[2]}};
+  return SweepCtx<T>{c->g, dev<T>(c), c->ph, c->st, c->gen, c->lbw, {c->lbb[0], c->lbb[1], c->lbb[2]},
+                     c->vsplit ? 1 : 0};
 }
 
 int launch_result(astr_ctx* c, cudaError_t e, const char* what) {
@@ -1033,7 +1037,7 @@ int stats_finish(astr_ctx* c, double* out2) {
   const int last = c->g.ndims - 1;
   // partial sums: one per warp of the last convective sweep, or one per
   // block of the point statistics kernel (general metrics)
-  const long long nw = c->gen ? (long long)point_grid(c->g.n0).x
+  const long long nw = (c->gen || c->vsplit) ? (long long)point_grid(c->g.n0).x
                               : (last == 2 ? sweep_warps<2>(c->g, c->lbw, c->lbb)
                                            : (last == 1 ? sweep_warps<1>(c->g, c->lbw, c->lbb)
                                                         : sweep_warps<0>(c->g, c->lbw, c->lbb)));
@@ -1199,20 +1203,19 @@ int one_step(astr_ctx* c, double* stats) {
       RC(run_filter<T>(c, true));
     } else {
       const bool visc = c->pm.diffterm != 0;
-      const bool split_sig = visc && ((c->split_last & 1) || c->gen);
-      const bool split_rk = visc && (c->split_last & 2);
+      const bool split_sig = visc && ((c->split_last & 1) || c->gen || c->vsplit);
+      const bool split_rk = visc && ((c->split_last & 2) || c->vsplit);
+      const bool pt_stats = c->gen || c->vsplit;  // statistics by the point kernel
       if (c->pm.lfilter) RC(run_filter<T>(c, false));
       if (c->has_bc) RC(run_boucon<T>(c));
       RC(run_qswap<T>(c));
       // compact MP: the sweeps give the gradients (and the RK3 base), the
       // convective residual comes from the MP kernels
-      RC(run_convgrad<T>(c, !c->mp, true, visc && !split_sig, st1 && stats && !c->gen, st1));
-      if (c->gen) {
-        // general metrics: gradients contracted with the metrics, then the
-        // statistics from them
-        RC(gradphys_pointwise<T>(c));
-        if (st1 && stats) RC(stats_pointwise<T>(c));
-      }
+      RC(run_convgrad<T>(c, !c->mp, true, visc && !split_sig, st1 && stats && !pt_stats, st1));
+      // general metrics: gradients contracted with the metrics; then the
+      // statistics from them where the sweeps do not take them
+      if (c->gen) RC(gradphys_pointwise<T>(c));
+      if (pt_stats && st1 && stats) RC(stats_pointwise<T>(c));
       if (split_sig) RC(sigma_pointwise<T>(c));
       if (c->mp) RC(run_mpconv(c));
       if (c->channel) RC(run_chan<T>(c, st1));
@@ -1508,6 +1511,15 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
       }
     }
   }
+  {
+    // fewer y-line blocks than SMs: spread the variables of a line over
+    // blocks (mini-app ordering excluded: its last filter direction
+    // recovers the primitives of all variables)
+    const long long yblocks = ((g.im + 1 + c->lbb[1] - 1) / c->lbb[1]) * (long long)(g.km + 1);
+    c->vsplit = yblocks < 152 && params->order == ASTR_ORDER_MAIN;
+    if (const char* e = std::getenv("ASTR_VAR_SPLIT"))
+      c->vsplit = std::atoi(e) != 0 && params->order == ASTR_ORDER_MAIN;
+  }
   long long nw = std::max(sweep_warps<0>(g, c->lbw, c->lbb),
                           std::max(sweep_warps<1>(g, c->lbw, c->lbb), sweep_warps<2>(g, c->lbw, c->lbb)));
   nw = std::max(nw, (long long)((g.n0 + 255) / 256));  // point statistics blocks
@@ -1626,6 +1638,7 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
       const int rows = npdc[d] == 4 ? dim + 2 : dim + 4;
       c->mps.CH[d] = d < ndims ? pick_ch(rows, NCH_B) : 3;
       c->mps.lbb[d] = c->lbb[d];
+      c->mps.vsplit = c->vsplit ? 1 : 0;
       if (c->mps.CH[d] < 0) ok = false;
       fs.push_back(make_flux(npdc[d], dim, +1, params->bfacmpld, std::max(c->mps.CH[d], 3), hft));
       fs.push_back(make_flux(npdc[d], dim, -1, params->bfacmpld, std::max(c->mps.CH[d], 3), hft));
@@ -2023,13 +2036,19 @@ int astr_gpu_updatefvar(astr_ctx* c) {
 
 int astr_gpu_reduce_stats(astr_ctx* c, double* ke, double* en) {
   RC(ready(c));
-  // statistics over the current primitives and gradients: the last
-  // conv/grad direction with only the statistics enabled
-  CGFlags f{0, 0, 0, 0, 0, 1, 0};
-  const int last = c->g.ndims - 1;
+  // statistics over the current primitives and gradients: the point
+  // kernel where the step takes them from it (general metrics, variables
+  // split over blocks), else the last conv/grad direction with only the
+  // statistics enabled (stats_finish reads the matching partial sums)
   int r;
-  if (c->prec == ASTR_FP64) r = last == 2 ? launch_convgrad<double, 2>(c, f) : launch_convgrad<double, 1>(c, f);
-  else r = last == 2 ? launch_convgrad<float, 2>(c, f) : launch_convgrad<float, 1>(c, f);
+  if (c->gen || c->vsplit) {
+    r = c->prec == ASTR_FP64 ? stats_pointwise<double>(c) : stats_pointwise<float>(c);
+  } else {
+    CGFlags f{0, 0, 0, 0, 0, 1, 0};
+    const int last = c->g.ndims - 1;
+    if (c->prec == ASTR_FP64) r = last == 2 ? launch_convgrad<double, 2>(c, f) : launch_convgrad<double, 1>(c, f);
+    else r = last == 2 ? launch_convgrad<float, 2>(c, f) : launch_convgrad<float, 1>(c, f);
+  }
   RC(r);
   double o[2];
   RC(stats_finish(c, o));

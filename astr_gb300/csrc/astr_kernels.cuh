@@ -162,6 +162,7 @@ struct SweepCtx {
   bool gen;    // general (non-diagonal) metrics
   int lbw;     // lines (warps) per block of the one-warp-per-line x layout
   int lbb[3];  // lines per block of the block layout, per direction
+  int vsplit;  // 1: the variables of a line spread over gridDim.z blocks
 };
 
 __device__ __forceinline__ long long hidx(const Geo& g, int i, int j, int k) {
@@ -319,6 +320,13 @@ __device__ __forceinline__ T scan_block(T M, T L, T* sm) {
   __syncthreads();
   return r;
 }
+
+// Whether task t (a variable of the sweep) is this block's: with gridDim.z
+// > 1 the variables of a line are spread over the z blocks, one each (small
+// grids, where one block per line group would leave SMs idle).  Tested
+// inside the sweeps' constant-bound loops, so the unsplit kernels keep
+// their register allocation.
+__device__ __forceinline__ bool my_task(int t) { return gridDim.z == 1 || (int)blockIdx.z == t; }
 
 // Is chunk c of a y/z sweep one of the scheme's uniform chunks?  (x sweeps
 // hold a whole line in one warp, where a per-chunk branch would diverge.)

@@ -299,6 +299,7 @@ k_mp_cflux(Geo g, MPDev m, DScheme<double> SU, DScheme<double> SD, UpwindWeights
   mp_split_range(m.npdc[DIR], dim, iss, iee);
 #pragma unroll 1
   for (int v = 0; v < 10; ++v) {
+    if (!my_task(v)) continue;
     const DScheme<double>& S = v < 5 ? SU : SD;
     const bool up = v < 5;
     const double* f = m.fsw + v * nh + base;
@@ -594,7 +595,9 @@ cudaError_t launch_mp_split(const Geo& g, const DevT<double>& d, const MPDev& m,
 template <int DIR>
 cudaError_t launch_mp_cflux(const Geo& g, const MPDev& m, const MPSchemes& S, cudaStream_t st) {
   const int lb = S.lbb[DIR];
-  const dim3 gr = sweep_grid<DIR, true>(g, lb), bl = sweep_block<DIR, true>(lb);
+  dim3 gr = sweep_grid<DIR, true>(g, lb);
+  const dim3 bl = sweep_block<DIR, true>(lb);
+  gr.z = S.vsplit ? 10 : 1;
   // compact upwind RHS weights, src/flux.F90:243-253
   const double b = m.bfac;
   const UpwindWeights wt{1.0 / 18.0 - 1.0 / 36.0 * b, 19.0 / 18.0 - 9.0 / 36.0 * b,

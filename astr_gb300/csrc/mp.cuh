@@ -40,6 +40,7 @@ struct MPSchemes {
   DScheme<double> uw[3], dw[3];
   int CH[3];
   int lbb[3];  // lines per block of the block layout, per direction
+  int vsplit;  // 1: the ten variables of a line spread over gridDim.z blocks
 };
 
 // node range of the flux split (iss..iee), src/solver.F90:1318-1332

@@ -31,6 +31,7 @@ k_filter(Geo g, DevT<T> d, DScheme<T> S, FTab<T> Tb, Phys ph, int do_q2f) {
   const int per = g.per[DIR] ? 1 : 0;
 #pragma unroll 1
   for (int n = 0; n < 5; ++n) {
+    if (!my_task(n)) continue;
     T* v = d.q + n * g.nh;
     // FP64: the reference's form, x = A^{-1} B f.  FP32: the increment
     // form, x = f + A^{-1} (B - A) f (see filter_rhs_delta), with the
@@ -120,7 +121,10 @@ k_convgrad(Geo g, DevT<T> d, DScheme<T> S, Phys ph, CGFlags fl) {
   const T rdx = pc<T>(ph.rdx[DIR], ph.f_rdx[DIR]);
   const T* xd = d.xd + DIR * nh;
 
-  if (fl.conv) {
+  // tasks: the five convective fluxes (fl.conv), then the four gradients
+  // (fl.grad); the RK3 base, stress and statistics only without a split
+  const int nconv = fl.conv ? 5 : 0;
+  if (fl.conv && (gridDim.z == 1 || (int)blockIdx.z < nconv)) {
     constexpr bool stg = stage_flux<T>() && !GEN;
     const int NL = warp_lines<DIR>() ? (int)blockDim.y : (int)blockDim.x;  // lines in the block
     T* fa = reinterpret_cast<T*>(conv_smem);
@@ -155,6 +159,7 @@ k_convgrad(Geo g, DevT<T> d, DScheme<T> S, Phys ph, CGFlags fl) {
     }
 #pragma unroll 1
     for (int n = 0; n < 5; ++n) {
+      if (!my_task(n)) continue;
       auto f = [&](int node) -> T {
         const long long p = bh + hs * node;
         const T qn = d.q[p + n * nh];
@@ -218,6 +223,7 @@ k_convgrad(Geo g, DevT<T> d, DScheme<T> S, Phys ph, CGFlags fl) {
   if (fl.grad) {
 #pragma unroll 1
     for (int n = 0; n < 4; ++n) {
+      if (!my_task(n + nconv)) continue;
       const T* src = d.pr + (n < 3 ? 1 + n : 5) * nh;
       auto f = [&](int node) -> T { return src[bh + hs * node]; };
       T y[CH];
@@ -236,7 +242,7 @@ k_convgrad(Geo g, DevT<T> d, DScheme<T> S, Phys ph, CGFlags fl) {
       }
     }
   }
-  if (fl.qsave && lm.active) {
+  if (fl.qsave && lm.active && blockIdx.z == 0) {
     // RK3 base at stage 1 (src/mainloop.F90:427-433): q*J (mini-app: q)
 #pragma unroll
     for (int t = 0; t < CH; ++t) {
@@ -251,7 +257,7 @@ k_convgrad(Geo g, DevT<T> d, DScheme<T> S, Phys ph, CGFlags fl) {
       }
     }
   }
-  if (fl.last && fl.sigma && lm.active) {
+  if (fl.last && fl.sigma && lm.active && gridDim.z == 1) {
 #pragma unroll
     for (int t = 0; t < CH; ++t) {
       const int node = S.first + lm.c * CH + t;
@@ -325,6 +331,7 @@ k_visc(Geo g, DevT<T> d, DScheme<T> S, Phys ph, VFlags fl) {
   constexpr int s2 = DIR == 0 ? 2 : (DIR == 1 ? 4 : 5);
 #pragma unroll 1
   for (int n = 0; n < 4; ++n) {
+    if (!my_task(n)) continue;
     const int sc = n == 0 ? s0 : (n == 1 ? s1 : s2);
     const T* src = n < 3 ? d.sig + sc * n0 : d.qf + DIR * n0;
     auto f = [&](int node) -> T {
@@ -396,7 +403,9 @@ template <typename T, int DIR>
 cudaError_t launch_filter(const SweepCtx<T>& c, const DScheme<T>& S, const FTab<T>& Tb, int CH,
                           int do_q2f) {
   const int lb = sweep_lb<DIR, true>(c);
-  const dim3 gr = sweep_grid<DIR, true>(c.g, lb), bl = sweep_block<DIR, true>(lb);
+  dim3 gr = sweep_grid<DIR, true>(c.g, lb);
+  const dim3 bl = sweep_block<DIR, true>(lb);
+  gr.z = c.vsplit ? 5 : 1;
   ASTR_CH_SWITCH(CH, (k_filter<T, DIR, CHC><<<gr, bl, 0, c.st>>>(c.g, c.d, S, Tb, c.ph, do_q2f)));
   return cudaGetLastError();
 }
@@ -404,7 +413,10 @@ cudaError_t launch_filter(const SweepCtx<T>& c, const DScheme<T>& S, const FTab<
 template <typename T, int DIR, int CH, bool GEN>
 cudaError_t launch_convgrad_gen(const SweepCtx<T>& c, const DScheme<T>& S, CGFlags f) {
   const int lb = sweep_lb<DIR, false>(c);
-  const dim3 gr = sweep_grid<DIR>(c.g, lb), bl = sweep_block<DIR>(lb);
+  dim3 gr = sweep_grid<DIR>(c.g, lb);
+  const dim3 bl = sweep_block<DIR>(lb);
+  const int ntask = (f.conv ? 5 : 0) + (f.grad ? 4 : 0);
+  gr.z = c.vsplit && ntask > 1 ? ntask : 1;
   const size_t dyn = (stage_flux<T>() && !GEN && f.conv) ? 2 * (size_t)(S.n + 6) * lb * sizeof(T) : 0;
   static size_t attr_bytes = 48 * 1024;  // dynamic shared memory allowed so far (per instantiation)
   if (dyn > attr_bytes) {
@@ -442,7 +454,9 @@ cudaError_t launch_convgrad(const SweepCtx<T>& c, const DScheme<T>& S, int CH, C
 template <typename T, int DIR>
 cudaError_t launch_visc(const SweepCtx<T>& c, const DScheme<T>& S, int CH, VFlags f) {
   const int lb = sweep_lb<DIR, false>(c);
-  const dim3 gr = sweep_grid<DIR>(c.g, lb), bl = sweep_block<DIR>(lb);
+  dim3 gr = sweep_grid<DIR>(c.g, lb);
+  const dim3 bl = sweep_block<DIR>(lb);
+  gr.z = c.vsplit ? 4 : 1;
   if (c.gen) {
     ASTR_CH_SWITCH(CH, (k_visc<T, DIR, CHC, true><<<gr, bl, 0, c.st>>>(c.g, c.d, S, c.ph, f)));
   } else {
