@@ -35,6 +35,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -126,7 +127,7 @@ class ClockSampler:
     def __init__(self, gpu_index=0):
         self.gpu = gpu_index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+        self.path = os.path.join(tempfile.gettempdir(), f"astr_clocks_{os.getpid()}_{id(self)}.csv")
 
     def start(self):
         try:
