@@ -156,6 +156,7 @@ __global__ void k_rkupdate(Geo g, DevT<T> d, Phys ph, int q2f) {
 //   41 noslip (6306-6712): u = 0, T = T_w, p extrapolated, rho = p/T*const2,
 //      q with pressure;
 //   42 noslip_adibatic (6728-7036, x and y faces): p and T extrapolated;
+//   421 slipadibwall (7231-7430, y faces): p, T and u extrapolated;
 //   50 zeroextrap (2356-2652): x faces extrapolate T, the others rho; q with
 //      temperature on ymax only;
 //   60 symmetry (2664-2996): x faces and zmax remove the velocity along the
@@ -202,6 +203,15 @@ __global__ void k_face_bc(Geo g, DevT<T> d, Phys ph, int n, int type, double tw,
     pe = (1.0 / 3.0) * (4.0 * prim(p1, 4) - prim(p2, 4));
     te = (1.0 / 3.0) * (4.0 * prim(p1, 5) - prim(p2, 5));
     u = v = w = 0.0;
+    ro = pe / te * c2;
+  } else if (type == 421) {
+    // slipadibwall (7231-7430, y faces): p, T, u extrapolated; v = 0 on
+    // ymin, extrapolated on ymax (as the reference writes it); w = 0
+    pe = (1.0 / 3.0) * (4.0 * prim(p1, 4) - prim(p2, 4));
+    te = (1.0 / 3.0) * (4.0 * prim(p1, 5) - prim(p2, 5));
+    u = (1.0 / 3.0) * (4.0 * prim(p1, 1) - prim(p2, 1));
+    v = n == 3 ? (1.0 / 3.0) * (4.0 * prim(p1, 2) - prim(p2, 2)) : 0.0;
+    w = 0.0;
     ro = pe / te * c2;
   } else {
     u = bc_ex2(prim(p1, 1), prim(p2, 1));
@@ -1112,7 +1122,7 @@ int run_boucon(astr_ctx* c) {
   const double const6 = 1.0 / (gamma - 1.0);
   for (int n = 0; n < 2 * g.ndims; ++n) {
     const int type = c->bct[n];
-    if (type != 41 && type != 42 && type != 50 && type != 60) continue;
+    if (type != 41 && type != 42 && type != 50 && type != 60 && type != 421) continue;
     const int dir = n / 2;
     const long long cnt = (long long)((dir == 0 ? g.jm : g.im) + 1) * ((dir == 2 ? g.jm : g.km) + 1);
     prof_begin(c, KC_HALO);
@@ -1379,10 +1389,12 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
     bct[n] = params->bctype[n];
     if (params->channel && (n == 2 || n == 3) && (bct[n] == 0 || bct[n] == 1)) bct[n] = 41;
     if (bct[n] == 0 || bct[n] == 1) continue;
-    if (bct[n] != 41 && bct[n] != 42 && bct[n] != 50 && bct[n] != 60)
-      return fail(nullptr, ASTR_ERR_UNSUPPORTED, "bctype: 41, 42, 50 and 60 are built (0/1: none)");
+    if (bct[n] != 41 && bct[n] != 42 && bct[n] != 50 && bct[n] != 60 && bct[n] != 421)
+      return fail(nullptr, ASTR_ERR_UNSUPPORTED, "bctype: 41, 42, 421, 50 and 60 are built (0/1: none)");
     if (bct[n] == 42 && n >= 4)
       return fail(nullptr, ASTR_ERR_UNSUPPORTED, "bctype 42 exists for the x and y faces only");
+    if (bct[n] == 421 && n / 2 != 1)
+      return fail(nullptr, ASTR_ERR_UNSUPPORTED, "bctype 421 exists for the y faces only");
     if (n / 2 >= ndims || npdc[n / 2] != 4)
       return fail(nullptr, ASTR_ERR_ARG, "a boundary routine needs npdc = 4 in its direction");
     const double tw = params->twall_face[n] != 0.0 ? params->twall_face[n] : params->twall;

@@ -1337,6 +1337,17 @@ void face_node(orc_ctx& c, int n, int type, double tw, int i, int j, int k) {
     T[p] = te;
     R[p] = P[p] / T[p] * c.const2;
     fvar2q_prs_node(c, p);
+  } else if (type == 421) {  // slipadibwall, src/bc.F90:7231-7430 (y faces)
+    const double pe = NUM1D3 * (4.0 * P[p1] - P[p2]);
+    const double te = NUM1D3 * (4.0 * T[p1] - T[p2]);
+    const double ue = NUM1D3 * (4.0 * V[p1] - V[p2]);
+    // ymin: v = 0; ymax: v extrapolated too (as the reference writes it)
+    const double ve = n == 3 ? NUM1D3 * (4.0 * V[p1 + nh] - V[p2 + nh]) : 0.0;
+    V[p] = ue; V[p + nh] = ve; V[p + 2 * nh] = 0.0;
+    T[p] = te;
+    P[p] = pe;
+    R[p] = P[p] / T[p] * c.const2;
+    fvar2q_prs_node(c, p);
   } else if (type == 50) {  // zeroextrap, src/bc.F90:2356-2652
     const double ue = ex2(V[p1], V[p2]), ve = ex2(V[p1 + nh], V[p2 + nh]);
     const double we = ex2(V[p1 + 2 * nh], V[p2 + 2 * nh]);
@@ -1403,9 +1414,9 @@ void face_node(orc_ctx& c, int n, int type, double tw, int i, int j, int k) {
 void orc_boucon(orc_ctx* c) {
   for (int n = 0; n < 2 * c->ndims; ++n) {
     const int type = face_bctype(*c, n);
-    if (type != 41 && type != 42 && type != 50 && type != 60) continue;
+    if (type != 41 && type != 42 && type != 50 && type != 60 && type != 421) continue;
     const int d = n / 2;
-    if (c->npdc(d) != 4) continue;
+    if (c->npdc(d) != 4 || (type == 421 && d != 1)) continue;
     const double tw = face_twall(*c, n);
     const int a1 = d == 0 ? c->jm : c->im, b1 = d == 2 ? c->jm : c->km;
     for (int b = 0; b <= b1; ++b)

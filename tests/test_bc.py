@@ -1,6 +1,7 @@
 """Boundary routines of boucon (src/bc.F90:327-409) in the oracle, on CPU:
 the face values each routine sets (41 isothermal no-slip, 42 adiabatic
-no-slip, 50 zero-gradient extrapolation, 60 symmetry), and a closed box
+no-slip, 421 adiabatic slip wall, 50 zero-gradient extrapolation, 60
+symmetry), and a closed box
 stepping stably with walls on every face."""
 import numpy as np
 import pytest
@@ -77,6 +78,31 @@ def test_face_values():
                                    atol=1e-15)
         e = _face(prs, n) * 2.5 + 0.5 * _face(rho, n) * (_face(vel, n) ** 2).sum(axis=-1)
         np.testing.assert_allclose(_face(q[..., 4], n), e, rtol=1e-12)
+
+
+def test_slip_adiabatic_wall_face_values():
+    """421 (slipadibwall, src/bc.F90:7231-7430) on both y faces: p, T and u
+    extrapolated, w = 0; v = 0 on ymin and extrapolated on ymax, as the
+    reference writes the two faces; rho from p and T."""
+    o = bc_oracle((24, 20, 16), (3, 4, 3), (0, 0, 421, 421, 0, 0))
+    before = {k: o.field(k).copy() for k in ("vel", "prs", "tmp")}
+    o.call("boucon")
+    vel, prs, tmp, rho, q = (o.field(k) for k in ("vel", "prs", "tmp", "rho", "q"))
+    ex = lambda a, n: (4.0 * _face(a, n, 1) - _face(a, n, 2)) / 3.0
+    const2 = cases.refcal(MACH, 400.0)["const2"]
+    for n in (2, 3):
+        np.testing.assert_allclose(_face(prs, n), ex(before["prs"], n), rtol=1e-14)
+        np.testing.assert_allclose(_face(tmp, n), ex(before["tmp"], n), rtol=1e-14)
+        np.testing.assert_allclose(_face(vel[..., 0], n), ex(before["vel"][..., 0], n), rtol=1e-13,
+                                   atol=1e-14)
+        assert np.all(_face(vel[..., 2], n) == 0.0)
+        np.testing.assert_allclose(_face(rho, n), _face(prs, n) / _face(tmp, n) * const2,
+                                   rtol=1e-14)
+        e = _face(prs, n) * 2.5 + 0.5 * _face(rho, n) * (_face(vel, n) ** 2).sum(axis=-1)
+        np.testing.assert_allclose(_face(q[..., 4], n), e, rtol=1e-12)
+    assert np.all(_face(vel[..., 1], 2) == 0.0)
+    np.testing.assert_allclose(_face(vel[..., 1], 3), ex(before["vel"][..., 1], 3), rtol=1e-13,
+                               atol=1e-14)
 
 
 def test_closed_box_steps():

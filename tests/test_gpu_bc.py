@@ -1,6 +1,7 @@
 """Boundary routines of boucon on the GPU against the oracle (FP64, 1e-12):
 a 3-D box with a different routine on each face (isothermal and adiabatic
-no-slip, symmetry, zero-gradient extrapolation), the viscous terms and the
+no-slip, symmetry, zero-gradient extrapolation), adiabatic slip walls on the
+y faces, the viscous terms and the
 filter; a skewed curvilinear box where the symmetry faces project on the
 metric normal; and the FP32-storage form against FP64."""
 import numpy as np
@@ -47,6 +48,19 @@ def _mixed_box():
 
 def test_mixed_faces_match_oracle(gpu_lib):
     o = _mixed_box()
+    g = _gpu_from(o)
+    o.rk3_steps(4)
+    g.time_integration_rk(4)
+    s = g.download_state()
+    g.close()
+    _cmp(o, s)
+
+
+def test_slip_adiabatic_walls_match_oracle(gpu_lib):
+    """421 on both y faces (ymax keeps the extrapolated v), isothermal and
+    adiabatic no-slip on the x faces, z periodic."""
+    o = bc_oracle((24, 20, 16), (4, 4, 3), (41, 42, 421, 421, 0, 0), twall6=(1.2, 0, 0, 0, 0, 0),
+                  deltat=2e-3, lfilter=True)
     g = _gpu_from(o)
     o.rk3_steps(4)
     g.time_integration_rk(4)
