@@ -157,6 +157,7 @@ __global__ void k_rkupdate(Geo g, DevT<T> d, Phys ph, int q2f) {
 //      q with pressure;
 //   42 noslip_adibatic (6728-7036, x and y faces): p and T extrapolated;
 //   421 slipadibwall (7231-7430, y faces): p, T and u extrapolated;
+//   21 outflow (3404-3617, xmax and ymax faces);
 //   50 zeroextrap (2356-2652): x faces extrapolate T, the others rho; q with
 //      temperature on ymax only;
 //   60 symmetry (2664-2996): x faces and zmax remove the velocity along the
@@ -170,7 +171,7 @@ __device__ __forceinline__ double bc_ex2(double v1, double v2) {
 
 template <typename T>
 __global__ void k_face_bc(Geo g, DevT<T> d, Phys ph, int n, int type, double tw, double const1,
-                          double const6) {
+                          double const6, double pinf, double adt, double mach) {
   const int dir = n / 2, side = n % 2;
   const int na = (dir == 0 ? g.jm : g.im) + 1;
   const int nb = (dir == 2 ? g.jm : g.km) + 1;
@@ -213,6 +214,32 @@ __global__ void k_face_bc(Geo g, DevT<T> d, Phys ph, int n, int type, double tw,
     v = n == 3 ? (1.0 / 3.0) * (4.0 * prim(p1, 2) - prim(p2, 2)) : 0.0;
     w = 0.0;
     ro = pe / te * c2;
+  } else if (type == 21 && n == 1) {
+    // outflow xmax (3427-3532): the i-1 node copied (its supersonic branch
+    // is taken unconditionally); q in temperature form
+    u = prim(p1, 1);
+    v = prim(p1, 2);
+    w = prim(p1, 3);
+    pe = prim(p1, 4);
+    te = prim(p1, 5);
+    ro = pe / te * c2;
+    tform = true;
+  } else if (type == 21) {
+    // outflow ymax (3534-3615): extrapolated where the face is supersonic,
+    // else p relaxed towards pinf (adt = 0.25 deltat); T from p and rho
+    const double css = sqrt(prim(p, 5)) / mach;
+    const double vf = prim(p, 2);
+    u = bc_ex2(prim(p1, 1), prim(p2, 1));
+    v = bc_ex2(prim(p1, 2), prim(p2, 2));
+    w = bc_ex2(prim(p1, 3), prim(p2, 3));
+    if (vf >= css) {
+      pe = bc_ex2(prim(p1, 4), prim(p2, 4));
+      ro = bc_ex2(prim(p1, 0), prim(p2, 0));
+    } else {
+      pe = (prim(p, 4) + adt * pinf + prim(p, 0) * css * (v - vf)) / (1.0 + adt);
+      ro = pe / bc_ex2(prim(p1, 5), prim(p2, 5)) * c2;
+    }
+    te = pe / ro * c2;
   } else {
     u = bc_ex2(prim(p1, 1), prim(p2, 1));
     v = bc_ex2(prim(p1, 2), prim(p2, 2));
@@ -1120,14 +1147,16 @@ int run_boucon(astr_ctx* c) {
   const double gamma = 1.4, mach = c->pm.mach;
   const double const1 = 1.0 / (gamma * (gamma - 1.0) * (mach * mach));
   const double const6 = 1.0 / (gamma - 1.0);
+  // pinf = roinf tinf / const2 (src/solver.F90:120); outflow's alpha = 0.25
+  const double pinf = 1.0 / c->ph.const2, adt = 0.25 * c->pm.deltat;
   for (int n = 0; n < 2 * g.ndims; ++n) {
     const int type = c->bct[n];
-    if (type != 41 && type != 42 && type != 50 && type != 60 && type != 421) continue;
+    if (type != 41 && type != 42 && type != 50 && type != 60 && type != 421 && type != 21) continue;
     const int dir = n / 2;
     const long long cnt = (long long)((dir == 0 ? g.jm : g.im) + 1) * ((dir == 2 ? g.jm : g.km) + 1);
     prof_begin(c, KC_HALO);
     k_face_bc<T><<<point_grid(cnt), 256, 0, c->st>>>(g, dev<T>(c), c->ph, n, type, c->btw[n], const1,
-                                                     const6);
+                                                     const6, pinf, adt, mach);
     prof_end(c);
     RC(after_launch(c, "k_face_bc"));
   }
@@ -1389,8 +1418,11 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
     bct[n] = params->bctype[n];
     if (params->channel && (n == 2 || n == 3) && (bct[n] == 0 || bct[n] == 1)) bct[n] = 41;
     if (bct[n] == 0 || bct[n] == 1) continue;
-    if (bct[n] != 41 && bct[n] != 42 && bct[n] != 50 && bct[n] != 60 && bct[n] != 421)
-      return fail(nullptr, ASTR_ERR_UNSUPPORTED, "bctype: 41, 42, 421, 50 and 60 are built (0/1: none)");
+    if (bct[n] != 41 && bct[n] != 42 && bct[n] != 50 && bct[n] != 60 && bct[n] != 421 && bct[n] != 21)
+      return fail(nullptr, ASTR_ERR_UNSUPPORTED,
+                  "bctype: 21, 41, 42, 421, 50 and 60 are built (0/1: none)");
+    if (bct[n] == 21 && n != 1 && n != 3)
+      return fail(nullptr, ASTR_ERR_UNSUPPORTED, "bctype 21 exists for the xmax and ymax faces only");
     if (bct[n] == 42 && n >= 4)
       return fail(nullptr, ASTR_ERR_UNSUPPORTED, "bctype 42 exists for the x and y faces only");
     if (bct[n] == 421 && n / 2 != 1)

@@ -1348,6 +1348,32 @@ void face_node(orc_ctx& c, int n, int type, double tw, int i, int j, int k) {
     P[p] = pe;
     R[p] = P[p] / T[p] * c.const2;
     fvar2q_prs_node(c, p);
+  } else if (type == 21 && n == 1) {  // outflow xmax, src/bc.F90:3427-3532
+    // the first-order copy of the i-1 node (the supersonic branch is taken
+    // unconditionally); rho from p and T, q in temperature form
+    V[p] = V[p1]; V[p + nh] = V[p1 + nh]; V[p + 2 * nh] = V[p1 + 2 * nh];
+    P[p] = P[p1];
+    T[p] = T[p1];
+    R[p] = P[p] / T[p] * c.const2;
+    fvar2q_tmp_node(c, p);
+  } else if (type == 21) {  // outflow ymax, src/bc.F90:3534-3615
+    const double css = std::sqrt(T[p]) / c.cfg.mach;  // sos of the face node
+    const double ub = V[p + nh];
+    const double ue = ex2(V[p1], V[p2]), ve = ex2(V[p1 + nh], V[p2 + nh]);
+    const double we = ex2(V[p1 + 2 * nh], V[p2 + 2 * nh]);
+    const double pe = ex2(P[p1], P[p2]), te = ex2(T[p1], T[p2]), roe = ex2(R[p1], R[p2]);
+    if (ub >= css) {  // supersonic: everything extrapolated
+      P[p] = pe;
+      R[p] = roe;
+    } else {  // subsonic: relaxation of p towards pinf (alpha = 0.25)
+      const double adt = 0.25 * c.cfg.deltat;
+      P[p] = (P[p] + adt * c.pinf + R[p] * css * (ve - V[p + nh])) / (1.0 + adt);
+      T[p] = te;
+      R[p] = P[p] / T[p] * c.const2;
+    }
+    V[p] = ue; V[p + nh] = ve; V[p + 2 * nh] = we;
+    T[p] = P[p] / R[p] * c.const2;  // nondimensional: T from p and rho
+    fvar2q_prs_node(c, p);
   } else if (type == 50) {  // zeroextrap, src/bc.F90:2356-2652
     const double ue = ex2(V[p1], V[p2]), ve = ex2(V[p1 + nh], V[p2 + nh]);
     const double we = ex2(V[p1 + 2 * nh], V[p2 + 2 * nh]);
@@ -1414,9 +1440,9 @@ void face_node(orc_ctx& c, int n, int type, double tw, int i, int j, int k) {
 void orc_boucon(orc_ctx* c) {
   for (int n = 0; n < 2 * c->ndims; ++n) {
     const int type = face_bctype(*c, n);
-    if (type != 41 && type != 42 && type != 50 && type != 60 && type != 421) continue;
+    if (type != 41 && type != 42 && type != 50 && type != 60 && type != 421 && type != 21) continue;
     const int d = n / 2;
-    if (c->npdc(d) != 4 || (type == 421 && d != 1)) continue;
+    if (c->npdc(d) != 4 || (type == 421 && d != 1) || (type == 21 && n != 1 && n != 3)) continue;
     const double tw = face_twall(*c, n);
     const int a1 = d == 0 ? c->jm : c->im, b1 = d == 2 ? c->jm : c->km;
     for (int b = 0; b <= b1; ++b)

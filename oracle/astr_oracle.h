@@ -56,8 +56,8 @@ typedef struct {
   double shkcrt;           /* shock-sensor threshold */
   /* boundary routine of each face (xmin, xmax, ymin, ymax, zmin, zmax),
    * bctype of src/bc.F90:327-409: 41 isothermal no-slip, 42 adiabatic
-   * no-slip, 421 adiabatic slip (y faces), 50 zero-gradient extrapolation,
-   * 60 symmetry; 0 or 1 none.
+   * no-slip, 421 adiabatic slip (y faces), 21 outflow (xmax, ymax), 50
+   * zero-gradient extrapolation, 60 symmetry; 0 or 1 none.
    * A channel (channel = 1) with 0 on the y faces has 41 there. */
   int bctype[6];
   double twall6[6];        /* wall temperature of each 41 face (0: twall) */

@@ -1,7 +1,7 @@
 """Boundary routines of boucon (src/bc.F90:327-409) in the oracle, on CPU:
 the face values each routine sets (41 isothermal no-slip, 42 adiabatic
-no-slip, 421 adiabatic slip wall, 50 zero-gradient extrapolation, 60
-symmetry), and a closed box
+no-slip, 421 adiabatic slip wall, 21 outflow, 50 zero-gradient
+extrapolation, 60 symmetry), and a closed box
 stepping stably with walls on every face."""
 import numpy as np
 import pytest
@@ -12,10 +12,10 @@ H = 5
 MACH = 0.3
 
 
-def box_state(dims, lengths=(2.0 * np.pi, 2.0 * np.pi, 2.0 * np.pi), mach=MACH):
+def box_state(dims, lengths=(2.0 * np.pi, 2.0 * np.pi, 2.0 * np.pi), mach=MACH, vbulk=0.0):
     """TGV fields at Mach 0.3 on a box whose nodes include both ends of every
     direction (non-periodic layout), shifted by a quarter period so that the
-    velocity does not vanish on the faces."""
+    velocity does not vanish on the faces; vbulk is added to v."""
     im, jm, km = dims
     x, y, z = cases.gridcube(im, jm, km, *lengths)
     X = x.reshape(-1, 1, 1) + 0.7
@@ -25,7 +25,7 @@ def box_state(dims, lengths=(2.0 * np.pi, 2.0 * np.pi, 2.0 * np.pi), mach=MACH):
     shape = (im + 1, jm + 1, km + 1)
     rho = (1.0 + 0.1 * np.sin(X) * np.cos(Y)) * np.ones(shape)
     u = np.sin(X) * np.cos(Y) * np.cos(Z) * np.ones(shape)
-    v = -np.cos(X) * np.sin(Y) * np.cos(Z) * np.ones(shape)
+    v = vbulk - np.cos(X) * np.sin(Y) * np.cos(Z) * np.ones(shape)
     w = (0.2 * np.sin(Z) * np.cos(X) if km > 0 else 0.0) * np.ones(shape)
     p = c["pinf"] + 1.0 / 16.0 * (np.cos(2 * X) + np.cos(2 * Y)) * (np.cos(2 * Z) + 2.0)
     T = p / rho * c["const2"]
@@ -33,9 +33,9 @@ def box_state(dims, lengths=(2.0 * np.pi, 2.0 * np.pi, 2.0 * np.pi), mach=MACH):
     return cases._pack_state(im, jm, km, rho, u, v, w, p, T, q5), (x, y, z)
 
 
-def bc_oracle(dims, npdc, bctype, twall6=(0.0,) * 6, **kw):
+def bc_oracle(dims, npdc, bctype, twall6=(0.0,) * 6, vbulk=0.0, **kw):
     from oracle import pyoracle as po
-    st, grid = box_state(dims)
+    st, grid = box_state(dims, vbulk=vbulk)
     kw.setdefault("mach", MACH)
     kw.setdefault("reynolds", 400.0)
     return po.from_state(st, dims, grid=grid, npdc=npdc, bctype=bctype, twall6=twall6, **kw)
@@ -103,6 +103,44 @@ def test_slip_adiabatic_wall_face_values():
     assert np.all(_face(vel[..., 1], 2) == 0.0)
     np.testing.assert_allclose(_face(vel[..., 1], 3), ex(before["vel"][..., 1], 3), rtol=1e-13,
                                atol=1e-14)
+
+
+def test_outflow_face_values():
+    """21 (outflow, src/bc.F90:3404-3617) on xmax and ymax.  xmax copies the
+    i-1 node; ymax extrapolates where the face is supersonic (v >= sqrt(T)/M)
+    and else relaxes p towards pinf, taking T extrapolated for rho and then
+    T from p and rho.  A bulk v of 3.5 at Mach 0.3 puts both branches on the
+    ymax face."""
+    o = bc_oracle((24, 20, 16), (4, 4, 3), (0, 21, 0, 21, 0, 0), vbulk=3.5, deltat=2e-3)
+    before = {k: o.field(k).copy() for k in ("vel", "prs", "tmp", "rho")}
+    o.call("boucon")
+    vel, prs, tmp, rho, q = (o.field(k) for k in ("vel", "prs", "tmp", "rho", "q"))
+    c = cases.refcal(MACH, 400.0)
+    const2, pinf = c["const2"], c["pinf"]
+    # xmax: the i-1 node, all nodes of the face (edges included: ymax comes later)
+    for f in ("vel", "prs", "tmp"):
+        assert np.array_equal(_face(o.field(f), 1), _face(before[f], 1, 1))
+    np.testing.assert_allclose(_face(rho, 1), _face(prs, 1) / _face(tmp, 1) * const2, rtol=1e-15)
+    np.testing.assert_allclose(_face(q[..., 4], 1),
+                               _face(rho, 1) * (_face(tmp, 1) * c["const1"] +
+                                                0.5 * (_face(vel, 1) ** 2).sum(axis=-1)), rtol=1e-14)
+    # ymax
+    ex = lambda a: (4.0 * _face(a, 3, 1) - _face(a, 3, 2)) / 3.0
+    vf, tf, pf, rf = (_face(before[k], 3) for k in ("vel", "tmp", "prs", "rho"))
+    vf = vf[..., 1]
+    css = np.sqrt(tf) / MACH
+    sup = vf >= css
+    assert 0.1 < sup.mean() < 0.9, sup.mean()
+    np.testing.assert_allclose(_face(vel, 3), ex(before["vel"]), rtol=1e-13, atol=1e-14)
+    adt = 0.25 * 2e-3
+    p_sub = (pf + adt * pinf + rf * css * (ex(before["vel"])[..., 1] - vf)) / (1.0 + adt)
+    p_exp = np.where(sup, ex(before["prs"]), p_sub)
+    r_exp = np.where(sup, ex(before["rho"]), p_sub / ex(before["tmp"]) * const2)
+    np.testing.assert_allclose(_face(prs, 3), p_exp, rtol=1e-14)
+    np.testing.assert_allclose(_face(rho, 3), r_exp, rtol=1e-14)
+    np.testing.assert_allclose(_face(tmp, 3), p_exp / r_exp * const2, rtol=1e-14)
+    e = _face(prs, 3) * 2.5 + 0.5 * _face(rho, 3) * (_face(vel, 3) ** 2).sum(axis=-1)
+    np.testing.assert_allclose(_face(q[..., 4], 3), e, rtol=1e-12)
 
 
 def test_closed_box_steps():

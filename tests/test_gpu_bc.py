@@ -1,7 +1,7 @@
 """Boundary routines of boucon on the GPU against the oracle (FP64, 1e-12):
 a 3-D box with a different routine on each face (isothermal and adiabatic
 no-slip, symmetry, zero-gradient extrapolation), adiabatic slip walls on the
-y faces, the viscous terms and the
+y faces, outflow on xmax and ymax, the viscous terms and the
 filter; a skewed curvilinear box where the symmetry faces project on the
 metric normal; and the FP32-storage form against FP64."""
 import numpy as np
@@ -64,6 +64,20 @@ def test_slip_adiabatic_walls_match_oracle(gpu_lib):
     g = _gpu_from(o)
     o.rk3_steps(4)
     g.time_integration_rk(4)
+    s = g.download_state()
+    g.close()
+    _cmp(o, s)
+
+
+def test_outflow_faces_match_oracle(gpu_lib):
+    """21 on xmax (the i-1 copy) and ymax (supersonic extrapolation or the
+    subsonic pressure relaxation: a bulk v of 3.5 at Mach 0.3 puts both on
+    the face), walls on xmin and ymin, z periodic."""
+    o = bc_oracle((24, 20, 16), (4, 4, 3), (41, 21, 42, 21, 0, 0), twall6=(1.2, 0, 0, 0, 0, 0),
+                  vbulk=3.5, deltat=2e-3, lfilter=True)
+    g = _gpu_from(o)
+    o.rk3_steps(3)
+    g.time_integration_rk(3)
     s = g.download_state()
     g.close()
     _cmp(o, s)
