@@ -158,6 +158,7 @@ __global__ void k_rkupdate(Geo g, DevT<T> d, Phys ph, int q2f) {
 //   42 noslip_adibatic (6728-7036, x and y faces): p and T extrapolated;
 //   421 slipadibwall (7231-7430, y faces): p, T and u extrapolated;
 //   21 outflow (3404-3617, xmax and ymax faces);
+//   51 farfield (3008-3392, y and z faces);
 //   50 zeroextrap (2356-2652): x faces extrapolate T, the others rho; q with
 //      temperature on ymax only;
 //   60 symmetry (2664-2996): x faces and zmax remove the velocity along the
@@ -239,6 +240,50 @@ __global__ void k_face_bc(Geo g, DevT<T> d, Phys ph, int n, int type, double tw,
       pe = (prim(p, 4) + adt * pinf + prim(p, 0) * css * (v - vf)) / (1.0 + adt);
       ro = pe / bc_ex2(prim(p1, 5), prim(p2, 5)) * c2;
     }
+    te = pe / ro * c2;
+  } else if (type == 51 && n == 3) {
+    // farfield ymax (3106-3233): its characteristic treatment is commented
+    // out, so everything is extrapolated; q in temperature form
+    u = bc_ex2(prim(p1, 1), prim(p2, 1));
+    v = bc_ex2(prim(p1, 2), prim(p2, 2));
+    w = bc_ex2(prim(p1, 3), prim(p2, 3));
+    pe = bc_ex2(prim(p1, 4), prim(p2, 4));
+    ro = bc_ex2(prim(p1, 0), prim(p2, 0));
+    te = pe / ro * c2;
+    tform = true;
+  } else if (type == 51) {
+    // farfield ymin (3024-3104), zmin (3235-3312), zmax (3314-3389):
+    // free-stream inflow (Riemann invariants, isentropic rho) where the
+    // normal velocity points inwards, else outflow at pinf; free stream
+    // uinf = roinf = 1, vinf = winf = 0
+    const int m = dir == 1 ? 2 : 3;
+    const double css = sqrt(prim(p, 5)) / mach;
+    const double ue = bc_ex2(prim(p1, 1), prim(p2, 1));
+    const double ve = bc_ex2(prim(p1, 2), prim(p2, 2));
+    const double we = bc_ex2(prim(p1, 3), prim(p2, 3));
+    const double pex = bc_ex2(prim(p1, 4), prim(p2, 4));
+    const double roe = bc_ex2(prim(p1, 0), prim(p2, 0));
+    const double csse = bc_ex2(sqrt(prim(p1, 5)) / mach, sqrt(prim(p2, 5)) / mach);
+    const double vn_e = dir == 1 ? ve : we;
+    const double sgn = side ? -1.0 : 1.0;
+    const double vnf = prim(p, m), rof = prim(p, 0);
+    double vn;
+    if (side ? vnf <= 0.0 : vnf >= 0.0) {
+      vn = sgn * 0.5 * (pinf - pex) / (rof * css) + 0.5 * (0.0 + vn_e);
+      pe = 0.5 * (pinf + pex) + sgn * 0.5 * rof * css * (0.0 - vn_e);
+      ro = 1.0 * pow(pe / pinf, 1.0 / 1.4);
+      u = 1.0;
+      v = w = 0.0;
+    } else {
+      pe = pinf;
+      ro = roe + (pe - pex) / csse / csse;
+      vn = vn_e - sgn * (pex - pe) / roe / csse;
+      u = ue;
+      v = ve;
+      w = we;
+    }
+    if (dir == 1) v = vn;
+    else w = vn;
     te = pe / ro * c2;
   } else {
     u = bc_ex2(prim(p1, 1), prim(p2, 1));
@@ -1151,7 +1196,9 @@ int run_boucon(astr_ctx* c) {
   const double pinf = 1.0 / c->ph.const2, adt = 0.25 * c->pm.deltat;
   for (int n = 0; n < 2 * g.ndims; ++n) {
     const int type = c->bct[n];
-    if (type != 41 && type != 42 && type != 50 && type != 60 && type != 421 && type != 21) continue;
+    if (type != 41 && type != 42 && type != 50 && type != 60 && type != 421 && type != 21 &&
+        type != 51)
+      continue;
     const int dir = n / 2;
     const long long cnt = (long long)((dir == 0 ? g.jm : g.im) + 1) * ((dir == 2 ? g.jm : g.km) + 1);
     prof_begin(c, KC_HALO);
@@ -1418,9 +1465,12 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
     bct[n] = params->bctype[n];
     if (params->channel && (n == 2 || n == 3) && (bct[n] == 0 || bct[n] == 1)) bct[n] = 41;
     if (bct[n] == 0 || bct[n] == 1) continue;
-    if (bct[n] != 41 && bct[n] != 42 && bct[n] != 50 && bct[n] != 60 && bct[n] != 421 && bct[n] != 21)
+    if (bct[n] != 41 && bct[n] != 42 && bct[n] != 50 && bct[n] != 60 && bct[n] != 421 &&
+        bct[n] != 21 && bct[n] != 51)
       return fail(nullptr, ASTR_ERR_UNSUPPORTED,
-                  "bctype: 21, 41, 42, 421, 50 and 60 are built (0/1: none)");
+                  "bctype: 21, 41, 42, 421, 50, 51 and 60 are built (0/1: none)");
+    if (bct[n] == 51 && n < 2)
+      return fail(nullptr, ASTR_ERR_UNSUPPORTED, "bctype 51 exists for the y and z faces only");
     if (bct[n] == 21 && n != 1 && n != 3)
       return fail(nullptr, ASTR_ERR_UNSUPPORTED, "bctype 21 exists for the xmax and ymax faces only");
     if (bct[n] == 42 && n >= 4)

@@ -85,7 +85,8 @@ typedef struct {
                               (6306-6712), 42 adiabatic no-slip (6728-7036,
                               x and y faces), 421 adiabatic slip wall
                               (7231-7430, y faces), 21 outflow (3404-3617,
-                              xmax and ymax), 50 zero-gradient extrapolation
+                              xmax and ymax), 51 farfield (3008-3392, y and
+                              z faces), 50 zero-gradient extrapolation
                               (2356-2652), 60 symmetry (2664-2996); 0 or 1:
                               none.  A face with a routine needs npdc = 4 in
                               its direction.  A channel has 41 on the y

@@ -1374,6 +1374,49 @@ void face_node(orc_ctx& c, int n, int type, double tw, int i, int j, int k) {
     V[p] = ue; V[p + nh] = ve; V[p + 2 * nh] = we;
     T[p] = P[p] / R[p] * c.const2;  // nondimensional: T from p and rho
     fvar2q_prs_node(c, p);
+  } else if (type == 51 && n == 3) {  // farfield ymax, src/bc.F90:3106-3233
+    // the characteristic treatment there is commented out: all extrapolated,
+    // T from p and rho, q in temperature form
+    const double ue = ex2(V[p1], V[p2]), ve = ex2(V[p1 + nh], V[p2 + nh]);
+    const double we = ex2(V[p1 + 2 * nh], V[p2 + 2 * nh]);
+    P[p] = ex2(P[p1], P[p2]);
+    R[p] = ex2(R[p1], R[p2]);
+    V[p] = ue; V[p + nh] = ve; V[p + 2 * nh] = we;
+    T[p] = P[p] / R[p] * c.const2;
+    fvar2q_tmp_node(c, p);
+  } else if (type == 51) {  // farfield ymin 3024-3104, zmin 3235-3312, zmax 3314-3389
+    // inflow where the normal velocity points into the domain (Riemann
+    // invariants against the free stream, isentropic rho), else outflow at
+    // pinf; the normal component is v on ymin and w on the z faces
+    const long m = (d == 1 ? 1 : 2) * nh;  // offset of the normal velocity
+    const double css = std::sqrt(T[p]) / c.cfg.mach;
+    const double ue = ex2(V[p1], V[p2]), ve = ex2(V[p1 + nh], V[p2 + nh]);
+    const double we = ex2(V[p1 + 2 * nh], V[p2 + 2 * nh]);
+    const double pe = ex2(P[p1], P[p2]), roe = ex2(R[p1], R[p2]);
+    const double csse = ex2(std::sqrt(T[p1]) / c.cfg.mach, std::sqrt(T[p2]) / c.cfg.mach);
+    const double vn_e = d == 1 ? ve : we;
+    const double vinf = 0.0, winf = 0.0;  // refcal, nondimensional (src/solver.F90:114-118)
+    const double vn_inf = d == 1 ? vinf : winf;
+    const double sgn = side ? -1.0 : 1.0;  // zmax faces the other way
+    const bool inflow = side ? V[p + m] <= 0.0 : V[p + m] >= 0.0;
+    if (inflow) {
+      const double vn = sgn * 0.5 * (c.pinf - pe) / (R[p] * css) + 0.5 * (vn_inf + vn_e);
+      const double pb = 0.5 * (c.pinf + pe) + sgn * 0.5 * R[p] * css * (vn_inf - vn_e);
+      V[p] = c.uinf;
+      V[p + nh] = d == 1 ? vn : vinf;
+      V[p + 2 * nh] = d == 1 ? winf : vn;
+      P[p] = pb;
+      R[p] = c.roinf * std::pow(P[p] / c.pinf, 1.0 / GAMMA);
+    } else {
+      P[p] = c.pinf;
+      R[p] = roe + (P[p] - pe) / csse / csse;
+      const double vn = vn_e - sgn * (pe - P[p]) / roe / csse;
+      V[p] = ue;
+      V[p + nh] = d == 1 ? vn : ve;
+      V[p + 2 * nh] = d == 1 ? we : vn;
+    }
+    T[p] = P[p] / R[p] * c.const2;
+    fvar2q_prs_node(c, p);
   } else if (type == 50) {  // zeroextrap, src/bc.F90:2356-2652
     const double ue = ex2(V[p1], V[p2]), ve = ex2(V[p1 + nh], V[p2 + nh]);
     const double we = ex2(V[p1 + 2 * nh], V[p2 + 2 * nh]);
@@ -1440,9 +1483,13 @@ void face_node(orc_ctx& c, int n, int type, double tw, int i, int j, int k) {
 void orc_boucon(orc_ctx* c) {
   for (int n = 0; n < 2 * c->ndims; ++n) {
     const int type = face_bctype(*c, n);
-    if (type != 41 && type != 42 && type != 50 && type != 60 && type != 421 && type != 21) continue;
+    if (type != 41 && type != 42 && type != 50 && type != 60 && type != 421 && type != 21 &&
+        type != 51)
+      continue;
     const int d = n / 2;
-    if (c->npdc(d) != 4 || (type == 421 && d != 1) || (type == 21 && n != 1 && n != 3)) continue;
+    if (c->npdc(d) != 4 || (type == 421 && d != 1) || (type == 21 && n != 1 && n != 3) ||
+        (type == 51 && d == 0))
+      continue;
     const double tw = face_twall(*c, n);
     const int a1 = d == 0 ? c->jm : c->im, b1 = d == 2 ? c->jm : c->km;
     for (int b = 0; b <= b1; ++b)

@@ -58,6 +58,7 @@ def _params(**kw):
     ((4, 3, 3), dict(bctype=(11, 21, 0, 0, 0, 0)), "UNSUPPORTED", "bctype"),
     ((4, 3, 3), dict(bctype=(421, 0, 0, 0, 0, 0)), "UNSUPPORTED", "y faces"),
     ((4, 3, 3), dict(bctype=(21, 0, 0, 0, 0, 0)), "UNSUPPORTED", "xmax and ymax"),
+    ((4, 3, 3), dict(bctype=(0, 51, 0, 0, 0, 0)), "UNSUPPORTED", "y and z faces"),
     ((4, 3, 3), dict(bctype=(41, 0, 0, 0, 0, 0), twall=0.0), "ARG", "wall temperature"),
     ((3, 3, 3), dict(conschm=1, precision=1), "UNSUPPORTED", "FP64"),
     ((3, 3, 3), dict(conschm=7), "ARG", "conschm"),

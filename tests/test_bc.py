@@ -1,7 +1,7 @@
 """Boundary routines of boucon (src/bc.F90:327-409) in the oracle, on CPU:
 the face values each routine sets (41 isothermal no-slip, 42 adiabatic
-no-slip, 421 adiabatic slip wall, 21 outflow, 50 zero-gradient
-extrapolation, 60 symmetry), and a closed box
+no-slip, 421 adiabatic slip wall, 21 outflow, 51 farfield, 50
+zero-gradient extrapolation, 60 symmetry), and a closed box
 stepping stably with walls on every face."""
 import numpy as np
 import pytest
@@ -141,6 +141,48 @@ def test_outflow_face_values():
     np.testing.assert_allclose(_face(tmp, 3), p_exp / r_exp * const2, rtol=1e-14)
     e = _face(prs, 3) * 2.5 + 0.5 * _face(rho, 3) * (_face(vel, 3) ** 2).sum(axis=-1)
     np.testing.assert_allclose(_face(q[..., 4], 3), e, rtol=1e-12)
+
+
+def test_farfield_face_values():
+    """51 (farfield, src/bc.F90:3008-3392) on the y and z faces.  ymax is
+    extrapolated (its characteristic treatment is commented out); ymin, zmin
+    and zmax take the free stream through the Riemann invariants where the
+    normal velocity points into the domain, else pinf with the outgoing
+    invariant.  The TGV box has both signs of v on ymin and of w on the z
+    faces."""
+    o = bc_oracle((24, 20, 16), (4, 4, 4), (0, 0, 51, 51, 51, 51), deltat=2e-3)
+    before = {k: o.field(k).copy() for k in ("vel", "prs", "tmp", "rho")}
+    o.call("boucon")
+    vel, prs, tmp, rho, q = (o.field(k) for k in ("vel", "prs", "tmp", "rho", "q"))
+    c = cases.refcal(MACH, 400.0)
+    const2, pinf = c["const2"], c["pinf"]
+    # ymax: extrapolated, T from p and rho, q with temperature
+    ex = lambda a, n: (4.0 * _face(a, n, 1) - _face(a, n, 2)) / 3.0
+    for f in ("vel", "prs", "rho"):
+        np.testing.assert_allclose(_face(o.field(f), 3), ex(before[f], 3), rtol=1e-13, atol=1e-14)
+    np.testing.assert_allclose(_face(tmp, 3), _face(prs, 3) / _face(rho, 3) * const2, rtol=1e-15)
+    for n, m in ((2, 1), (4, 2), (5, 2)):
+        sgn = -1.0 if n % 2 else 1.0
+        vf = _face(before["vel"], n)[..., m]
+        inflow = sgn * vf >= 0.0
+        assert 0.1 < inflow.mean() < 0.9, (n, inflow.mean())
+        css = np.sqrt(_face(before["tmp"], n)) / MACH
+        rf = _face(before["rho"], n)
+        vne, pe, roe = ex(before["vel"], n)[..., m], ex(before["prs"], n), ex(before["rho"], n)
+        csse = (4.0 * np.sqrt(_face(before["tmp"], n, 1)) / MACH -
+                np.sqrt(_face(before["tmp"], n, 2)) / MACH) / 3.0
+        p_in = 0.5 * (pinf + pe) - sgn * 0.5 * rf * css * vne
+        vn_in = sgn * 0.5 * (pinf - pe) / (rf * css) + 0.5 * vne
+        p_exp = np.where(inflow, p_in, pinf)
+        r_exp = np.where(inflow, (p_in / pinf) ** (1.0 / 1.4), roe + (pinf - pe) / csse ** 2)
+        vn_exp = np.where(inflow, vn_in, vne - sgn * (pe - pinf) / roe / csse)
+        np.testing.assert_allclose(_face(prs, n), p_exp, rtol=1e-14)
+        np.testing.assert_allclose(_face(rho, n), r_exp, rtol=1e-13)
+        np.testing.assert_allclose(_face(vel, n)[..., m], vn_exp, rtol=1e-12, atol=1e-14)
+        assert np.all(_face(vel, n)[..., 0][inflow] == 1.0)
+        np.testing.assert_allclose(_face(tmp, n), p_exp / r_exp * const2, rtol=1e-13)
+        e = _face(prs, n) * 2.5 + 0.5 * _face(rho, n) * (_face(vel, n) ** 2).sum(axis=-1)
+        np.testing.assert_allclose(_face(q[..., 4], n), e, rtol=1e-12)
 
 
 def test_closed_box_steps():

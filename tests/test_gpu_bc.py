@@ -1,7 +1,8 @@
 """Boundary routines of boucon on the GPU against the oracle (FP64, 1e-12):
 a 3-D box with a different routine on each face (isothermal and adiabatic
 no-slip, symmetry, zero-gradient extrapolation), adiabatic slip walls on the
-y faces, outflow on xmax and ymax, the viscous terms and the
+y faces, outflow on xmax and ymax, farfield on the y and z faces, the
+viscous terms and the
 filter; a skewed curvilinear box where the symmetry faces project on the
 metric normal; and the FP32-storage form against FP64."""
 import numpy as np
@@ -75,6 +76,19 @@ def test_outflow_faces_match_oracle(gpu_lib):
     the face), walls on xmin and ymin, z periodic."""
     o = bc_oracle((24, 20, 16), (4, 4, 3), (41, 21, 42, 21, 0, 0), twall6=(1.2, 0, 0, 0, 0, 0),
                   vbulk=3.5, deltat=2e-3, lfilter=True)
+    g = _gpu_from(o)
+    o.rk3_steps(3)
+    g.time_integration_rk(3)
+    s = g.download_state()
+    g.close()
+    _cmp(o, s)
+
+
+def test_farfield_faces_match_oracle(gpu_lib):
+    """51 on the y and z faces (both the inflow and the outflow branch on
+    ymin, zmin and zmax), walls on the x faces."""
+    o = bc_oracle((24, 20, 16), (4, 4, 4), (41, 42, 51, 51, 51, 51), twall6=(1.2, 0, 0, 0, 0, 0),
+                  deltat=2e-3, lfilter=True)
     g = _gpu_from(o)
     o.rk3_steps(3)
     g.time_integration_rk(3)
