@@ -64,7 +64,7 @@ class AstrParams(ctypes.Structure):
                 ("twall", ctypes.c_double), ("conschm", ctypes.c_int),
                 ("lchardecomp", ctypes.c_int), ("bfacmpld", ctypes.c_double),
                 ("shkcrt", ctypes.c_double), ("bctype", ctypes.c_int * 6),
-                ("twall_face", ctypes.c_double * 6)]
+                ("twall_face", ctypes.c_double * 6), ("xslip", ctypes.c_double)]
 
 
 class AstrStatus(ctypes.Structure):

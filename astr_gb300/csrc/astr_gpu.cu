@@ -156,6 +156,7 @@ __global__ void k_rkupdate(Geo g, DevT<T> d, Phys ph, int q2f) {
 //   41 noslip (6306-6712): u = 0, T = T_w, p extrapolated, rho = p/T*const2,
 //      q with pressure;
 //   42 noslip_adibatic (6728-7036, x and y faces): p and T extrapolated;
+//   411 slipisotwall (7038-7229, y faces): slip up to xslip on ymin;
 //   421 slipadibwall (7231-7430, y faces): p, T and u extrapolated;
 //   21 outflow (3404-3617, xmax and ymax faces);
 //   51 farfield (3008-3392, y and z faces);
@@ -172,7 +173,8 @@ __device__ __forceinline__ double bc_ex2(double v1, double v2) {
 
 template <typename T>
 __global__ void k_face_bc(Geo g, DevT<T> d, Phys ph, int n, int type, double tw, double const1,
-                          double const6, double pinf, double adt, double mach) {
+                          double const6, double pinf, double adt, double mach,
+                          const unsigned char* slip) {
   const int dir = n / 2, side = n % 2;
   const int na = (dir == 0 ? g.jm : g.im) + 1;
   const int nb = (dir == 2 ? g.jm : g.km) + 1;
@@ -205,6 +207,20 @@ __global__ void k_face_bc(Geo g, DevT<T> d, Phys ph, int n, int type, double tw,
     pe = (1.0 / 3.0) * (4.0 * prim(p1, 4) - prim(p2, 4));
     te = (1.0 / 3.0) * (4.0 * prim(p1, 5) - prim(p2, 5));
     u = v = w = 0.0;
+    ro = pe / te * c2;
+  } else if (type == 411) {
+    // slipisotwall (7038-7229, y faces): on ymin slip (u and T extrapolated,
+    // v = 0) where x <= xslip, isothermal no-slip beyond (wall blowing 0);
+    // ymax isothermal no-slip; p extrapolated
+    pe = (1.0 / 3.0) * (4.0 * prim(p1, 4) - prim(p2, 4));
+    if (n == 2 && slip[idx]) {
+      u = (1.0 / 3.0) * (4.0 * prim(p1, 1) - prim(p2, 1));
+      te = (1.0 / 3.0) * (4.0 * prim(p1, 5) - prim(p2, 5));
+    } else {
+      u = 0.0;
+      te = tw;
+    }
+    v = w = 0.0;
     ro = pe / te * c2;
   } else if (type == 421) {
     // slipadibwall (7231-7430, y faces): p, T, u extrapolated; v = 0 on
@@ -887,6 +903,7 @@ struct astr_ctx {
   double* chan_part = nullptr;  // 5 per block of k_chan_sums
   int chan_nblk = 0;
   double* ycoord = nullptr;     // y coordinates, halo layout
+  unsigned char* slip_mask = nullptr;  // 411 on ymin: node (i, k) at x <= xslip
   double chan_ly = 0.0;         // ymax - ymin
   long long nstep = 0;          // completed time steps (statcal's nstep)
   bool rkfirst_called = false;  // rkfirst's firstcall flag
@@ -1197,13 +1214,13 @@ int run_boucon(astr_ctx* c) {
   for (int n = 0; n < 2 * g.ndims; ++n) {
     const int type = c->bct[n];
     if (type != 41 && type != 42 && type != 50 && type != 60 && type != 421 && type != 21 &&
-        type != 51)
+        type != 51 && type != 411)
       continue;
     const int dir = n / 2;
     const long long cnt = (long long)((dir == 0 ? g.jm : g.im) + 1) * ((dir == 2 ? g.jm : g.km) + 1);
     prof_begin(c, KC_HALO);
     k_face_bc<T><<<point_grid(cnt), 256, 0, c->st>>>(g, dev<T>(c), c->ph, n, type, c->btw[n], const1,
-                                                     const6, pinf, adt, mach);
+                                                     const6, pinf, adt, mach, c->slip_mask);
     prof_end(c);
     RC(after_launch(c, "k_face_bc"));
   }
@@ -1466,21 +1483,22 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
     if (params->channel && (n == 2 || n == 3) && (bct[n] == 0 || bct[n] == 1)) bct[n] = 41;
     if (bct[n] == 0 || bct[n] == 1) continue;
     if (bct[n] != 41 && bct[n] != 42 && bct[n] != 50 && bct[n] != 60 && bct[n] != 421 &&
-        bct[n] != 21 && bct[n] != 51)
+        bct[n] != 21 && bct[n] != 51 && bct[n] != 411)
       return fail(nullptr, ASTR_ERR_UNSUPPORTED,
-                  "bctype: 21, 41, 42, 421, 50, 51 and 60 are built (0/1: none)");
+                  "bctype: 21, 41, 42, 411, 421, 50, 51 and 60 are built (0/1: none)");
     if (bct[n] == 51 && n < 2)
       return fail(nullptr, ASTR_ERR_UNSUPPORTED, "bctype 51 exists for the y and z faces only");
     if (bct[n] == 21 && n != 1 && n != 3)
       return fail(nullptr, ASTR_ERR_UNSUPPORTED, "bctype 21 exists for the xmax and ymax faces only");
     if (bct[n] == 42 && n >= 4)
       return fail(nullptr, ASTR_ERR_UNSUPPORTED, "bctype 42 exists for the x and y faces only");
-    if (bct[n] == 421 && n / 2 != 1)
-      return fail(nullptr, ASTR_ERR_UNSUPPORTED, "bctype 421 exists for the y faces only");
+    if ((bct[n] == 421 || bct[n] == 411) && n / 2 != 1)
+      return fail(nullptr, ASTR_ERR_UNSUPPORTED, "bctypes 411 and 421 exist for the y faces only");
     if (n / 2 >= ndims || npdc[n / 2] != 4)
       return fail(nullptr, ASTR_ERR_ARG, "a boundary routine needs npdc = 4 in its direction");
     const double tw = params->twall_face[n] != 0.0 ? params->twall_face[n] : params->twall;
-    if (bct[n] == 41 && !(tw > 0.0)) return fail(nullptr, ASTR_ERR_ARG, "bctype 41 needs a wall temperature > 0");
+    if ((bct[n] == 41 || bct[n] == 411) && !(tw > 0.0))
+      return fail(nullptr, ASTR_ERR_ARG, "bctypes 41 and 411 need a wall temperature > 0");
   }
   if (params->conschm != ASTR_CONSCHM_CENTRAL && params->conschm != ASTR_CONSCHM_MP)
     return fail(nullptr, ASTR_ERR_ARG, "conschm must be ASTR_CONSCHM_CENTRAL or ASTR_CONSCHM_MP");
@@ -1624,7 +1642,7 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
   for (int n = 0; n < 6; ++n) {
     c->bct[n] = bct[n];
     c->btw[n] = params->twall_face[n] != 0.0 ? params->twall_face[n] : params->twall;
-    if (bct[n] >= 41) c->has_bc = true;
+    if (bct[n] != 0 && bct[n] != 1) c->has_bc = true;
   }
   if (const char* e = std::getenv("ASTR_SPLIT_LAST")) c->split_last = std::atoi(e) & 3;
   if (c->channel) {
@@ -1634,6 +1652,7 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
     c->chan_part = (double*)alloc(5 * (size_t)c->chan_nblk * 8);
     c->ycoord = (double*)alloc(nh * 8);
   }
+  if (bct[2] == 411) c->slip_mask = (unsigned char*)alloc((size_t)(g.im + 1) * (g.km + 1));
   // schemes: per direction derivative + filter, in both precisions
   std::vector<HostScheme> hs;
   for (int dd = 0; dd < 3; ++dd) {
@@ -1858,15 +1877,28 @@ int astr_gpu_set_metrics(astr_ctx* c, const double* dxi, const double* jacob) {
 
 int astr_gpu_set_grid(astr_ctx* c, const double* x) {
   if (!c || !x) return fail(c, ASTR_ERR_ARG, "null argument");
-  if (!c->channel) return ASTR_OK;
+  if (!c->channel && !c->slip_mask) return ASTR_OK;
   const size_t nh = (size_t)c->g.nh;
-  const double* y = x + nh;  // x(..,2)
-  CK(cudaMemcpyAsync(c->ycoord, y, nh * 8, cudaMemcpyHostToDevice, c->st));
   const long long NI = c->g.NI, NJ = c->g.NJ;
   auto h = [&](int i, int j, int k) {
     return (size_t)((i + HMD) + NI * ((j + HMD) + NJ * (long long)(k + HMD)));
   };
-  c->chan_ly = y[h(0, c->g.jm, 0)] - y[h(0, 0, 0)];
+  std::vector<unsigned char> mask;
+  if (c->slip_mask) {
+    // slipisotwall's test x(i,0,k,1) <= xslip (src/bc.F90:7132), node (i, k)
+    // at i + (im+1) k, the face kernel's thread order on a y face
+    const int im = c->g.im, km = c->g.km;
+    mask.resize((size_t)(im + 1) * (km + 1));
+    for (int k = 0; k <= km; ++k)
+      for (int i = 0; i <= im; ++i)
+        mask[(size_t)i + (size_t)(im + 1) * k] = x[h(i, 0, k)] <= c->pm.xslip ? 1 : 0;
+    CK(cudaMemcpyAsync(c->slip_mask, mask.data(), mask.size(), cudaMemcpyHostToDevice, c->st));
+  }
+  if (c->channel) {
+    const double* y = x + nh;  // x(..,2)
+    CK(cudaMemcpyAsync(c->ycoord, y, nh * 8, cudaMemcpyHostToDevice, c->st));
+    c->chan_ly = y[h(0, c->g.jm, 0)] - y[h(0, 0, 0)];
+  }
   CK(cudaStreamSynchronize(c->st));
   c->grid_set = true;
   return ASTR_OK;
@@ -2071,8 +2103,8 @@ static int ready(astr_ctx* c) {
   if (!c->metrics_set && c->pm.order == ASTR_ORDER_MAIN)
     return fail(c, ASTR_ERR_STATE, "metrics not set (astr_gpu_set_metrics)");
   if (!c->state_set) return fail(c, ASTR_ERR_STATE, "state not uploaded (astr_gpu_upload_state)");
-  if (c->channel && !c->grid_set)
-    return fail(c, ASTR_ERR_STATE, "channel grid not set (astr_gpu_set_grid)");
+  if ((c->channel || c->slip_mask) && !c->grid_set)
+    return fail(c, ASTR_ERR_STATE, "grid not set (astr_gpu_set_grid): a channel or bctype 411");
   return ASTR_OK;
 }
 

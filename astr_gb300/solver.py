@@ -46,7 +46,7 @@ class GpuSolver:
                  beter_halo=1.11, beter_bound=0.98, mach=0.1, reynolds=1600.0, prandtl=0.72,
                  ref_tem=273.15, suth_const=None, deltat=1e-3, ia=None, ja=None, ka=None,
                  channel=False, twall=1.0, conschm="643c", lchardecomp=True, bfacmpld=0.3,
-                 shkcrt=0.01, bctype=(0, 0, 0, 0, 0, 0), twall_face=(0.0,) * 6):
+                 shkcrt=0.01, bctype=(0, 0, 0, 0, 0, 0), twall_face=(0.0,) * 6, xslip=0.0):
         L = capi.load()
         if conschm not in ("643c", "543c"):
             raise ValueError(f"conschm {conschm!r}: 643c (central) or 543c (compact MP)")
@@ -61,7 +61,7 @@ class GpuSolver:
                                       capi.CONSCHM_MP if conschm == "543c" else capi.CONSCHM_CENTRAL,
                                       int(lchardecomp), bfacmpld, shkcrt,
                                       (ctypes.c_int * 6)(*bctype),
-                                      (ctypes.c_double * 6)(*twall_face))
+                                      (ctypes.c_double * 6)(*twall_face), xslip)
         h = ctypes.c_void_p()
         rc = L.astr_gpu_create(ctypes.byref(self.dims), ctypes.byref(self.params), ctypes.byref(h))
         if rc != capi.ASTR_OK:

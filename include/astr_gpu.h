@@ -83,7 +83,8 @@ typedef struct {
                               ymax, zmin, zmax), bctype of boucon
                               (src/bc.F90:327-409): 41 isothermal no-slip
                               (6306-6712), 42 adiabatic no-slip (6728-7036,
-                              x and y faces), 421 adiabatic slip wall
+                              x and y faces), 411 isothermal slip/no-slip
+                              wall (7038-7229, y faces), 421 adiabatic slip wall
                               (7231-7430, y faces), 21 outflow (3404-3617,
                               xmax and ymax), 51 farfield (3008-3392, y and
                               z faces), 50 zero-gradient extrapolation
@@ -91,7 +92,11 @@ typedef struct {
                               none.  A face with a routine needs npdc = 4 in
                               its direction.  A channel has 41 on the y
                               faces unless set otherwise.                    */
-  double twall_face[6];    /* wall temperature of each 41 face (0: twall)   */
+  double twall_face[6];    /* wall temperature of each 41/411 face (0: twall) */
+  double xslip;            /* 411 on ymin: slip where x(i,0,k,1) <= xslip,
+                              isothermal no-slip beyond (the slip-nonslip
+                              point, src/bc.F90:29, 7132); needs the grid
+                              (astr_gpu_set_grid)                           */
 } astr_params;
 
 /* Convective schemes.  CENTRAL is '643c' (convrsdcal6,
@@ -128,7 +133,8 @@ int astr_gpu_set_metrics(astr_ctx* ctx, const double* dxi, const double* jacob);
 
 /* Node coordinates x(-hm:..,1:3) in Fortran layout (gridgeom's x after its
  * halo fill).  A channel context keeps the y coordinates for the bulk
- * integrals of src_chan and massfluxchan; others ignore the call. */
+ * integrals of src_chan and massfluxchan; a context with 411 on ymin keeps
+ * which of that face's nodes lie at x <= xslip; others ignore the call. */
 int astr_gpu_set_grid(astr_ctx* ctx, const double* x);
 
 /* Asynchronous stepping (no counterpart in the reference; used by the
@@ -156,8 +162,9 @@ int astr_gpu_crashcheck(astr_ctx* ctx, long long* ncrash, int* ijk);
  * metrics, as everywhere in this library. */
 int astr_gpu_cflcal(astr_ctx* ctx, double deltat, double* cfl, double* delta3);
 
-/* boucon (src/bc.F90:327-409) for the per-routine drop-in: the noslip
- * isothermal j-walls of a channel context; no-op otherwise. */
+/* boucon (src/bc.F90:327-409) for the per-routine drop-in: the boundary
+ * routine of every face that has one (bctype, the channel's isothermal
+ * j-walls included); no-op when no face has one. */
 int astr_gpu_boucon(astr_ctx* ctx);
 
 /* Channel controller state: out[0] force(1), out[1] mass flux and out[2]

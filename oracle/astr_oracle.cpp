@@ -1337,6 +1337,24 @@ void face_node(orc_ctx& c, int n, int type, double tw, int i, int j, int k) {
     T[p] = te;
     R[p] = P[p] / T[p] * c.const2;
     fvar2q_prs_node(c, p);
+  } else if (type == 411) {  // slipisotwall, src/bc.F90:7038-7229 (y faces)
+    // ymin: slip (u and T extrapolated, v = 0) up to x = xslip, isothermal
+    // no-slip beyond (the wall-blowing velocity is 0 without its input
+    // file); ymax: isothermal no-slip
+    const double pe = NUM1D3 * (4.0 * P[p1] - P[p2]);
+    if (n == 2 && c.x[p] <= c.cfg.xslip) {
+      const double ue = NUM1D3 * (4.0 * V[p1] - V[p2]);
+      const double te = NUM1D3 * (4.0 * T[p1] - T[p2]);
+      V[p] = ue; V[p + nh] = 0.0;
+      T[p] = te;
+    } else {
+      V[p] = 0.0; V[p + nh] = 0.0;
+      T[p] = tw;
+    }
+    V[p + 2 * nh] = 0.0;
+    P[p] = pe;
+    R[p] = P[p] / T[p] * c.const2;
+    fvar2q_prs_node(c, p);
   } else if (type == 421) {  // slipadibwall, src/bc.F90:7231-7430 (y faces)
     const double pe = NUM1D3 * (4.0 * P[p1] - P[p2]);
     const double te = NUM1D3 * (4.0 * T[p1] - T[p2]);
@@ -1484,11 +1502,11 @@ void orc_boucon(orc_ctx* c) {
   for (int n = 0; n < 2 * c->ndims; ++n) {
     const int type = face_bctype(*c, n);
     if (type != 41 && type != 42 && type != 50 && type != 60 && type != 421 && type != 21 &&
-        type != 51)
+        type != 51 && type != 411)
       continue;
     const int d = n / 2;
-    if (c->npdc(d) != 4 || (type == 421 && d != 1) || (type == 21 && n != 1 && n != 3) ||
-        (type == 51 && d == 0))
+    if (c->npdc(d) != 4 || ((type == 421 || type == 411) && d != 1) ||
+        (type == 21 && n != 1 && n != 3) || (type == 51 && d == 0))
       continue;
     const double tw = face_twall(*c, n);
     const int a1 = d == 0 ? c->jm : c->im, b1 = d == 2 ? c->jm : c->km;

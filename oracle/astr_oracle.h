@@ -56,11 +56,14 @@ typedef struct {
   double shkcrt;           /* shock-sensor threshold */
   /* boundary routine of each face (xmin, xmax, ymin, ymax, zmin, zmax),
    * bctype of src/bc.F90:327-409: 41 isothermal no-slip, 42 adiabatic
-   * no-slip, 421 adiabatic slip (y faces), 21 outflow (xmax, ymax), 50
+   * no-slip, 411 isothermal slip/no-slip (y faces), 421 adiabatic slip
+   * (y faces), 21 outflow (xmax, ymax), 51 farfield (y, z faces), 50
    * zero-gradient extrapolation, 60 symmetry; 0 or 1 none.
    * A channel (channel = 1) with 0 on the y faces has 41 there. */
   int bctype[6];
-  double twall6[6];        /* wall temperature of each 41 face (0: twall) */
+  double twall6[6];        /* wall temperature of each 41/411 face (0: twall) */
+  /* 411 on ymin: slip where x(i,0,k,1) <= xslip, no-slip beyond */
+  double xslip;
 } orc_config;
 
 orc_ctx* orc_create(const orc_config* cfg);

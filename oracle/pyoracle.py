@@ -58,6 +58,7 @@ class OrcConfig(ctypes.Structure):
         ("conschm_mp", ctypes.c_int), ("lchardecomp", ctypes.c_int),
         ("bfacmpld", ctypes.c_double), ("shkcrt", ctypes.c_double),
         ("bctype", ctypes.c_int * 6), ("twall6", ctypes.c_double * 6),
+        ("xslip", ctypes.c_double),
     ]
 
 
@@ -126,7 +127,7 @@ class Oracle:
                  mach=0.1, reynolds=1600.0, prandtl=0.72, ref_tem=273.15,
                  suth_const=None, deltat=1e-3, ia=None, ja=None, ka=None, channel=False,
                  twall=1.0, conschm="643c", lchardecomp=True, bfacmpld=0.3, shkcrt=0.01,
-                 bctype=(0, 0, 0, 0, 0, 0), twall6=(0.0,) * 6):
+                 bctype=(0, 0, 0, 0, 0, 0), twall6=(0.0,) * 6, xslip=0.0):
         if suth_const is None:
             suth_const = 110.4 if mode == MODE_MINIAPP else 110.3
         self.cfg = OrcConfig(im, jm, km, im if ia is None else ia, jm if ja is None else ja,
@@ -135,7 +136,8 @@ class Oracle:
                              beter_halo, beter_bound, mach, reynolds, prandtl, ref_tem,
                              suth_const, deltat, twall, int(conschm == "543c"),
                              int(lchardecomp), bfacmpld, shkcrt,
-                             (ctypes.c_int * 6)(*bctype), (ctypes.c_double * 6)(*twall6))
+                             (ctypes.c_int * 6)(*bctype), (ctypes.c_double * 6)(*twall6),
+                             xslip)
         if conschm not in ("643c", "543c"):
             raise ValueError(f"conschm {conschm!r}: 643c (central) or 543c (compact MP)")
         self.L = lib()

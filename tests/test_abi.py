@@ -57,6 +57,8 @@ def _params(**kw):
     ((3, 3, 4), dict(bctype=(0, 0, 0, 0, 42, 0)), "UNSUPPORTED", "x and y faces"),
     ((4, 3, 3), dict(bctype=(11, 21, 0, 0, 0, 0)), "UNSUPPORTED", "bctype"),
     ((4, 3, 3), dict(bctype=(421, 0, 0, 0, 0, 0)), "UNSUPPORTED", "y faces"),
+    ((4, 3, 3), dict(bctype=(0, 411, 0, 0, 0, 0), twall=1.0), "UNSUPPORTED", "y faces"),
+    ((3, 4, 3), dict(bctype=(0, 0, 411, 0, 0, 0), twall=0.0), "ARG", "wall temperature"),
     ((4, 3, 3), dict(bctype=(21, 0, 0, 0, 0, 0)), "UNSUPPORTED", "xmax and ymax"),
     ((4, 3, 3), dict(bctype=(0, 51, 0, 0, 0, 0)), "UNSUPPORTED", "y and z faces"),
     ((4, 3, 3), dict(bctype=(41, 0, 0, 0, 0, 0), twall=0.0), "ARG", "wall temperature"),

@@ -1,6 +1,7 @@
 """Boundary routines of boucon (src/bc.F90:327-409) in the oracle, on CPU:
 the face values each routine sets (41 isothermal no-slip, 42 adiabatic
-no-slip, 421 adiabatic slip wall, 21 outflow, 51 farfield, 50
+no-slip, 411 isothermal slip/no-slip wall, 421 adiabatic slip wall, 21
+outflow, 51 farfield, 50
 zero-gradient extrapolation, 60 symmetry), and a closed box
 stepping stably with walls on every face."""
 import numpy as np
@@ -103,6 +104,31 @@ def test_slip_adiabatic_wall_face_values():
     assert np.all(_face(vel[..., 1], 2) == 0.0)
     np.testing.assert_allclose(_face(vel[..., 1], 3), ex(before["vel"][..., 1], 3), rtol=1e-13,
                                atol=1e-14)
+
+
+def test_slip_isothermal_wall_face_values():
+    """411 (slipisotwall, src/bc.F90:7038-7229) on both y faces: on ymin the
+    nodes at x <= xslip slip (u and T extrapolated, v = w = 0), the others
+    are isothermal no-slip walls; ymax is an isothermal no-slip wall; p
+    extrapolated everywhere, rho from p and T."""
+    o = bc_oracle((24, 20, 16), (3, 4, 3), (0, 0, 411, 411, 0, 0), twall6=(0, 0, 1.1, 0.9, 0, 0),
+                  xslip=3.0)
+    before = {k: o.field(k).copy() for k in ("vel", "prs", "tmp")}
+    o.call("boucon")
+    vel, prs, tmp, rho = (o.field(k) for k in ("vel", "prs", "tmp", "rho"))
+    ex = lambda a, n: (4.0 * _face(a, n, 1) - _face(a, n, 2)) / 3.0
+    const2 = cases.refcal(MACH, 400.0)["const2"]
+    slip = _face(o.field("x")[..., 0], 2) <= 3.0
+    assert 0.2 < slip.mean() < 0.8
+    np.testing.assert_allclose(_face(tmp, 2)[slip], ex(before["tmp"], 2)[slip], rtol=1e-14)
+    np.testing.assert_allclose(_face(vel[..., 0], 2)[slip], ex(before["vel"][..., 0], 2)[slip],
+                               rtol=1e-13, atol=1e-14)
+    assert np.all(_face(tmp, 2)[~slip] == 1.1) and np.all(_face(vel[..., 0], 2)[~slip] == 0.0)
+    assert np.all(_face(vel[..., 1:], 2) == 0.0)
+    assert np.all(_face(vel, 3) == 0.0) and np.all(_face(tmp, 3) == 0.9)
+    for n in (2, 3):
+        np.testing.assert_allclose(_face(prs, n), ex(before["prs"], n), rtol=1e-14)
+        np.testing.assert_allclose(_face(rho, n), _face(prs, n) / _face(tmp, n) * const2, rtol=1e-15)
 
 
 def test_outflow_face_values():

@@ -1,7 +1,7 @@
 """Boundary routines of boucon on the GPU against the oracle (FP64, 1e-12):
 a 3-D box with a different routine on each face (isothermal and adiabatic
-no-slip, symmetry, zero-gradient extrapolation), adiabatic slip walls on the
-y faces, outflow on xmax and ymax, farfield on the y and z faces, the
+no-slip, symmetry, zero-gradient extrapolation), slip walls (isothermal with
+a slip region, adiabatic) on the y faces, outflow on xmax and ymax, farfield on the y and z faces, the
 viscous terms and the
 filter; a skewed curvilinear box where the symmetry faces project on the
 metric normal; and the FP32-storage form against FP64."""
@@ -14,13 +14,13 @@ from test_bc import H, MACH, bc_oracle
 pytestmark = pytest.mark.gpu
 
 
-def _gpu_from(o, precision=capi.FP64):
+def _gpu_from(o, precision=capi.FP64, **kw):
     from astr_gb300.solver import GpuSolver
     c = o.cfg
     g = GpuSolver(o.im, o.jm, o.km, precision=precision, npdc=(c.npdci, c.npdcj, c.npdck),
                   mach=c.mach, reynolds=c.reynolds, deltat=c.deltat, lfilter=bool(c.lfilter),
                   diffterm=bool(c.diffterm), twall=c.twall, bctype=tuple(c.bctype),
-                  twall_face=tuple(c.twall6))
+                  twall_face=tuple(c.twall6), **kw)
     g.set_metrics(o.field("dxi").copy(order="F"), o.field("jacob").copy(order="F"))
     g.upload_state(o.field("q"), o.field("rho"), o.field("vel"), o.field("prs"), o.field("tmp"))
     return g
@@ -70,6 +70,23 @@ def test_slip_adiabatic_walls_match_oracle(gpu_lib):
     _cmp(o, s)
 
 
+def test_slip_isothermal_walls_match_oracle(gpu_lib):
+    """411 on both y faces: ymin slips up to x = xslip (the node mask comes
+    from the grid, astr_gpu_set_grid), isothermal no-slip beyond and on
+    ymax; stepping refuses to start before the grid is set."""
+    o = bc_oracle((24, 20, 16), (4, 4, 3), (41, 42, 411, 411, 0, 0),
+                  twall6=(1.2, 0, 1.1, 0.9, 0, 0), xslip=3.0, deltat=2e-3, lfilter=True)
+    g = _gpu_from(o, xslip=3.0)
+    with pytest.raises(capi.AstrError, match="grid not set"):
+        g.time_integration_rk(1)
+    g.set_grid(o.field("x").copy(order="F"))
+    o.rk3_steps(4)
+    g.time_integration_rk(4)
+    s = g.download_state()
+    g.close()
+    _cmp(o, s)
+
+
 def test_outflow_faces_match_oracle(gpu_lib):
     """21 on xmax (the i-1 copy) and ymax (supersonic extrapolation or the
     subsonic pressure relaxation: a bulk v of 3.5 at Mach 0.3 puts both on
@@ -79,6 +96,19 @@ def test_outflow_faces_match_oracle(gpu_lib):
     g = _gpu_from(o)
     o.rk3_steps(3)
     g.time_integration_rk(3)
+    s = g.download_state()
+    g.close()
+    _cmp(o, s)
+
+
+def test_outflow_only_matches_oracle(gpu_lib):
+    """Outflow faces as the only boundary routines (xmin and ymin without
+    one): boucon still runs."""
+    o = bc_oracle((24, 20, 16), (4, 4, 3), (0, 21, 0, 21, 0, 0), vbulk=3.5, deltat=2e-3,
+                  lfilter=True)
+    g = _gpu_from(o)
+    o.rk3_steps(2)
+    g.time_integration_rk(2)
     s = g.download_state()
     g.close()
     _cmp(o, s)
