@@ -1569,7 +1569,7 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
   }
   if (e != cudaSuccess) {
     std::string m = std::string("cudaStreamCreate: ") + cudaGetErrorString(e);
-    delete c;
+    astr_gpu_destroy(c);  // the streams and events created before the failure
     return fail(nullptr, ASTR_ERR_CUDA, m);
   }
   bool ok = true;
