@@ -297,7 +297,7 @@ def state_error(q, ref):
     return out
 
 
-def form_roofline(kt, f32, pts_int, fp64_peak, hbm_peak):
+def form_roofline(kt, f32, pts_int, fp64_peak, hbm_peak, hbm_source):
     classes = {}
     for k in ("filter", "convgrad", "pointwise", "visc"):
         tms, cnt = kt[k]
@@ -320,7 +320,7 @@ def form_roofline(kt, f32, pts_int, fp64_peak, hbm_peak):
     if f32:
         roof = {"bound": "hbm", "kernel": dom, "achieved": round(dc["gbs"], 1),
                 "peak": hbm_peak, "unit": "GB/s", "frac": round(dc["gbs"] / hbm_peak, 4),
-                "peak_source": "hbm_gbs of measured (MEASURED_PEAKS.json, burst copy)"}
+                "peak_source": hbm_source}
     else:
         roof = {"bound": "fp64", "kernel": dom, "achieved": round(dc["tflops"], 4),
                 "peak": round(fp64_peak, 4), "unit": "TFLOP/s",
@@ -367,7 +367,12 @@ def run_gpu(args, rank, world, dist):
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except Exception:
         pass
-    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    if "hbm_gbs" in peaks:
+        hbm_peak = float(peaks["hbm_gbs"])
+        hbm_source = "hbm_gbs of measured (MEASURED_PEAKS.json, burst copy)"
+    else:
+        hbm_peak = 6800.0
+        hbm_source = "6800 GB/s of fallback (no MEASURED_PEAKS.json on this machine)"
     fp64_peak = ctypes_peak()
 
     forms = {}
@@ -383,7 +388,8 @@ def run_gpu(args, rank, world, dist):
         forms[name] = {
             "value": round(world * pts * 3 * args.steps / (ms / 1e3) / 1e6, 3),
             "ms_per_step": round(ms / args.steps, 3),
-            "roofline": form_roofline(kt, prec == capi.FP32_STORAGE, pts_int, fp64_peak, hbm_peak),
+            "roofline": form_roofline(kt, prec == capi.FP32_STORAGE, pts_int, fp64_peak, hbm_peak,
+                                      hbm_source),
             "footprint_gb": round(capi.load().astr_gpu_footprint(g.dims, g.params) / 1e9, 2),
             "stats_first_step": {"kenergy": float(hist0[0, 0]), "enstrophy": float(hist0[0, 1])},
         }
