@@ -75,3 +75,44 @@ def test_create_checks_without_gpu(gpu_lib, npdc, kw, code, text):
     rc = gpu_lib.astr_gpu_create(ctypes.byref(d), ctypes.byref(p), ctypes.byref(h))
     assert rc == getattr(capi, "ASTR_ERR_" + code), (rc, capi.last_error(None))
     assert text in capi.last_error(None)
+
+
+C_HOST = r"""
+#include "astr_gpu.h"
+#include <stdio.h>
+int main(void) {
+  astr_dims d = {512, 512, 512, 512, 512, 512, 3, 3, 3};
+  astr_params p = {0};
+  astr_dims bad = {4, 4, 4, 4, 4, 4, 3, 3, 3};
+  astr_ctx* c = NULL;
+  char buf[256];
+  int rc;
+  printf("footprint %zu\n", astr_gpu_footprint(&d, &p));
+  p.mach = 0.1; p.reynolds = 1600.0; p.deltat = 1e-3; p.alfa_filter = 0.49;
+  rc = astr_gpu_create(&bad, &p, &c);
+  astr_gpu_last_error(NULL, buf, (int)sizeof buf);
+  printf("create %d %s\n", rc, buf);
+  return c == NULL ? 0 : 1;
+}
+"""
+
+
+def test_plain_c_host(gpu_lib, tmp_path):
+    """The header is strict C99 (a C or Fortran host includes or mirrors
+    it) and a C program links the library and calls it without a GPU."""
+    import shutil
+    import subprocess
+    from astr_gb300 import capi
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not found")
+    src = tmp_path / "host.c"
+    src.write_text(C_HOST)
+    exe = tmp_path / "host"
+    libdir = os.path.dirname(capi.LIB_PATH)
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror",
+                    "-I", os.path.join(ROOT, "include"), str(src), "-L", libdir, "-lastr_gb300",
+                    "-Wl,-rpath," + libdir, "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    lines = out.splitlines()
+    assert 40e9 < int(lines[0].split()[1]) < 80e9
+    assert lines[1].startswith(f"create {capi.ASTR_ERR_ARG} grid too small")
