@@ -327,7 +327,7 @@ def form_roofline(kt, f32, pts_int, fp64_peak, hbm_peak, hbm_source):
                 "frac": round(dc["tflops"] / fp64_peak, 4),
                 "peak_source": "FP64 FMA loop measured live in this run",
                 "hbm_achieved_gbs": round(dc["gbs"], 1),
-                "hbm_frac_of_measured": round(dc["gbs"] / hbm_peak, 4)}
+                "hbm_frac": round(dc["gbs"] / hbm_peak, 4), "hbm_peak_source": hbm_source}
     roof["traffic"] = traffic
     roof["classes"] = {k: {kk: rnd(vv) for kk, vv in v.items()} for k, v in classes.items()}
     return roof
