@@ -47,6 +47,13 @@ class GpuSolver:
                  ref_tem=273.15, suth_const=None, deltat=1e-3, ia=None, ja=None, ka=None,
                  channel=False, twall=1.0, conschm="643c", lchardecomp=True, bfacmpld=0.3,
                  shkcrt=0.01, bctype=(0, 0, 0, 0, 0, 0), twall_face=(0.0,) * 6, xslip=0.0):
+        """The keywords are the fields of ``astr_params`` under the reference's
+        names: npdc = (npdci, npdcj, npdck), 3 periodic, 4 both ends physical;
+        conschm "643c" (central) or "543c" (compact MP, with lchardecomp,
+        bfacmpld, shkcrt); bctype, the routine of each face (xmin, xmax, ymin,
+        ymax, zmin, zmax; 21, 41, 42, 411, 421, 50, 51, 60, 0/1 none) with
+        twall_face (0: twall) for the isothermal faces and xslip for 411,
+        whose slip region needs set_grid; channel for the channel flow."""
         L = capi.load()
         if conschm not in ("643c", "543c"):
             raise ValueError(f"conschm {conschm!r}: 643c (central) or 543c (compact MP)")
