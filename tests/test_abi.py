@@ -116,3 +116,34 @@ def test_plain_c_host(gpu_lib, tmp_path):
     lines = out.splitlines()
     assert 40e9 < int(lines[0].split()[1]) < 80e9
     assert lines[1].startswith(f"create {capi.ASTR_ERR_ARG} grid too small")
+
+
+# Faces on which each routine of boucon exists (src/bc.F90: noslip 6306-6712
+# all faces; noslip_adibatic 6728-7036 x and y; slipisotwall 7038-7229 and
+# slipadibwall 7231-7430 y; outflow 3404-3617 xmax and ymax; farfield
+# 3008-3392 y and z; zeroextrap 2356-2652 and symmetry 2664-2996 all faces).
+FACES = {41: range(6), 42: range(4), 411: (2, 3), 421: (2, 3), 21: (1, 3), 51: range(2, 6),
+         50: range(6), 60: range(6)}
+
+
+@pytest.mark.parametrize("btype", sorted(FACES) + [11, 12, 22, 23, 31, 52])
+def test_routine_face_table(gpu_lib, btype):
+    """create accepts a routine exactly on the faces where the reference
+    has it and refuses the routines that are not built.  Accepted contexts
+    get past validation (ASTR_OK with a GPU, ASTR_ERR_CUDA without one)."""
+    from astr_gb300 import capi
+    for n in range(6):
+        npdc = [3, 3, 3]
+        npdc[n // 2] = 4
+        d = capi.AstrDims(16, 16, 16, 16, 16, 16, *npdc)
+        bct = [0] * 6
+        bct[n] = btype
+        p = _params(bctype=tuple(bct), twall=1.0, xslip=1.0)
+        h = ctypes.c_void_p()
+        rc = gpu_lib.astr_gpu_create(ctypes.byref(d), ctypes.byref(p), ctypes.byref(h))
+        if rc == capi.ASTR_OK:
+            gpu_lib.astr_gpu_destroy(h)
+        accepted = rc in (capi.ASTR_OK, capi.ASTR_ERR_CUDA)
+        assert accepted == (n in FACES.get(btype, ())), (btype, n, rc, capi.last_error(None))
+        if not accepted:
+            assert rc == capi.ASTR_ERR_UNSUPPORTED
