@@ -105,17 +105,25 @@ constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 double* g_scratch_ptr[kMaxDevices] = {nullptr};
 
-// Device address of the scratch array on the current device, looked up
-// once per device (the array's name is a host-side stand-in in host code).
-int scratch_for_current_device(double** out) {
+// Device address of the scratch array in the current context.  The array's
+// name is only a host-side stand-in in host code, so its address is looked
+// up with cudaGetSymbolAddress on every call whose stream is not being
+// captured (the lookup follows the current context, so a cudaDeviceReset or
+// another context on the same device never leaves a stale address behind).
+// While a capture is active the address recorded by the last uncaptured call
+// on this device is used; with none recorded the call fails.
+int scratch_for_current_device(cudaStream_t st, double** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return ASTR_ERR_CUDA;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  const bool capturing = cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone;
   std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_scratch_ptr[dev]) {
+  if (!capturing) {
     void* p = nullptr;
     if (cudaGetSymbolAddress(&p, g_stats_scratch) != cudaSuccess || !p) return ASTR_ERR_CUDA;
     g_scratch_ptr[dev] = static_cast<double*>(p);
   }
+  if (!g_scratch_ptr[dev]) return ASTR_ERR_CUDA;
   *out = g_scratch_ptr[dev];
   return ASTR_OK;
 }
@@ -129,7 +137,9 @@ extern "C" int astr_gpu_stats_noalloc(const double* rho, const double* vel, cons
   Dims g;
   g.im = dims->im; g.jm = dims->jm; g.km = dims->km;
   g.ndims = dims->ka > 0 ? 3 : 2;
-  if (g.im < 1 || g.jm < 1 || g.km < 0) return ASTR_ERR_ARG;
+  // the block sizes astr_gpu_create accepts: im, jm (, km) >= 8, km == 0 in 2-D
+  if (g.im < 8 || g.jm < 8 || (g.ndims == 3 && g.km < 8) || (g.ndims == 2 && g.km != 0))
+    return ASTR_ERR_ARG;
   g.NI = g.im + 2 * kHM + 1;
   g.NJ = g.jm + 2 * kHM + 1;
   g.I = g.im + 1;
@@ -138,14 +148,26 @@ extern "C" int astr_gpu_stats_noalloc(const double* rho, const double* vel, cons
   const long long nblocks = (g.n0 + kPointsPerBlock - 1) / kPointsPerBlock;
   // one slot pair per block plus the result pair must fit the scratch array
   if (nblocks + 1 > ASTR_NOALLOC_STATS_MAX_BLOCKS) return ASTR_ERR_UNSUPPORTED;
-  double* scratch = nullptr;
-  const int rc = scratch_for_current_device(&scratch);
-  if (rc != ASTR_OK) return rc;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  k_stats_partials<<<(unsigned)nblocks, kThreads, 0, st>>>(g, rho, vel, dvel, scratch);
+  double* scratch = nullptr;
+  const int rc = scratch_for_current_device(st, &scratch);
+  if (rc != ASTR_OK) return rc;
+  // cudaLaunchKernel returns each launch's own status, so an error left
+  // pending by the caller's unrelated work is neither reported here nor
+  // cleared
+  {
+    void* args[] = {&g, (void*)&rho, (void*)&vel, (void*)&dvel, &scratch};
+    if (cudaLaunchKernel((const void*)k_stats_partials, dim3((unsigned)nblocks), dim3(kThreads), args,
+                         0, st) != cudaSuccess)
+      return ASTR_ERR_CUDA;
+  }
   double* result = scratch + 2 * nblocks;
-  k_stats_total<<<1, 1024, 0, st>>>(scratch, (int)nblocks, result);
-  if (cudaGetLastError() != cudaSuccess) return ASTR_ERR_CUDA;
+  {
+    int nb = (int)nblocks;
+    void* args[] = {&scratch, &nb, &result};
+    if (cudaLaunchKernel((const void*)k_stats_total, dim3(1), dim3(1024), args, 0, st) != cudaSuccess)
+      return ASTR_ERR_CUDA;
+  }
   double h[2];
   if (cudaMemcpyAsync(h, result, sizeof(h), cudaMemcpyDeviceToHost, st) != cudaSuccess)
     return ASTR_ERR_CUDA;

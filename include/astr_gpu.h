@@ -259,12 +259,16 @@ int astr_gpu_measure_fp64_peak(double* tflops);
  * stream) and waits for it before returning.
  * Scratch: a fixed device array of 2*ASTR_NOALLOC_STATS_MAX_BLOCKS doubles
  * (1 MiB, held by every GPU that loads the library until exit), one pair of
- * partial sums per 4096 interior nodes; blocks with more than
- * 4096 * (ASTR_NOALLOC_STATS_MAX_BLOCKS - 1) = 268,431,360 interior nodes
- * are rejected with ASTR_ERR_UNSUPPORTED.  All calls share that array, so
- * calls whose work overlaps on the GPU race; serialise them.  The first call
- * on a device looks up the array's device address; make it before any
- * stream capture. */
+ * partial sums per 4096 stored nodes; a block whose stored nodes
+ * (im+1)*(jm+1)*(km+1) exceed 4096 * (ASTR_NOALLOC_STATS_MAX_BLOCKS - 1) =
+ * 268,431,360 is rejected with ASTR_ERR_UNSUPPORTED, and dims that
+ * astr_gpu_create would reject (im, jm (, km) < 8; km != 0 in 2-D) with
+ * ASTR_ERR_ARG.  All calls share that array, so calls whose work overlaps on
+ * the GPU race; serialise them.  A call outside a stream capture looks up
+ * the array's device address in the current context; a call made while its
+ * stream is being captured reuses the address found by the last uncaptured
+ * call on that device, so make one call on the device before capturing.
+ * Errors left pending by other work are neither reported nor cleared. */
 #define ASTR_NOALLOC_STATS_MAX_BLOCKS 65536
 int astr_gpu_stats_noalloc(const double* rho, const double* vel, const double* dvel,
                            const astr_dims* dims, double l0, void* stream,

@@ -5,7 +5,8 @@ kinetic-energy / enstrophy history of the 128^3 Taylor-Green vortex written
 by the compact-scheme mini-app (``miniapps/tgv_solver_3d/state.ref_128``,
 columns nstep, time, KE, enstrophy).  This script copies its numbers into
 ``tgv128_state_ref.txt`` so the tests can run where the reference tree is
-absent.  Usage: ``python tests/golden/make_golden.py [/path/to/astr]``.
+absent.  Usage: ``python tests/golden/make_golden.py /path/to/astr`` (the root of
+the ASTR source tree; required).
 """
 import os
 import sys
@@ -28,4 +29,6 @@ def main(root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py /path/to/astr")
+    main(sys.argv[1])
