@@ -16,7 +16,9 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libastr_gb300.so")
 SOURCES = ["astr_gpu.cu", "sweep_x_f64.cu", "sweep_y_f64.cu", "sweep_z_f64.cu",
-           "sweep_x_f32.cu", "sweep_y_f32.cu", "sweep_z_f32.cu", "stats_noalloc.cu", "mp.cu"]
+           "sweep_x_f32.cu", "sweep_y_f32.cu", "sweep_z_f32.cu", "stats_noalloc.cu", "mp.cu",
+           "sweep2_x_f64.cu", "sweep2_y_f64.cu", "sweep2_z_f64.cu", "sweep2_x_f32.cu",
+           "sweep2_y_f32.cu", "sweep2_z_f32.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "--expt-relaxed-constexpr"]

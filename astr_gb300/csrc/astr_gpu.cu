@@ -18,6 +18,7 @@
 // Two precision forms share the kernels: plain FP64 (T = double), and FP32
 // storage (T = float) with the RK3 base and a master copy of q in FP64.
 #include "launch.cuh"
+#include "launch2.cuh"
 #include "mp.cuh"
 #include "../../include/astr_gpu.h"
 
@@ -146,6 +147,21 @@ __global__ void k_rkupdate(Geo g, DevT<T> d, Phys ph, int q2f) {
   const long long p = hidx(g, i, j, k);
   for (int m = 0; m < 5; ++m) rk_update(g, d, ph, p, idx, m, (double)d.qrhs[m * g.n0 + idx]);
   if (q2f) q2fvar_store(g, d, ph, p);
+}
+
+// RK3 base at stage 1 (src/mainloop.F90:427-433): q*J (mini-app: q), in
+// FP64 from the FP64 state or master.
+template <typename T>
+__global__ void k_qsave(Geo g, DevT<T> d, Phys ph) {
+  int i, j, k;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (!point_of(g, idx, i, j, k)) return;
+  const long long p = hidx(g, i, j, k);
+  const double J = d.jac64[p];
+  for (int m = 0; m < 5; ++m) {
+    const double qv = q64(d, p, idx, m, g.nh, g.n0);
+    d.qsave[m * g.n0 + idx] = ph.mini ? qv : qv * J;
+  }
 }
 
 // Boundary routines of boucon (src/bc.F90:327-409) on face n (0-based:
@@ -694,49 +710,58 @@ struct HostScheme {
     u_ac1 = ac1[m];
     u_ac3 = ac3[m];
     const int nk = filter ? 6 : 2;
-    for (int j = 0; j < nk; ++j) u_K[j] = K[(size_t)j * n + m];
+    const size_t ks = K.size() / nk;  // row stride: n, or the padded row count
+    for (int j = 0; j < nk; ++j) u_K[j] = K[(size_t)j * ks + m];
     if (filter)
-      for (int j = 0; j < 5; ++j) u_KD[j] = KD[(size_t)j * n + m];
+      for (int j = 0; j < 5; ++j) u_KD[j] = KD[(size_t)j * ks + m];
   }
-  void finish(int CH, const HostFTab& t) {
-    ac1.assign(n, 0.0); ac2.assign(n, 0.0); ac3.assign(n, 0.0);
+  // np: rows of the stored arrays (n, or 32 x CH for the tiled sweeps,
+  // whose rows past n decouple: a = c = 0, so ac1 = ac3 = 0 there, the
+  // carry weights vanish across them, and their coefficients are zero).
+  void finish(int CH, const HostFTab& t, int np = 0) {
+    if (np < n) np = n;
+    a.resize(np, 0.0);
+    c.resize(np, 0.0);
+    ac1.assign(np, 0.0); ac2.assign(np, 0.0); ac3.assign(np, 0.0);
     ac1[0] = c[0];
-    for (int i = 1; i < n; ++i) {
+    for (int i = 1; i < np; ++i) {
       ac1[i] = c[i] / (1.0 - a[i] * ac1[i - 1]);
       ac2[i] = 1.0 / (1.0 - a[i] * ac1[i - 1]);
       ac3[i] = a[i] / (1.0 - a[i] * ac1[i - 1]);
     }
-    G.assign(n, 0.0); H.assign(n, 0.0);
-    for (int s = 0; s < n; s += CH) {
-      const int e = std::min(s + CH, n) - 1;
+    for (int i = n; i < np; ++i) ac2[i] = 0.0;
+    G.assign(np, 0.0); H.assign(np, 0.0);
+    for (int s = 0; s < np; s += CH) {
+      const int e = std::min(s + CH, np) - 1;
       double p = 1.0;
       for (int r = s; r <= e; ++r) { p *= -ac3[r]; G[r] = p; }
       p = 1.0;
       for (int r = e; r >= s; --r) { p *= -ac1[r]; H[r] = p; }
     }
     // ac2-folded interior coefficients (row 0 is never an interior row)
+    const size_t ks = (size_t)np;
     if (filter) {
-      K.assign(6 * (size_t)n, 0.0);
-      KD.assign(5 * (size_t)n, 0.0);
+      K.assign(6 * ks, 0.0);
+      KD.assign(5 * ks, 0.0);
       for (int r = 0; r < n; ++r) {
         K[r] = 2.0 * t.c10[0] * ac2[r];
-        for (int m = 1; m < 6; ++m) K[m * (size_t)n + r] = t.c10[m] * ac2[r];
+        for (int m = 1; m < 6; ++m) K[m * ks + r] = t.c10[m] * ac2[r];
         // second-difference weights of (B - A) f on interior rows
         KD[r] = (t.c10[1] - a[r]) * ac2[r];
-        for (int m = 2; m < 6; ++m) KD[(m - 1) * (size_t)n + r] = t.c10[m] * ac2[r];
+        for (int m = 2; m < 6; ++m) KD[(m - 1) * ks + r] = t.c10[m] * ac2[r];
       }
     } else {
-      K.assign(2 * (size_t)n, 0.0);
+      K.assign(2 * ks, 0.0);
       for (int r = 0; r < n; ++r) {
         K[r] = H_NUM7D9 * ac2[r];
-        K[n + r] = H_NUM1D36 * ac2[r];
+        K[ks + r] = H_NUM1D36 * ac2[r];
       }
     }
     find_uniform(CH);
   }
 };
 
-HostScheme make_deriv(int ntype, int dim, int CH, const HostFTab& t) {
+HostScheme make_deriv(int ntype, int dim, int CH, const HostFTab& t, int np = 0) {
   HostScheme s;
   int i0 = ntype == 4 ? 0 : -1, im = ntype == 4 ? dim : dim + 1;
   s.first = i0; s.n = im - i0 + 1; s.ntype = ntype; s.dim = dim;
@@ -749,11 +774,11 @@ HostScheme make_deriv(int ntype, int dim, int CH, const HostFTab& t) {
     s.a[s.n - 1] = s.c[s.n - 1] = 2.0;
     s.a[s.n - 2] = s.c[s.n - 2] = 0.25;
   }
-  s.finish(CH, t);
+  s.finish(CH, t, np);
   return s;
 }
 
-HostScheme make_filter(int ntype, int dim, double alfa, int CH, const HostFTab& t) {
+HostScheme make_filter(int ntype, int dim, double alfa, int CH, const HostFTab& t, int np = 0) {
   HostScheme s;
   int i0 = ntype == 4 ? 0 : -3, im = ntype == 4 ? dim : dim + 3;
   double b = ntype == 4 ? 0.98 : 1.11;
@@ -761,7 +786,7 @@ HostScheme make_filter(int ntype, int dim, double alfa, int CH, const HostFTab& 
   s.a.assign(s.n, alfa); s.c.assign(s.n, alfa);
   s.a[0] = s.c[0] = b;
   s.a[s.n - 1] = s.c[s.n - 1] = b;
-  s.finish(CH, t);
+  s.finish(CH, t, np);
   return s;
 }
 
@@ -928,6 +953,14 @@ struct astr_ctx {
   // small grids: the variables of a line spread over blocks (gridDim.z) and
   // the stress, RK3 update and statistics run as point kernels
   bool vsplit = false;
+  // tile-staged sweeps (sweeps2.cuh): main ordering, diagonal metrics;
+  // padded schemes per direction and their uniform-chunk constants
+  bool v2 = false;
+  DScheme<double> v2d64[3], v2f64[3];
+  DScheme<float> v2d32[3], v2f32[3];
+  struct V2U {
+    double a1 = 0, a3 = 0, K[6] = {0, 0, 0, 0, 0, 0}, KD[5] = {0, 0, 0, 0, 0}, gp[33] = {}, hp[33] = {};
+  } v2ud[3], v2uf[3];
   // compact MP convective scheme (conschm 543c): scratch and schemes
   bool mp = false;
   MPDev mpd{};
@@ -1075,9 +1108,67 @@ int launch_face(astr_ctx* c, bool mini) {
 
 dim3 point_grid(long long n) { return dim3((unsigned)((n + 255) / 256)); }
 
+// The tiled sweeps run where the context built them and the metrics are
+// diagonal (the compact MP path keeps the register-window sweeps).
+bool use_v2(const astr_ctx* c) { return c->v2 && !c->gen && !c->mp; }
+
+template <typename T> const DScheme<T>& v2_sd(astr_ctx* c, int dir);
+template <> const DScheme<double>& v2_sd<double>(astr_ctx* c, int dir) { return c->v2d64[dir]; }
+template <> const DScheme<float>& v2_sd<float>(astr_ctx* c, int dir) { return c->v2d32[dir]; }
+template <typename T> const DScheme<T>& v2_sf(astr_ctx* c, int dir);
+template <> const DScheme<double>& v2_sf<double>(astr_ctx* c, int dir) { return c->v2f64[dir]; }
+template <> const DScheme<float>& v2_sf<float>(astr_ctx* c, int dir) { return c->v2f32[dir]; }
+
+template <typename T>
+V2Args<T> v2_args(astr_ctx* c, int dir, bool filter) {
+  V2Args<T> a;
+  a.g = c->g;
+  a.d = dev<T>(c);
+  a.S = filter ? v2_sf<T>(c, dir) : v2_sd<T>(c, dir);
+  a.Tb = ftab<T>(c);
+  a.ph = c->ph;
+  const astr_ctx::V2U& u = filter ? c->v2uf[dir] : c->v2ud[dir];
+  a.a1 = u.a1; a.a3 = u.a3;
+  for (int m = 0; m < 6; ++m) a.K[m] = u.K[m];
+  for (int m = 0; m < 5; ++m) a.KD[m] = u.KD[m];
+  for (int t = 0; t < 33; ++t) { a.gp[t] = u.gp[t]; a.hp[t] = u.hp[t]; }
+  return a;
+}
+
+template <typename T, int DIR>
+int launch2_filter_c(astr_ctx* c) {
+  prof_begin(c, KC_FILTER);
+  const cudaError_t e = astr::launch2_filter<T, DIR>(v2_args<T>(c, DIR, true), c->st, c->CHf[DIR],
+                                                     c->vsplit ? 1 : 0);
+  prof_end(c);
+  return launch_result(c, e, "k2_filter");
+}
+template <typename T, int DIR>
+int launch2_convgrad_c(astr_ctx* c, CGFlags f) {
+  prof_begin(c, KC_CONVGRAD);
+  const cudaError_t e = astr::launch2_convgrad<T, DIR>(v2_args<T>(c, DIR, false), c->st, c->CH[DIR], f,
+                                                       c->vsplit ? 1 : 0);
+  prof_end(c);
+  return launch_result(c, e, "k2_convgrad");
+}
+template <typename T, int DIR>
+int launch2_visc_c(astr_ctx* c) {
+  prof_begin(c, KC_VISC);
+  const cudaError_t e = astr::launch2_visc<T, DIR>(v2_args<T>(c, DIR, false), c->st, c->CH[DIR],
+                                                   c->vsplit ? 1 : 0);
+  prof_end(c);
+  return launch_result(c, e, "k2_visc");
+}
+
 template <typename T>
 int run_filter(astr_ctx* c, bool q2f_last) {
   const int nd = c->g.ndims;
+  if (use_v2(c) && !q2f_last) {
+    RC((launch2_filter_c<T, 0>(c)));
+    RC((launch2_filter_c<T, 1>(c)));
+    if (nd == 3) RC((launch2_filter_c<T, 2>(c)));
+    return ASTR_OK;
+  }
   RC((launch_filter<T, 0>(c, 0)));
   RC((launch_filter<T, 1>(c, (q2f_last && nd == 2) ? 1 : 0)));
   if (nd == 3) RC((launch_filter<T, 2>(c, q2f_last ? 1 : 0)));
@@ -1111,6 +1202,12 @@ int run_convgrad(astr_ctx* c, bool conv, bool grad, bool sigma, bool stats, bool
     f.sigma = sigma && f.last;
     f.stats = stats && f.last;
     f.qsave = qsave && dir == 0;
+    if (use_v2(c) && (conv || grad) && !f.sigma && !f.stats && !f.qsave) {
+      const int r2 = dir == 0 ? launch2_convgrad_c<T, 0>(c, f)
+                              : (dir == 1 ? launch2_convgrad_c<T, 1>(c, f) : launch2_convgrad_c<T, 2>(c, f));
+      RC(r2);
+      continue;
+    }
     int r = dir == 0 ? launch_convgrad<T, 0>(c, f)
                      : (dir == 1 ? launch_convgrad<T, 1>(c, f) : launch_convgrad<T, 2>(c, f));
     RC(r);
@@ -1125,6 +1222,11 @@ int run_visc(astr_ctx* c, bool fuse_rk, bool q2f) {
     VFlags f;
     f.last = fuse_rk && dir == nd - 1;
     f.q2f = q2f;
+    if (use_v2(c) && !f.last) {
+      const int r2 = dir == 0 ? launch2_visc_c<T, 0>(c) : (dir == 1 ? launch2_visc_c<T, 1>(c) : launch2_visc_c<T, 2>(c));
+      RC(r2);
+      continue;
+    }
     int r = dir == 0 ? launch_visc<T, 0>(c, f)
                      : (dir == 1 ? launch_visc<T, 1>(c, f) : launch_visc<T, 2>(c, f));
     RC(r);
@@ -1136,7 +1238,7 @@ int stats_finish(astr_ctx* c, double* out2) {
   const int last = c->g.ndims - 1;
   // partial sums: one per warp of the last convective sweep, or one per
   // block of the point statistics kernel (general metrics)
-  const long long nw = (c->gen || c->vsplit) ? (long long)point_grid(c->g.n0).x
+  const long long nw = (c->gen || c->vsplit || use_v2(c)) ? (long long)point_grid(c->g.n0).x
                               : (last == 2 ? sweep_warps<2>(c->g, c->lbw, c->lbb)
                                            : (last == 1 ? sweep_warps<1>(c->g, c->lbw, c->lbb)
                                                         : sweep_warps<0>(c->g, c->lbw, c->lbb)));
@@ -1189,6 +1291,14 @@ int sigma_pointwise(astr_ctx* c) {
   k_sigma<T><<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, dev<T>(c), c->ph);
   prof_end(c);
   return after_launch(c, "k_sigma");
+}
+
+template <typename T>
+int qsave_pointwise(astr_ctx* c) {
+  prof_begin(c, KC_POINT);
+  k_qsave<T><<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, dev<T>(c), c->ph);
+  prof_end(c);
+  return after_launch(c, "k_qsave");
 }
 
 template <typename T>
@@ -1306,15 +1416,19 @@ int one_step(astr_ctx* c, double* stats) {
       RC(run_filter<T>(c, true));
     } else {
       const bool visc = c->pm.diffterm != 0;
-      const bool split_sig = visc && ((c->split_last & 1) || c->gen || c->vsplit);
-      const bool split_rk = visc && ((c->split_last & 2) || c->vsplit);
-      const bool pt_stats = c->gen || c->vsplit;  // statistics by the point kernel
+      // the tiled sweeps leave the stress, the RK3 base and update and the
+      // statistics to point kernels
+      const bool v2 = use_v2(c);
+      const bool split_sig = visc && ((c->split_last & 1) || c->gen || c->vsplit || v2);
+      const bool split_rk = visc && ((c->split_last & 2) || c->vsplit || v2);
+      const bool pt_stats = c->gen || c->vsplit || v2;  // statistics by the point kernel
       if (c->pm.lfilter) RC(run_filter<T>(c, false));
       if (c->has_bc) RC(run_boucon<T>(c));
       RC(run_qswap<T>(c));
+      if (v2 && st1) RC(qsave_pointwise<T>(c));
       // compact MP: the sweeps give the gradients (and the RK3 base), the
       // convective residual comes from the MP kernels
-      RC(run_convgrad<T>(c, !c->mp, true, visc && !split_sig, st1 && stats && !pt_stats, st1));
+      RC(run_convgrad<T>(c, !c->mp, true, visc && !split_sig, st1 && stats && !pt_stats, st1 && !v2));
       // general metrics: gradients contracted with the metrics; then the
       // statistics from them where the sweeps do not take them
       if (c->gen) RC(gradphys_pointwise<T>(c));
@@ -1689,6 +1803,7 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
     d4.H = coef32 + off + 3 * n; d4.ac2 = coef32 + off + 4 * n; d4.A = coef32 + off + 5 * n;
     d4.K = coef32 + off + 6 * n; d4.KD = nkd ? coef32 + off + 6 * n + nk : nullptr;
     d8.n = d4.n = s.n; d8.first = d4.first = s.first; d8.ntype = d4.ntype = s.ntype;
+    d8.ks = d4.ks = s.n;
     d8.dim = d4.dim = s.dim;
     d8.ulo = d4.ulo = s.ulo; d8.uhi = d4.uhi = s.uhi;
     d8.u_ac1 = s.u_ac1; d8.u_ac3 = s.u_ac3;
@@ -1721,6 +1836,82 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
   };
   fill(c->d64, (double*)nullptr);
   fill(c->d32, (float*)nullptr);
+  {
+    // Tile-staged sweeps: main ordering, lines of at most 32 x 17 rows, every
+    // halo array addressable with 32-bit offsets (small grids spread the
+    // variables of a line over blocks as the register-window sweeps do).
+    // ASTR_V2=0 keeps the register-window sweeps.
+    bool el = params->order == ASTR_ORDER_MAIN && g.nh < (1LL << 31) / 6;
+    for (int d = 0; d < ndims; ++d) el = el && c->CH[d] <= 17 && c->CHf[d] <= 17;
+    // FP64 form: the register-window sweeps, whose occupancy keeps the FP64
+    // pipe busier (ASTR_V2=2 selects the tiled sweeps there too)
+    int v2mode = 1;
+    if (const char* ev = std::getenv("ASTR_V2")) v2mode = std::atoi(ev);
+    el = el && v2mode != 0 && (c->prec == ASTR_FP32_STORAGE || v2mode == 2);
+    if (el) {
+      std::vector<HostScheme> ps;
+      for (int dd = 0; dd < ndims; ++dd) {
+        ps.push_back(make_deriv(npdc[dd], dimv[dd], c->CH[dd], hft, 32 * c->CH[dd]));
+        ps.push_back(make_filter(npdc[dd], dimv[dd], params->alfa_filter, c->CHf[dd], hft,
+                                 32 * c->CHf[dd]));
+      }
+      size_t ptot = 0;
+      for (auto& q : ps) ptot += 6 * q.a.size() + q.K.size() + q.KD.size();
+      double* p64 = (double*)alloc(ptot * 8);
+      float* p32 = (float*)alloc(ptot * 4);
+      if (!ok) {
+        astr_gpu_destroy(c);
+        return fail(nullptr, ASTR_ERR_OOM, "device allocation failed");
+      }
+      std::vector<double> hb(ptot);
+      std::vector<float> fb2(ptot);
+      size_t po = 0;
+      for (size_t idx = 0; idx < ps.size(); ++idx) {
+        const HostScheme& q = ps[idx];
+        const size_t np = q.a.size(), nk = q.K.size(), nkd = q.KD.size();
+        const std::vector<double>* arr[6] = {&q.ac1, &q.ac3, &q.G, &q.H, &q.ac2, &q.a};
+        for (int a = 0; a < 6; ++a) std::memcpy(&hb[po + a * np], arr[a]->data(), np * 8);
+        std::memcpy(&hb[po + 6 * np], q.K.data(), nk * 8);
+        if (nkd) std::memcpy(&hb[po + 6 * np + nk], q.KD.data(), nkd * 8);
+        const size_t len = 6 * np + nk + nkd;
+        for (size_t i = 0; i < len; ++i) fb2[po + i] = (float)hb[po + i];
+        DScheme<double> d8{};
+        DScheme<float> d4{};
+        d8.ac1 = p64 + po; d8.ac3 = p64 + po + np; d8.G = p64 + po + 2 * np;
+        d8.H = p64 + po + 3 * np; d8.ac2 = p64 + po + 4 * np; d8.A = p64 + po + 5 * np;
+        d8.K = p64 + po + 6 * np; d8.KD = nkd ? p64 + po + 6 * np + nk : nullptr;
+        d4.ac1 = p32 + po; d4.ac3 = p32 + po + np; d4.G = p32 + po + 2 * np;
+        d4.H = p32 + po + 3 * np; d4.ac2 = p32 + po + 4 * np; d4.A = p32 + po + 5 * np;
+        d4.K = p32 + po + 6 * np; d4.KD = nkd ? p32 + po + 6 * np + nk : nullptr;
+        d8.n = d4.n = q.n; d8.first = d4.first = q.first; d8.ntype = d4.ntype = q.ntype;
+        d8.dim = d4.dim = q.dim; d8.ks = d4.ks = (int)np;
+        d8.ulo = d4.ulo = q.ulo; d8.uhi = d4.uhi = q.uhi;
+        astr_ctx::V2U u;
+        const int CHs = (int)(np / 32);
+        if (q.ulo <= q.uhi) {
+          u.a1 = q.u_ac1; u.a3 = q.u_ac3;
+          for (int m = 0; m < 6; ++m) u.K[m] = q.u_K[m];
+          for (int m = 0; m < 5; ++m) u.KD[m] = q.u_KD[m];
+          for (int t = 0; t < CHs; ++t) {
+            u.gp[t] = q.G[(size_t)q.ulo * CHs + t];
+            u.hp[t] = q.H[(size_t)q.ulo * CHs + t];
+          }
+        }
+        const int dd = (int)idx / 2;
+        if (idx % 2 == 0) { c->v2d64[dd] = d8; c->v2d32[dd] = d4; c->v2ud[dd] = u; }
+        else { c->v2f64[dd] = d8; c->v2f32[dd] = d4; c->v2uf[dd] = u; }
+        po += len;
+      }
+      e = cudaMemcpy(p64, hb.data(), ptot * 8, cudaMemcpyHostToDevice);
+      if (e == cudaSuccess) e = cudaMemcpy(p32, fb2.data(), ptot * 4, cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) {
+        std::string m = std::string("initialisation: ") + cudaGetErrorString(e);
+        astr_gpu_destroy(c);
+        return fail(nullptr, ASTR_ERR_CUDA, m);
+      }
+      c->v2 = true;
+    }
+  }
   if (params->conschm == ASTR_CONSCHM_MP) {
     // compact MP: scratch, and the upwind / downwind interface schemes of
     // each direction (compact_flux_initiate, src/flux.F90:32-112)
@@ -1773,7 +1964,7 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
       DScheme<double> d8{};
       d8.ac1 = fcoef + fo; d8.ac3 = fcoef + fo + n; d8.G = fcoef + fo + 2 * n;
       d8.H = fcoef + fo + 3 * n; d8.ac2 = fcoef + fo + 4 * n;
-      d8.n = f.n; d8.first = f.first; d8.ntype = f.ntype; d8.dim = f.dim;
+      d8.n = f.n; d8.first = f.first; d8.ntype = f.ntype; d8.dim = f.dim; d8.ks = f.n;
       d8.ulo = 1; d8.uhi = 0;
       if (idx % 2 == 0) c->mps.uw[idx / 2] = d8;
       else c->mps.dw[idx / 2] = d8;
@@ -2164,10 +2355,10 @@ int astr_gpu_reduce_stats(astr_ctx* c, double* ke, double* en) {
   RC(ready(c));
   // statistics over the current primitives and gradients: the point
   // kernel where the step takes them from it (general metrics, variables
-  // split over blocks), else the last conv/grad direction with only the
+  // split over blocks, tiled sweeps), else the last conv/grad direction with only the
   // statistics enabled (stats_finish reads the matching partial sums)
   int r;
-  if (c->gen || c->vsplit) {
+  if (c->gen || c->vsplit || use_v2(c)) {
     r = c->prec == ASTR_FP64 ? stats_pointwise<double>(c) : stats_pointwise<float>(c);
   } else {
     CGFlags f{0, 0, 0, 0, 0, 1, 0};

@@ -74,6 +74,7 @@ struct DScheme {
   int first;     // grid node of row 0
   int ntype;     // 3: periodic / inner block, 4: physical boundary at both ends
   int dim;       // im, jm or km
+  int ks;        // row stride of K and KD: n, or 32 x CH in the padded arrays of the tiled sweeps
   // Chunks ulo..uhi lie where the Thomas factors have reached their steady
   // values exactly (bit for bit) and hold no boundary row: there the
   // factors and folded coefficients are these constants, and the carry

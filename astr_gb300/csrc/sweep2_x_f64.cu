@@ -1,0 +1,6 @@
+// Tile-staged sweeps along x (direction 0) in double; see sweeps2.cuh.
+#include "sweeps2.cuh"
+
+namespace astr {
+ASTR_INSTANTIATE_SWEEPS2(double, 0)
+}  // namespace astr
