@@ -51,7 +51,24 @@ template <typename T>
 constexpr int v2_nl() { return sizeof(T) == 4 ? ASTR_V2_NL32 : ASTR_V2_NL64; }
 template <typename T>
 constexpr int v2_nt() { return 32 * v2_nl<T>(); }
-constexpr int V2_MINB = ASTR_V2_MINB;
+// The filter and viscous sweeps hold fewer tiles and fit more blocks per SM;
+// timed on the 512^3 TGV (FP32 storage): the filter 8.6 (two blocks), 7.7
+// (three), 7.2 ms (four) per launch; the viscous sweep 3.7, 3.4, 4.2 ms.
+#ifndef ASTR_V2_MINB_F
+#define ASTR_V2_MINB_F 4
+#endif
+#ifndef ASTR_V2_MINB_V
+#define ASTR_V2_MINB_V 3
+#endif
+// Convective + gradient sweeps: one task tile instead of two (the next
+// task's copies then start after the current task's outputs).
+#ifndef ASTR_V2_CG_SINGLE
+#define ASTR_V2_CG_SINGLE 0
+#endif
+constexpr bool V2_CG_SINGLE = ASTR_V2_CG_SINGLE != 0;
+constexpr int V2_MINB = ASTR_V2_MINB;      // convective + gradient sweeps
+constexpr int V2_MINB_F = ASTR_V2_MINB_F;  // filter
+constexpr int V2_MINB_V = ASTR_V2_MINB_V;  // viscous sweeps
 static_assert(ASTR_V2_NL32 == 4 || ASTR_V2_NL32 == 8 || ASTR_V2_NL32 == 16, "FP32 lines per block");
 static_assert(ASTR_V2_NL64 == 4 || ASTR_V2_NL64 == 8 || ASTR_V2_NL64 == 16, "FP64 lines per block");
 
@@ -127,6 +144,43 @@ __device__ __forceinline__ int v2_zs(const Geo& g) {
   return DIR == 0 ? 1 : (DIR == 1 ? (int)g.I : (int)g.IJ);
 }
 
+// Affine carry scan across the 32 chunks of each line of the block (as
+// scan_block, astr_kernels.cuh), without the closing barrier: the forward
+// and backward scans use separate halves of the scan memory, and every
+// reuse of a half is separated from its last read by the other scan's
+// barriers or the end-of-task barrier.
+template <bool FWD, typename T>
+__device__ __forceinline__ T scan2(T M, T L, T* sm) {
+  T* sM = sm;
+  T* sL = sm + 32 * SM_PITCH;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  sM[ty * SM_PITCH + tx] = M;
+  sL[ty * SM_PITCH + tx] = L;
+  __syncthreads();
+  const int nl = blockDim.x;
+  const int tid = tx + nl * ty;
+  const int w = tid >> 5, lane = tid & 31;
+  if (w < nl) {
+    T m = sM[lane * SM_PITCH + w];
+    T l = sL[lane * SM_PITCH + w];
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const T Mo = FWD ? __shfl_up_sync(0xffffffffu, m, off) : __shfl_down_sync(0xffffffffu, m, off);
+      const T Lo = FWD ? __shfl_up_sync(0xffffffffu, l, off) : __shfl_down_sync(0xffffffffu, l, off);
+      const bool ok = FWD ? (lane >= off) : (lane + off < 32);
+      if (ok) {
+        l = l + m * Lo;
+        m = m * Mo;
+      }
+    }
+    sL[lane * SM_PITCH + w] = l;
+  }
+  __syncthreads();
+  if (FWD) return ty == 0 ? T(0) : sL[(ty - 1) * SM_PITCH + tx];
+  return ty == 31 ? T(0) : sL[(ty + 1) * SM_PITCH + tx];
+}
+constexpr int V2_SCAN_WORDS = 4 * 32 * SM_PITCH;  // two scans x (M, L)
+
 // Chunked Thomas solve of chunk c (see astr_kernels.cuh), coefficients from
 // U in uniform chunks and from the padded arrays elsewhere.
 template <int CH, typename T>
@@ -143,7 +197,7 @@ __device__ __forceinline__ void solve2(T (&y)[CH], const DScheme<T>& S, const UC
     for (int t = 1; t < CH; ++t) y[t] = y[t] - y[t - 1] * __ldg(S.ac3 + s + t);
     M = __ldg(S.G + s + CH - 1);
   }
-  const T Yp = scan_block<true>(M, y[CH - 1], sm);
+  const T Yp = scan2<true>(M, y[CH - 1], sm);
   if (uni) {
 #pragma unroll
     for (int t = 0; t < CH; ++t) y[t] = fma(U.gp[t], Yp, y[t]);
@@ -161,7 +215,7 @@ __device__ __forceinline__ void solve2(T (&y)[CH], const DScheme<T>& S, const UC
     for (int t = CH - 2; t >= 0; --t) y[t] = y[t] - __ldg(S.ac1 + s + t) * y[t + 1];
     Mb = __ldg(S.H + s);
   }
-  const T Xn = scan_block<false>(Mb, y[0], sm);
+  const T Xn = scan2<false>(Mb, y[0], sm + 2 * 32 * SM_PITCH);
   if (uni) {
 #pragma unroll
     for (int t = 0; t < CH; ++t) y[t] = fma(U.hp[t], Xn, y[t]);
@@ -327,7 +381,7 @@ inline size_t v2_smem_bytes(int CH, int R, int P, int ntile) {
   const int NL = v2_nl<T>();
   const int nrt = 32 * CH + 2 * R;
   const size_t tw_ = DIR == 0 ? (size_t)NL * P : (size_t)nrt * NL;
-  return (ntile * tw_ + SCAN_SMEM_WORDS) * sizeof(T);
+  return (ntile * tw_ + V2_SCAN_WORDS) * sizeof(T);
 }
 
 // Pitch of an x tile: at least nrt words, 32/NL mod 32 (FP32) or 16/NL mod
@@ -357,7 +411,7 @@ inline UCo<T, CH> make_uco(const V2Args<T>& a) {
 // variables in place.
 // ---------------------------------------------------------------------------
 template <typename T, int DIR, int CH>
-__global__ void __launch_bounds__(v2_nt<T>(), V2_MINB)
+__global__ void __launch_bounds__(v2_nt<T>(), sizeof(T) == 4 ? V2_MINB_F : 2)
 k2_filter(Geo g, DevT<T> d, DScheme<T> S, UCo<T, CH> U, FTab<T> Tb, int P) {
   constexpr int NL = v2_nl<T>(), R = 5, NRT = 32 * CH + 2 * R, E = (NRT + 31) / 32;
   constexpr bool delta = sizeof(T) == 4;
@@ -472,7 +526,7 @@ k2_convgrad(Geo g, DevT<T> d, DScheme<T> S, UCo<T, CH> U, CGFlags fl, int P) {
   T* tB = tA + TWd;
   T* tC = tB + TWd;
   T* buf0 = tC + TWd;
-  T* scan = buf0 + 2 * TWd;
+  T* scan = buf0 + (V2_CG_SINGLE ? 1 : 2) * TWd;
   const int ol = threadIdx.x, c = threadIdx.y;
   const bool uni = c >= S.ulo && c <= S.uhi;
   const int hs = v2_hs<DIR>(g), zs = v2_zs<DIR>(g);
@@ -581,7 +635,7 @@ k2_convgrad(Geo g, DevT<T> d, DScheme<T> S, UCo<T, CH> U, CGFlags fl, int P) {
 #pragma unroll 1
   for (int t = t0; t < t1; ++t) {
     const bool more = t + 1 < t1;
-    if (more) issue(t + 1, buf0 + (cur ^ 1) * TWd);
+    if (more && !V2_CG_SINGLE) issue(t + 1, buf0 + (cur ^ 1) * TWd);
     T* bc = buf0 + cur * TWd;
     T y[CH];
     rhs_deriv2<DIR, NL, CH>(y, bc, P, ol, S, U, c, uni);
@@ -623,9 +677,17 @@ k2_convgrad(Geo g, DevT<T> d, DScheme<T> S, UCo<T, CH> U, CGFlags fl, int P) {
         }
       }
     }
-    if (more) finish(t + 1, buf0 + (cur ^ 1) * TWd);
+    if (V2_CG_SINGLE) {
+      if (DIR == 0) __syncthreads();  // the output pass has read the tile
+      if (more) {
+        issue(t + 1, buf0);
+        finish(t + 1, buf0);
+      }
+    } else {
+      if (more) finish(t + 1, buf0 + (cur ^ 1) * TWd);
+      cur ^= 1;
+    }
     __syncthreads();
-    cur ^= 1;
   }
 }
 
@@ -634,7 +696,7 @@ k2_convgrad(Geo g, DevT<T> d, DScheme<T> S, UCo<T, CH> U, CGFlags fl, int P) {
 // update after the last one runs as a point kernel.
 // ---------------------------------------------------------------------------
 template <typename T, int DIR, int CH>
-__global__ void __launch_bounds__(v2_nt<T>(), V2_MINB)
+__global__ void __launch_bounds__(v2_nt<T>(), sizeof(T) == 4 ? V2_MINB_V : 2)
 k2_visc(Geo g, DevT<T> d, DScheme<T> S, UCo<T, CH> U, int P) {
   constexpr int NL = v2_nl<T>(), R = 3, NRT = 32 * CH + 2 * R, E = (NRT + 31) / 32;
   extern __shared__ __align__(16) unsigned char v2_smem[];
@@ -793,7 +855,7 @@ cudaError_t launch2_filter_ch(const V2Args<T>& a, cudaStream_t st, int vsplit) {
 template <typename T, int DIR, int CHC>
 cudaError_t launch2_convgrad_ch(const V2Args<T>& a, cudaStream_t st, CGFlags f, int vsplit) {
   const int P = v2_pitch<T>(CHC, 3);
-  const size_t smem = v2_smem_bytes<T, DIR>(CHC, 3, P, 5);
+  const size_t smem = v2_smem_bytes<T, DIR>(CHC, 3, P, V2_CG_SINGLE ? 4 : 5);
   cudaError_t e = v2_allow_smem(k2_convgrad<T, DIR, CHC>, smem);
   if (e != cudaSuccess) return e;
   const int ntask = (f.conv ? 5 : 0) + (f.grad ? 4 : 0);
