@@ -60,7 +60,7 @@ FLOPS_PER_PT = {"filter": 110.0, "convgrad": 113.0, "pointwise": 48.0,
                 "visc": 52.0, "visc_last": 106.0}
 
 
-def bytes_per_pt(kind, d, stage1, f32):
+def bytes_per_pt(kind, d, stage1, f32, tiled=False):
     """Algorithmic DRAM bytes per interior point of one launch: every array
     element the kernel must read or write once.  w = storage word (8 or 4);
     m = FP64 word of the RK3 base, the FP32 form's master state and 1/J.
@@ -77,6 +77,8 @@ def bytes_per_pt(kind, d, stage1, f32):
     """
     w = 4.0 if f32 else 8.0
     m = 8.0
+    if tiled:
+        return tiled_bytes_per_pt(kind, d, f32)
     if kind == "filter":
         return 10 * w + (10 * m if f32 else 0.0)
     if kind == "convgrad":
@@ -97,10 +99,67 @@ def bytes_per_pt(kind, d, stage1, f32):
     raise ValueError(kind)
 
 
-def class_work(kind, f32, launches, pts):
+def tiled_bytes_per_pt(kind, d, f32):
+    """The same count for the tile-staged sweeps, which leave the RK3 base,
+    the stress and the RK3 update to point kernels.
+      filter: as above
+      convgrad x: q 5, u v w p T, dxi, J in; qrhs 5 + 4 gradients out; y, z
+        add qrhs 5 in
+      visc (every direction): stress 3 + heat flux 1, dxi, J, qrhs 4 in;
+        qrhs 4 out
+      pointwise, per step: 3 stress launches (12 gradients, T, u v w in;
+        stress 6 + heat flux 3 out), 3 RK3 updates (qrhs 5, qsave 5 (FP64),
+        q or the FP64 master 5, J and 1/J (FP64) in; q 5 (+ master 5) and the
+        primitives 6 out) and 1 RK3 base (q or master 5, J in; qsave 5 out),
+        averaged over the 7 launches"""
+    w = 4.0 if f32 else 8.0
+    m = 8.0
+    if kind == "filter":
+        return 10 * w + (10 * m if f32 else 0.0)
+    if kind == "convgrad":
+        return 21 * w if d == 0 else 26 * w
+    if kind == "visc":
+        return 14 * w
+    if kind == "pointwise":
+        sig = 25 * w
+        if f32:
+            rk = 5 * w + 5 * m + 5 * m + 2 * m + 5 * w + 5 * m + 6 * w
+        else:
+            rk = 5 * w + 5 * m + 5 * w + 2 * m + 5 * w + 6 * w
+        base = 5 * m + m + 5 * m
+        return (3 * sig + 3 * rk + base) / 7.0
+    raise ValueError(kind)
+
+
+# Algorithmic bytes per unique point and RK3 stage of the pass model
+# (P1) of the scope table: s = stream word (4 or 8), S = 8 (FP64 master and
+# RK3 base).  Per launch of a class: filter 10 s (three directions of 30 s);
+# convective + gradient sweeps (A + B + C) / 3 = (14 + 19 + 32) s / 3;
+# viscous sweeps (D + E + F) / 3 = ((12 + 12 + 17.33) s + 6.67 S) / 3.
+def p1_bytes_per_launch(kind, f32):
+    s = 4.0 if f32 else 8.0
+    S = 8.0
+    if kind == "filter":
+        return 10.0 * s
+    if kind == "convgrad":
+        return (14.0 + 19.0 + 32.0) * s / 3.0
+    if kind == "visc":
+        return ((12.0 + 12.0 + 17.0 + 1.0 / 3.0) * s + (6.0 + 2.0 / 3.0) * S) / 3.0
+    return None
+
+
+def class_work(kind, f32, launches, pts, tiled=False):
     """Algorithmic bytes and flops of `launches` launches of one kernel class
     over whole RK3 steps (per step: 3 stages x 3 directions, or 3 stages x 1
     point launch)."""
+    if tiled:
+        nb = tiled_bytes_per_pt(kind, 0, f32) if kind != "convgrad" else \
+            (tiled_bytes_per_pt(kind, 0, f32) + 2 * tiled_bytes_per_pt(kind, 1, f32)) / 3.0
+        fl = {"filter": FLOPS_PER_PT["filter"], "convgrad": FLOPS_PER_PT["convgrad"],
+              "visc": FLOPS_PER_PT["visc"] + 0.0,
+              "pointwise": (3 * FLOPS_PER_PT["pointwise"] + 3 * (FLOPS_PER_PT["visc_last"] -
+                                                                  FLOPS_PER_PT["visc"]) + 5) / 7.0}[kind]
+        return nb * pts * launches, fl * pts * launches
     dirs = (0,) if kind == "pointwise" else (0, 1, 2)
     per_step_b = sum(bytes_per_pt(kind, d, s == 0, f32) for s in range(3) for d in dirs)
     if kind == "visc":
@@ -216,31 +275,54 @@ def cpu_port_throughput(n, steps, threads=None):
     return n ** 3 * 3 * steps / dt / 1e6, po.get_threads(), dt
 
 
+def mem_available_gb():
+    try:
+        for line in open("/proc/meminfo"):
+            if line.startswith("MemAvailable:"):
+                return float(line.split()[1]) / 1024 ** 2
+    except Exception:
+        pass
+    return 0.0
+
+
 def run_reference(args, rank, world, dist):
+    """The oracle (C++ restatement of the reference routines) on all host
+    cores.  At the headline size (512^3) when the host has the memory for it
+    (about 66 GB), with at most 2 timed steps after 1 warm-up step (each
+    step is some 30-70 s of CPU work); otherwise 128^3 steps, whose per-point
+    rate stands in for 512^3 (stated in config.sample)."""
     if rank != 0:
         return 0
-    n = 128
     from oracle import pyoracle as po
     threads = os.cpu_count()
     po.set_threads(threads)
+    need = 1.24 * ((512 + 11) / (128 + 11)) ** 3  # GB, scaled from a 128^3 measurement
+    big = mem_available_gb() >= 1.5 * need and not os.environ.get("ASTR_REF_SMALL")
+    n = 512 if big else 128
+    steps = min(args.steps, 2) if big else args.steps
+    warmup = 1 if big else args.warmup
     o = po.tgv_main(n)
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         o.rk3_steps(1)
     t0 = time.perf_counter()
-    o.rk3_steps(args.steps)
+    o.rk3_steps(steps)
     dt = time.perf_counter() - t0
-    v = n ** 3 * 3 * args.steps / dt / 1e6
+    v = n ** 3 * 3 * steps / dt / 1e6
+    sample = (f"C++ restatement of the reference routines, TGV {n}^3 (main-solver order), "
+              f"{steps} timed RK3 steps after {warmup} warm-up, 1 process, "
+              f"{po.get_threads()} OpenMP threads")
+    if not big:
+        sample += "; the 512^3 workload did not fit the host memory, its per-point rate stands in"
     line = {
         "impl": "reference", "metric": METRIC, "value": round(v, 3), "unit": UNIT,
-        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": round(1e3 * dt / args.steps, 3), "higher_is_better": True,
+        "n_gpus": world, "steps": steps, "warmup": warmup,
+        "ms_per_step": round(1e3 * dt / steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "Taylor-Green vortex 512^3, main-solver RK3 stage order",
-                   "sample": f"TGV {n}^3, one RK3 step per timed step"},
+                   "sample": f"TGV {n}^3, one RK3 step per timed step",
+                   "same_size": big},
         "cpu_baseline": {"value": round(v, 3), "unit": UNIT, "cores": po.get_threads(),
-                         "kind": "port",
-                         "sample": f"C++ restatement of the reference routines, TGV {n}^3, "
-                                   f"{args.steps} RK3 steps, 1 process, {po.get_threads()} OpenMP threads"},
+                         "kind": "port", "sample": sample},
         "e2e": {"value": round(v, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -297,13 +379,13 @@ def state_error(q, ref):
     return out
 
 
-def form_roofline(kt, f32, pts_int, fp64_peak, hbm_peak, hbm_source):
+def form_roofline(kt, f32, pts_int, fp64_peak, hbm_peak, hbm_source, tiled=False, pts_unique=None):
     classes = {}
     for k in ("filter", "convgrad", "pointwise", "visc"):
         tms, cnt = kt[k]
         if cnt == 0:
             continue
-        nbytes, flops = class_work(k, f32, cnt, pts_int)
+        nbytes, flops = class_work(k, f32, cnt, pts_int, tiled)
         classes[k] = {"ms": tms, "launches": cnt, "avg_ms": tms / cnt,
                       "gbs": nbytes / (tms / 1e3) / 1e9, "tflops": flops / (tms / 1e3) / 1e12,
                       "bytes_per_launch": nbytes / cnt, "flops_per_launch": flops / cnt}
@@ -329,6 +411,17 @@ def form_roofline(kt, f32, pts_int, fp64_peak, hbm_peak, hbm_source):
                 "hbm_achieved_gbs": round(dc["gbs"], 1),
                 "hbm_frac": round(dc["gbs"] / hbm_peak, 4), "hbm_peak_source": hbm_source}
     roof["traffic"] = traffic
+    roof["bytes_model"] = ("per-kernel: every array element the launch reads or writes once "
+                           "(stored nodes)")
+    # the same kernel against the scope table's pass-model bytes (P1, unique
+    # points): the fraction a fully fused pass structure would score
+    p1 = p1_bytes_per_launch(dom, f32)
+    if p1 is not None and pts_unique:
+        a1 = p1 * pts_unique / (dc["avg_ms"] / 1e3) / 1e9
+        roof["p1"] = {"bytes_per_point_launch": round(p1, 2), "achieved": round(a1, 1),
+                      "unit": "GB/s", "frac": round(a1 / hbm_peak, 4),
+                      "note": "pass-model (P1) bytes per unique point and launch of this class "
+                              "over its average CUDA-event launch time, against the same peak"}
     roof["classes"] = {k: {kk: rnd(vv) for kk, vv in v.items()} for k, v in classes.items()}
     return roof
 
@@ -382,23 +475,51 @@ def run_gpu(args, rank, world, dist):
     if args.form != "both":
         # one form only (for profiling); no error against FP64
         runs = [r for r in runs if r[0] == args.form]
+    # end to end through the C ABI with page-locked host buffers, per form:
+    # every step uploads the state q (the primitives are recomputed from it
+    # on the device, astr_gpu_upload_q), runs one RK3 step, and downloads q
+    pinned_q = capi.PinnedArray(st["q"].shape)
+    pinned_q.array[...] = st["q"]
+    qout = capi.PinnedArray(st["q"].shape)
+    e2e_steps = max(10, args.steps)
+    launches_per_step = 0
+    v2env = os.environ.get("ASTR_V2", "1")
     for name, prec in runs:
         g = make_solver(n, prec, metrics, st)
+        f32 = prec == capi.FP32_STORAGE
+        tiled = (f32 and v2env != "0") or v2env == "2"
         ms, kt, clk, hist0 = time_form(g, args, dist)
         forms[name] = {
             "value": round(world * pts * 3 * args.steps / (ms / 1e3) / 1e6, 3),
             "ms_per_step": round(ms / args.steps, 3),
-            "roofline": form_roofline(kt, prec == capi.FP32_STORAGE, pts_int, fp64_peak, hbm_peak,
-                                      hbm_source),
+            "roofline": form_roofline(kt, f32, pts_int, fp64_peak, hbm_peak, hbm_source, tiled, pts),
+            "sweeps": "tiled" if tiled else "register-window",
             "footprint_gb": round(capi.load().astr_gpu_footprint(g.dims, g.params) / 1e9, 2),
             "stats_first_step": {"kenergy": float(hist0[0, 0]), "enstrophy": float(hist0[0, 1])},
         }
         clocks[name] = clk
         finals[name] = interior_q(g, n) if rank == 0 else None
+        # one untimed round trip (first-use costs of the transfer path)
+        g.upload_q(pinned_q.array)
+        g.time_integration_rk(1)
+        g._c(g.L.astr_gpu_download_state(g.h, capi.dptr(qout.array), None, None, None, None))
+        barrier(dist)
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            g.upload_q(pinned_q.array)
+            g.time_integration_rk(1)
+            g._c(g.L.astr_gpu_download_state(g.h, capi.dptr(qout.array), None, None, None, None))
+        t_e2e = max_over_ranks(dist, time.perf_counter() - t0)
+        forms[name]["e2e"] = {"value": round(world * pts * 3 * e2e_steps / t_e2e / 1e6, 3),
+                              "unit": UNIT, "h2d_bytes_per_step": pinned_q.nbytes,
+                              "d2h_bytes_per_step": qout.nbytes + 16, "steps": e2e_steps}
         if name == runs[-1][0]:
-            head = g
-        else:
-            g.close()
+            g0 = g.launches
+            g.timed_steps(1)
+            launches_per_step = g.launches - g0
+        g.close()
+    pinned_q.free()
+    qout.free()
     err = None
     if rank == 0 and len(runs) == 2:
         err = state_error(finals["fp32_storage"], finals["fp64"])
@@ -406,40 +527,30 @@ def run_gpu(args, rank, world, dist):
         err["reference"] = "plain FP64 GPU form, same initial state and steps"
     finals.clear()
 
-    # end to end through the C ABI with page-locked host buffers (headline
-    # form): every step uploads the state q (the primitives are recomputed
-    # from it on the device, astr_gpu_upload_q), runs one RK3 step with its
-    # statistics, and downloads q
-    g = head
-    pinned = {}
-    for k in ("q",):
-        pa = capi.PinnedArray(st[k].shape)
-        pa.array[...] = st[k]
-        pinned[k] = pa
-    qout = capi.PinnedArray(st["q"].shape)
-    del st
-    e2e_steps = max(1, min(args.steps, 3))
-    # one untimed round trip (first-use costs of the transfer path)
-    g.upload_q(pinned["q"].array)
-    g.time_integration_rk(1)
-    g._c(g.L.astr_gpu_download_state(g.h, capi.dptr(qout.array), None, None, None, None))
-    barrier(dist)
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        g.upload_q(pinned["q"].array)
-        g.time_integration_rk(1)
-        g._c(g.L.astr_gpu_download_state(g.h, capi.dptr(qout.array), None, None, None, None))
-    t_e2e = time.perf_counter() - t0
-    t_e2e = max_over_ranks(dist, t_e2e)
-    h2d = sum(pinned[k].nbytes for k in pinned)
-    d2h = qout.nbytes + 16
-    e2e_value = world * pts * 3 * e2e_steps / t_e2e / 1e6
-    for pa in list(pinned.values()) + [qout]:
-        pa.free()
-    g0 = g.launches
-    g.timed_steps(1)
-    launches_per_step = g.launches - g0
-    g.close()
+    # kinetic-energy / enstrophy histories of both forms over the scale
+    # test's 200 steps from the same initial state (untimed)
+    history = None
+    if rank == 0 and len(runs) == 2 and args.history_steps > 0:
+        hist = {}
+        for name, prec in runs:
+            g = make_solver(n, prec, metrics, st)
+            hist[name] = g.time_integration_rk(args.history_steps)
+            if name == "fp64":
+                q64_end = interior_q(g, n)
+            else:
+                q32_end = interior_q(g, n)
+            g.close()
+        h64, h32 = hist["fp64"], hist["fp32_storage"]
+        rel = np.abs(h32 - h64) / np.abs(h64)
+        history = {"steps": args.history_steps,
+                   "kenergy_max_rel_diff": float(rel[:, 0].max()),
+                   "enstrophy_max_rel_diff": float(rel[:, 1].max()),
+                   "kenergy_fp64_first_last": [float(h64[0, 0]), float(h64[-1, 0])],
+                   "enstrophy_fp64_first_last": [float(h64[0, 1]), float(h64[-1, 1])],
+                   "final_state_error": state_error(q32_end, q64_end),
+                   "reference": "plain FP64 GPU form, same initial state, statistics every step"}
+        del q64_end, q32_end
+    e2e_line = forms[runs[-1][0]]["e2e"]
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -466,10 +577,10 @@ def run_gpu(args, rank, world, dist):
             "fp32_over_fp64": (round(f32["value"] / forms["fp64"]["value"], 3)
                                if len(forms) == 2 else None),
             "error_vs_fp64": err,
+            "history_vs_fp64": history,
             "gpu_launches": launches_per_step * args.steps,
             "roofline": f32["roofline"],
-            "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "steps": e2e_steps},
+            "e2e": e2e_line,
             "cpu_baseline": cpu,
             "clocks": clocks[runs[-1][0]],
             "clocks_fp64": clocks.get("fp64"),
@@ -823,6 +934,7 @@ def main():
     ap.add_argument("--vortex-n", type=int, default=512)
     ap.add_argument("--vortex-steps", type=int, default=1000)
     ap.add_argument("--history", type=int, default=0)
+    ap.add_argument("--history-steps", type=int, default=200)
     ap.add_argument("--history-out", default="")
     args = ap.parse_args()
     if args.warmup < 3:
