@@ -118,6 +118,81 @@ def test_plain_c_host(gpu_lib, tmp_path):
     assert lines[1].startswith(f"create {capi.ASTR_ERR_ARG} grid too small")
 
 
+C_HOST_NULLS = r"""
+#include "astr_gpu.h"
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+/* Every nullable argument of the state, residual and step entry points
+   passed as NULL, one at a time and all together, on a uniform 16^3 box. */
+#define CHECK(x) do { int rc_ = (x); if (rc_ != ASTR_OK) { printf("FAIL %s -> %d\n", #x, rc_); return 1; } } while (0)
+int main(void) {
+  const int n = 16;
+  const size_t nh = (size_t)(n + 11) * (n + 11) * (n + 11), n0 = (size_t)(n + 1) * (n + 1) * (n + 1);
+  astr_dims d = {n, n, n, n, n, n, 3, 3, 3};
+  astr_params p = {0};
+  astr_ctx* c = NULL;
+  astr_status st;
+  double hist[4], dx = 6.283185307179586 / n, pinf = 1.0 / (1.4 * 0.01);
+  double *q = malloc(5 * nh * sizeof(double)), *rho = malloc(nh * sizeof(double));
+  double *vel = calloc(3 * nh, sizeof(double)), *prs = malloc(nh * sizeof(double));
+  double *tmp = malloc(nh * sizeof(double)), *x1 = malloc(nh * sizeof(double));
+  double *jac = malloc(nh * sizeof(double)), *qrhs = malloc(5 * n0 * sizeof(double));
+  double *dvel = malloc(9 * n0 * sizeof(double)), *dtmp = malloc(3 * n0 * sizeof(double));
+  size_t i;
+  p.order = ASTR_ORDER_MAIN; p.precision = ASTR_FP64; p.lfilter = 1; p.diffterm = 1;
+  p.alfa_filter = 0.49; p.beter_halo = 1.11; p.beter_bound = 0.98; p.mach = 0.1;
+  p.reynolds = 1600.0; p.prandtl = 0.72; p.ref_tem = 273.15; p.suth_const = 110.3;
+  p.deltat = 1e-3;
+  for (i = 0; i < nh; ++i) {
+    rho[i] = 1.0; prs[i] = pinf; tmp[i] = 1.0; x1[i] = 1.0 / dx; jac[i] = dx * dx * dx;
+    q[i] = 1.0; q[nh + i] = q[2 * nh + i] = q[3 * nh + i] = 0.0; q[4 * nh + i] = pinf / 0.4;
+  }
+  CHECK(astr_gpu_create(&d, &p, &c));
+  CHECK(astr_gpu_set_metrics_diag(c, x1, x1, x1, jac));
+  CHECK(astr_gpu_upload_state(c, q, rho, vel, prs, tmp));
+  CHECK(astr_gpu_rk3_step(c, 1, NULL, NULL));
+  CHECK(astr_gpu_rk3_step(c, 2, hist, NULL));
+  CHECK(astr_gpu_rk3_step(c, 1, NULL, &st));
+  CHECK(astr_gpu_download_state(c, NULL, NULL, NULL, NULL, NULL));
+  for (i = 0; i < nh; ++i) rho[i] = prs[i] = -1.0;
+  CHECK(astr_gpu_download_state(c, NULL, rho, NULL, NULL, NULL));
+  CHECK(astr_gpu_download_state(c, NULL, NULL, NULL, prs, NULL));
+  CHECK(astr_gpu_download_state(c, q, NULL, vel, NULL, tmp));
+  CHECK(astr_gpu_download_rhs(c, NULL, NULL, NULL));
+  CHECK(astr_gpu_download_rhs(c, qrhs, NULL, NULL));
+  CHECK(astr_gpu_download_rhs(c, NULL, dvel, NULL));
+  CHECK(astr_gpu_download_rhs(c, NULL, NULL, dtmp));
+  astr_gpu_destroy(c);
+  /* a uniform state stays uniform */
+  printf("rho %.15g prs %.15g ke %.3g crash %d\n", rho[nh / 2], prs[nh / 2] / pinf, hist[2], st.crash);
+  return fabs(rho[nh / 2] - 1.0) < 1e-12 && fabs(prs[nh / 2] / pinf - 1.0) < 1e-12 ? 0 : 2;
+}
+"""
+
+
+@pytest.mark.gpu
+def test_plain_c_host_null_arguments(gpu_lib, tmp_path):
+    """A C host passes NULL for each array the state, residual and step
+    entry points may skip (the contract the Fortran binding's c_null_ptr
+    arguments rely on)."""
+    import shutil
+    import subprocess
+    from astr_gb300 import capi
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not found")
+    src = tmp_path / "nulls.c"
+    src.write_text(C_HOST_NULLS)
+    exe = tmp_path / "nulls"
+    libdir = os.path.dirname(capi.LIB_PATH)
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror",
+                    "-I", os.path.join(ROOT, "include"), str(src), "-L", libdir, "-lastr_gb300",
+                    "-Wl,-rpath," + libdir, "-lm", "-o", str(exe)], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    print(r.stdout)
+    assert r.returncode == 0, r.stdout + r.stderr
+
+
 # Faces on which each routine of boucon exists (src/bc.F90: noslip 6306-6712
 # all faces; noslip_adibatic 6728-7036 x and y; slipisotwall 7038-7229 and
 # slipadibwall 7231-7430 y; outflow 3404-3617 xmax and ymax; farfield
