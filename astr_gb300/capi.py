@@ -41,7 +41,8 @@ EXPORTS = [
     "astr_gpu_set_profiling", "astr_gpu_kernel_times", "astr_gpu_measure_fp64_peak",
     "astr_gpu_stats_noalloc", "astr_gpu_set_grid", "astr_gpu_channel_state",
     "astr_gpu_boucon", "astr_gpu_step_async", "astr_gpu_poll", "astr_gpu_crashcheck",
-    "astr_gpu_cflcal", "astr_gpu_upload_q",
+    "astr_gpu_cflcal", "astr_gpu_upload_q", "astr_gpu_set_crash_control", "astr_gpu_databakup",
+    "astr_gpu_crashfix", "astr_gpu_crash_report",
 ]
 NOALLOC_STATS_MAX_BLOCKS = 65536
 KERNEL_CLASSES = ["filter", "halo", "convgrad", "visc", "pointwise", "stats", "mp"]
@@ -131,6 +132,14 @@ def load(path: str = LIB_PATH):
                                          vp, dp, dp]
     L.astr_gpu_stats_noalloc.restype = ip
     L.astr_gpu_crashcheck.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ip)]
+    L.astr_gpu_set_crash_control.argtypes = [vp, ip]
+    L.astr_gpu_set_crash_control.restype = ip
+    L.astr_gpu_databakup.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_longlong)]
+    L.astr_gpu_databakup.restype = ip
+    L.astr_gpu_crashfix.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
+    L.astr_gpu_crashfix.restype = ip
+    L.astr_gpu_crash_report.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
+    L.astr_gpu_crash_report.restype = ip
     L.astr_gpu_crashcheck.restype = ip
     L.astr_gpu_cflcal.argtypes = [vp, ctypes.c_double, dp, dp]
     L.astr_gpu_cflcal.restype = ip

@@ -501,6 +501,134 @@ __global__ void k_crashcheck(Geo g, DevT<T> d, unsigned long long* out) {
   }
 }
 
+// --- Crash control (lcracon): databakup, crinod, crashfix ----------------
+// src/mainloop.F90:709-1198.  Snapshots hold the interior conserved state
+// in FP64 (the FP32-storage form's master) plus the channel controller.
+template <typename T>
+__global__ void k_snap_save(Geo g, DevT<T> d, double* dst) {
+  int i, j, k;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (!point_of(g, idx, i, j, k)) return;
+  const long long p = hidx(g, i, j, k);
+  for (int m = 0; m < 5; ++m) dst[m * g.n0 + idx] = q64(d, p, idx, m, g.nh, g.n0);
+}
+template <typename T>
+__global__ void k_snap_load(Geo g, DevT<T> d, const double* src) {
+  int i, j, k;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (!point_of(g, idx, i, j, k)) return;
+  const long long p = hidx(g, i, j, k);
+  for (int m = 0; m < 5; ++m) {
+    const double v = src[m * g.n0 + idx];
+    d.q[m * g.nh + p] = (T)v;
+    if (d.qm) d.qm[m * g.n0 + idx] = v;
+  }
+}
+// crashcheck's node test (q1 >= 0 fails: negative or NaN density) into the
+// critical-node mask
+template <typename T>
+__global__ void k_crinod_mark(Geo g, DevT<T> d, unsigned char* crinod) {
+  int i, j, k;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (!point_of(g, idx, i, j, k)) return;
+  if (!(q64(d, hidx(g, i, j, k), idx, 0, g.nh, g.n0) >= 0.0)) crinod[idx] = 1;
+}
+// crinod_expansion (src/mainloop.F90:985-1033): every critical node marks
+// its 3x3x3 neighbourhood (interior nodes here; the reference's mask also
+// spans two halo layers, which no computation reads)
+__global__ void k_crinod_expand(Geo g, const unsigned char* in, unsigned char* out) {
+  int i, j, k;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (!point_of(g, idx, i, j, k)) return;
+  unsigned char v = 0;
+  for (int kk = -1; kk <= 1 && !v; ++kk)
+    for (int jj = -1; jj <= 1 && !v; ++jj)
+      for (int ii = -1; ii <= 1 && !v; ++ii) {
+        const int a = i + ii, b = j + jj, e = k + kk;
+        if (a < 0 || a > g.im || b < 0 || b > g.jm || e < 0 || e > g.km) continue;
+        v = in[zidx(g, a, b, e)];
+      }
+  out[idx] = v;
+}
+// crashfix, pass 1 (src/mainloop.F90:1045-1198): nodes whose density,
+// pressure or temperature is below its floor (or not a number) are flagged
+// and marked critical; count[0] counts them.
+template <typename T>
+__global__ void k_crashfix_flag(Geo g, DevT<T> d, double eps_rho, double eps_prs, double eps_tmp,
+                                unsigned char* flag, unsigned char* crinod, unsigned long long* count) {
+  int i, j, k;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (!point_of(g, idx, i, j, k)) return;
+  const long long p = hidx(g, i, j, k);
+  const double ro = d.pr[p], pp = d.pr[p + 4 * g.nh], tt = d.pr[p + 5 * g.nh];
+  const bool bad = !(ro >= eps_rho && pp >= eps_prs && tt >= eps_tmp);
+  flag[idx] = bad ? 1 : 0;
+  if (bad) {
+    crinod[idx] = 1;
+    atomicAdd(count, 1ULL);
+  }
+}
+// crashfix, pass 2: one block walks the interior in the reference's loop
+// order (i fastest) and, node by node, replaces q at each flagged node by
+// the mean of its 26 neighbours whose rho, p and T are non-negative
+// (neighbours outside the domain in i or j skipped, as the reference's
+// ig0/jg0 test does; k neighbours may be halo nodes), then recovers that
+// node's primitives; later nodes see the earlier fixes, as in the serial
+// loop.  Returns at once when pass 1 flagged nothing.
+template <typename T>
+__global__ void k_crashfix_apply(Geo g, DevT<T> d, Phys ph, const unsigned char* flag,
+                                 unsigned long long* count) {
+  if (count[0] == 0) return;
+  __shared__ int any;
+  const long long n0 = g.n0;
+  for (long long base = 0; base < n0; base += blockDim.x) {
+    const long long idx = base + threadIdx.x;
+    const bool f = idx < n0 && flag[idx];
+    if (threadIdx.x == 0) any = 0;
+    __syncthreads();
+    if (f) any = 1;
+    __syncthreads();
+    if (!any) continue;
+    if (threadIdx.x == 0) {
+      for (int t = 0; t < (int)blockDim.x && base + t < n0; ++t) {
+        const long long z = base + t;
+        if (!flag[z]) continue;
+        const int i = (int)(z % g.I), j = (int)((z / g.I) % (g.jm + 1)), k = (int)(z / g.IJ);
+        double qa[5] = {0, 0, 0, 0, 0};
+        int norm = 0;
+        // kk runs over -1..1 in 2-D as well: the reference reads the k halo
+        // planes (copies of plane 0 as the last qswap left them)
+        for (int kk = -1; kk <= 1; ++kk)
+          for (int jj = -1; jj <= 1; ++jj)
+            for (int ii = -1; ii <= 1; ++ii) {
+              if (ii == 0 && jj == 0 && kk == 0) continue;
+              const int a = i + ii, b = j + jj, e = k + kk;
+              if (a < 0 || a > g.im || b < 0 || b > g.jm) continue;
+              const long long pn = hidx(g, a, b, e);
+              const double ro = d.pr[pn], pp = d.pr[pn + 4 * g.nh], tt = d.pr[pn + 5 * g.nh];
+              if (ro >= 0.0 && pp >= 0.0 && tt >= 0.0) {
+                const bool inner = e >= 0 && e <= g.km;
+                for (int m = 0; m < 5; ++m)
+                  qa[m] += inner ? q64(d, pn, zidx(g, a, b, e), m, g.nh, g.n0) : (double)d.q[m * g.nh + pn];
+                ++norm;
+              }
+            }
+        if (norm >= 1) {
+          const long long p = hidx(g, i, j, k);
+          for (int m = 0; m < 5; ++m) {
+            const double v = qa[m] / (double)norm;
+            d.q[m * g.nh + p] = (T)v;
+            if (d.qm) d.qm[m * n0 + z] = v;
+          }
+          q2fvar_store(g, d, ph, p);
+          atomicAdd(count + 1, 1ULL);
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // cflcal (src/commcal.F90:27-87), diagonal metrics: per direction the
 // largest of 0 and dxi(d,d)*u_d + sqrt(T)/mach*|dxi(d,d)| over the interior
 // nodes.  The maxima are non-negative, so their bit patterns order like the
@@ -961,6 +1089,19 @@ struct astr_ctx {
   struct V2U {
     double a1 = 0, a3 = 0, K[6] = {0, 0, 0, 0, 0, 0}, KD[5] = {0, 0, 0, 0, 0}, gp[33] = {}, hp[33] = {};
   } v2ud[3], v2uf[3];
+  // crash control (lcracon, src/mainloop.F90:709-1198)
+  bool cracon = false, cc_started = false;
+  double* snap[2] = {nullptr, nullptr};  // 5 interior FP64 arrays + CHAN_N each
+  bool snap_valid[2] = {false, false};
+  long long snap_nstep[2] = {0, 0};
+  int snap_rec[2] = {0, 0};              // recover_counter of each snapshot
+  int datpnt = -1;                       // -1: none yet ('o'), 0: 'a', 1: 'b'
+  long long nxtbakup = 0, feqbakup = 5;
+  unsigned char* crinod = nullptr;       // critical nodes (interior)
+  unsigned char* crinod2 = nullptr;      // expansion scratch
+  unsigned char* fixflag = nullptr;      // crashfix: flagged nodes of the pass
+  unsigned long long* fixcount = nullptr;  // crashfix: [flagged, wiped] of the pass
+  long long recoveries = 0, backups = 0, wiped = 0;
   // compact MP convective scheme (conschm 543c): scratch and schemes
   bool mp = false;
   MPDev mpd{};
@@ -1402,6 +1543,22 @@ int run_mpconv(astr_ctx* c) {
   return ASTR_OK;
 }
 
+// crashfix after each stage's primitive recovery (lcracon,
+// src/mainloop.F90:486): floors eps_rho = eps_tmp = 1e-5 and eps_prs =
+// thermal(eps_rho, eps_tmp) = eps_rho eps_tmp / const2 (nondimensional).
+template <typename T>
+int run_crashfix(astr_ctx* c) {
+  const double eps = 1e-5;
+  CK(cudaMemsetAsync(c->fixcount, 0, sizeof(unsigned long long), c->st));
+  prof_begin(c, KC_POINT);
+  k_crashfix_flag<T><<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, dev<T>(c), eps, eps * eps / c->ph.const2,
+                                                             eps, c->fixflag, c->crinod, c->fixcount);
+  prof_end(c);
+  RC(after_launch(c, "k_crashfix_flag"));
+  k_crashfix_apply<T><<<1, 256, 0, c->st>>>(c->g, dev<T>(c), c->ph, c->fixflag, c->fixcount);
+  return after_launch(c, "k_crashfix_apply");
+}
+
 template <typename T>
 int one_step(astr_ctx* c, double* stats) {
   const bool mini = c->pm.order == ASTR_ORDER_MINIAPP;
@@ -1438,6 +1595,7 @@ int one_step(astr_ctx* c, double* stats) {
       if (c->channel) RC(run_chan<T>(c, st1));
       if (visc) RC(run_visc<T>(c, !split_rk, !split_rk));
       if (!visc || split_rk) RC(rk_pointwise<T>(c, 1));
+      if (c->cracon) RC(run_crashfix<T>(c));
     }
     if (st1 && stats) RC(stats_finish(c, stats));
   }
@@ -2299,9 +2457,114 @@ static int ready(astr_ctx* c) {
   return ASTR_OK;
 }
 
+// databakup (src/mainloop.F90:824-972), device side: backup copies the
+// interior conserved state and the channel controller into the snapshot
+// datpnt points at and moves datpnt to the other one; recovery restores the
+// snapshot datpnt points at (the older of two), moves datpnt, recovers the
+// primitives (updatefvar) and, from the second recovery from the same
+// snapshot on, expands the critical nodes (crinod_expansion).  With a
+// single snapshot taken, datpnt points at the empty one, which the
+// reference would read unallocated; the one snapshot taken is used.
+static int databakup(astr_ctx* c, int recovery) {
+  const size_t n0 = (size_t)c->g.n0;
+  const size_t bytes = 5 * n0 * sizeof(double);
+  if (!recovery) {
+    const int slot = c->datpnt < 0 ? 0 : c->datpnt;
+    if (c->prec == ASTR_FP64)
+      k_snap_save<double><<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, c->d64, c->snap[slot]);
+    else
+      k_snap_save<float><<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, c->d32, c->snap[slot]);
+    RC(after_launch(c, "k_snap_save"));
+    if (c->chan_dev)
+      CK(cudaMemcpyAsync(c->snap[slot] + 5 * n0, c->chan_dev, CHAN_N * sizeof(double),
+                         cudaMemcpyDeviceToDevice, c->st));
+    c->snap_valid[slot] = true;
+    c->snap_nstep[slot] = c->nstep;
+    c->snap_rec[slot] = 0;
+    c->datpnt = 1 - slot;
+    c->backups += 1;
+    return ASTR_OK;
+  }
+  if (c->datpnt < 0 || (!c->snap_valid[0] && !c->snap_valid[1]))
+    return fail(c, ASTR_ERR_NONFINITE, "crash with no backup data available (databakup)");
+  int slot = c->datpnt;
+  if (!c->snap_valid[slot]) slot = 1 - slot;
+  if (c->prec == ASTR_FP64)
+    k_snap_load<double><<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, c->d64, c->snap[slot]);
+  else
+    k_snap_load<float><<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, c->d32, c->snap[slot]);
+  RC(after_launch(c, "k_snap_load"));
+  if (c->chan_dev)
+    CK(cudaMemcpyAsync(c->chan_dev, c->snap[slot] + 5 * n0, CHAN_N * sizeof(double),
+                       cudaMemcpyDeviceToDevice, c->st));
+  (void)bytes;
+  c->nstep = c->snap_nstep[slot];
+  c->snap_rec[slot] += 1;
+  c->datpnt = 1 - slot;
+  c->recoveries += 1;
+  if (c->prec == ASTR_FP64)
+    k_updatefvar<double><<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, c->d64, c->ph);
+  else
+    k_updatefvar<float><<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, c->d32, c->ph);
+  RC(after_launch(c, "k_updatefvar"));
+  if (c->snap_rec[slot] > 1) {
+    k_crinod_expand<<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, c->crinod, c->crinod2);
+    RC(after_launch(c, "k_crinod_expand"));
+    std::swap(c->crinod, c->crinod2);
+  }
+  CK(cudaMemsetAsync(c->d64.flag, 0, sizeof(int), c->st));
+  return ASTR_OK;
+}
+
+// crashcheck before a step (src/mainloop.F90:709-812, called at the top of
+// steploop's loop, 103-110) with lcracon: a crashed state (q1 >= 0 fails at
+// some node) is marked critical and rolled back; otherwise the state is
+// backed up when nstep reaches nxtbakup, whose interval then doubles up to
+// 500 steps.  Returns 1 in *recovered when it rolled back.
+static int crash_control_step(astr_ctx* c, int* recovered) {
+  *recovered = 0;
+  if (!c->cc_started) {
+    c->nxtbakup = c->nstep + c->feqbakup;  // steploop's set-up (src/mainloop.F90:90)
+    c->cc_started = true;
+  }
+  long long ncrash = 0;
+  RC(astr_gpu_crashcheck(c, &ncrash, nullptr));
+  if (ncrash > 0) {
+    if (c->prec == ASTR_FP64)
+      k_crinod_mark<double><<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, c->d64, c->crinod);
+    else
+      k_crinod_mark<float><<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, c->d32, c->crinod);
+    RC(after_launch(c, "k_crinod_mark"));
+    RC(databakup(c, 1));
+    *recovered = 1;
+  } else if (c->nstep == c->nxtbakup) {
+    RC(databakup(c, 0));
+    c->nxtbakup = c->nstep + c->feqbakup;
+    c->feqbakup = std::min<long long>(500, 2 * c->feqbakup);
+  }
+  return ASTR_OK;
+}
+
 int astr_gpu_rk3_step(astr_ctx* c, int nsteps, double* hist, astr_status* status) {
   RC(ready(c));
   if (nsteps < 0) return fail(c, ASTR_ERR_ARG, "nsteps < 0");
+  if (c->cracon) {
+    // crash control: crashcheck / databakup before every step, crashfix
+    // after every stage; a rollback is reported in status->crash
+    int any = 0;
+    for (int s = 0; s < nsteps; ++s) {
+      int rec = 0;
+      RC(crash_control_step(c, &rec));
+      any |= rec;
+      RC(step(c, hist ? hist + 2 * s : nullptr));
+    }
+    if (status) {
+      status->crash = any;
+      status->kenergy = hist && nsteps > 0 ? hist[2 * (nsteps - 1)] : 0.0;
+      status->enstrophy = hist && nsteps > 0 ? hist[2 * (nsteps - 1) + 1] : 0.0;
+    }
+    return ASTR_OK;
+  }
   for (int s = 0; s < nsteps; ++s) RC(step(c, hist ? hist + 2 * s : nullptr));
   if (status) {
     int flag = 0;
@@ -2349,6 +2612,78 @@ int astr_gpu_updatefvar(astr_ctx* c) {
   else
     k_updatefvar<float><<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, c->d32, c->ph);
   return after_launch(c, "k_updatefvar");
+}
+
+int astr_gpu_set_crash_control(astr_ctx* c, int on) {
+  if (!c) return fail(c, ASTR_ERR_ARG, "null context");
+  if (on && c->pm.order != ASTR_ORDER_MAIN)
+    return fail(c, ASTR_ERR_UNSUPPORTED, "crash control belongs to the main solver ordering");
+  if (on && !c->snap[0]) {
+    const size_t n0 = (size_t)c->g.n0;
+    auto alloc = [&](size_t bytes) -> void* {
+      void* p = nullptr;
+      if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
+      c->allocs.push_back(p);
+      return p;
+    };
+    c->snap[0] = (double*)alloc((5 * n0 + CHAN_N) * sizeof(double));
+    c->snap[1] = (double*)alloc((5 * n0 + CHAN_N) * sizeof(double));
+    c->crinod = (unsigned char*)alloc(n0);
+    c->crinod2 = (unsigned char*)alloc(n0);
+    c->fixflag = (unsigned char*)alloc(n0);
+    c->fixcount = (unsigned long long*)alloc(2 * sizeof(unsigned long long));
+    if (!c->snap[0] || !c->snap[1] || !c->crinod || !c->crinod2 || !c->fixflag || !c->fixcount)
+      return fail(c, ASTR_ERR_OOM, "crash control: device allocation failed");
+    CK(cudaMemset(c->crinod, 0, n0));
+    CK(cudaMemset(c->fixcount, 0, 2 * sizeof(unsigned long long)));
+  }
+  c->cracon = on != 0;
+  return ASTR_OK;
+}
+
+int astr_gpu_databakup(astr_ctx* c, int mode, long long* nstep) {
+  RC(ready(c));
+  if (!c->snap[0]) return fail(c, ASTR_ERR_STATE, "crash control not enabled (astr_gpu_set_crash_control)");
+  if (mode != 0 && mode != 1) return fail(c, ASTR_ERR_ARG, "mode: 0 backup, 1 recovery");
+  RC(databakup(c, mode));
+  CK(cudaStreamSynchronize(c->st));
+  if (nstep) *nstep = c->nstep;
+  return ASTR_OK;
+}
+
+int astr_gpu_crashfix(astr_ctx* c, long long* wiped) {
+  RC(ready(c));
+  if (!c->snap[0]) return fail(c, ASTR_ERR_STATE, "crash control not enabled (astr_gpu_set_crash_control)");
+  unsigned long long before[2];
+  CK(cudaMemcpyAsync(before, c->fixcount, sizeof(before), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  RC(c->prec == ASTR_FP64 ? run_crashfix<double>(c) : run_crashfix<float>(c));
+  unsigned long long after[2];
+  CK(cudaMemcpyAsync(after, c->fixcount, sizeof(after), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  if (wiped) *wiped = (long long)(after[1] - before[1]);
+  return ASTR_OK;
+}
+
+int astr_gpu_crash_report(astr_ctx* c, long long* out6) {
+  if (!c || !out6) return fail(c, ASTR_ERR_ARG, "null argument");
+  for (int m = 0; m < 6; ++m) out6[m] = 0;
+  out6[0] = c->recoveries;
+  out6[1] = c->backups;
+  out6[4] = c->nstep;
+  out6[5] = c->cracon ? c->nxtbakup : -1;
+  if (c->snap[0]) {
+    unsigned long long cnt[2];
+    CK(cudaMemcpyAsync(cnt, c->fixcount, sizeof(cnt), cudaMemcpyDeviceToHost, c->st));
+    std::vector<unsigned char> m((size_t)c->g.n0);
+    CK(cudaMemcpyAsync(m.data(), c->crinod, m.size(), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    out6[2] = (long long)cnt[1];
+    long long n = 0;
+    for (unsigned char v : m) n += v ? 1 : 0;
+    out6[3] = n;
+  }
+  return ASTR_OK;
 }
 
 int astr_gpu_reduce_stats(astr_ctx* c, double* ke, double* en) {
@@ -2426,6 +2761,8 @@ int astr_gpu_step_async(astr_ctx* c, int nsteps) {
   if (c->channel)
     return fail(c, ASTR_ERR_UNSUPPORTED, "a channel step depends on host counters; use astr_gpu_rk3_step");
   if (c->prof) return fail(c, ASTR_ERR_STATE, "profiling is on");
+  if (c->cracon)
+    return fail(c, ASTR_ERR_UNSUPPORTED, "crash control decides on the host before each step; use astr_gpu_rk3_step");
   if (nsteps == 0) return ASTR_OK;
   if (!c->step_graph) {
     // capture one step (no statistics, no host synchronisation inside)

@@ -195,6 +195,29 @@ class GpuSolver:
         self._c(self.L.astr_gpu_crashcheck(self.h, ctypes.byref(n), ijk))
         return n.value, (tuple(ijk) if n.value else None)
 
+    def set_crash_control(self, on: bool = True):
+        """lcracon: crashcheck / databakup before every step and crashfix
+        after every stage of time_integration_rk (src/mainloop.F90:709-1198)."""
+        self._c(self.L.astr_gpu_set_crash_control(self.h, 1 if on else 0))
+
+    def databakup(self, mode: str) -> int:
+        """databakup('backup' or 'recovery'); returns nstep after the call."""
+        n = ctypes.c_longlong()
+        self._c(self.L.astr_gpu_databakup(self.h, {"backup": 0, "recovery": 1}[mode], ctypes.byref(n)))
+        return n.value
+
+    def crashfix(self) -> int:
+        """One crashfix pass; returns the number of nodes it replaced."""
+        n = ctypes.c_longlong()
+        self._c(self.L.astr_gpu_crashfix(self.h, ctypes.byref(n)))
+        return n.value
+
+    def crash_report(self) -> dict:
+        out = (ctypes.c_longlong * 6)()
+        self._c(self.L.astr_gpu_crash_report(self.h, out))
+        keys = ("rollbacks", "backups", "wiped", "critical_nodes", "nstep", "next_backup")
+        return dict(zip(keys, (int(v) for v in out)))
+
     def cflcal(self, deltat: float):
         """(CFL number of the resident state at this time step, (Di, Dj, Dk))
         — cflcal, src/commcal.F90:27-87."""

@@ -155,6 +155,31 @@ int astr_gpu_poll(astr_ctx* ctx);
  * first such node (i fastest), or -1s.  The state is not modified. */
 int astr_gpu_crashcheck(astr_ctx* ctx, long long* ncrash, int* ijk);
 
+/* Crash control (lcracon; src/mainloop.F90:709-1198), main ordering.  On:
+ * astr_gpu_rk3_step runs crashcheck before every step, rolling a crashed
+ * state back to the older of two snapshots kept in HBM (databakup's
+ * 'recovery', which restores nstep and the channel controller, recovers the
+ * primitives and, from the second rollback to the same snapshot on, expands
+ * the critical-node mask by one node: crinod_expansion) and otherwise taking
+ * a snapshot when nstep reaches the next backup step (first after 5 steps,
+ * the interval doubling up to 500: databakup's 'backup'); after every stage
+ * it runs crashfix.  A rollback is reported in status->crash and is not an
+ * error.  Enabling allocates two snapshots (80 bytes per stored node) and
+ * three byte masks; astr_gpu_step_async refuses while it is on. */
+int astr_gpu_set_crash_control(astr_ctx* ctx, int on);
+/* databakup (src/mainloop.F90:824-972) on demand: mode 0 backup, 1 recovery
+ * (*nstep, may be NULL, receives the step count after the call).  Needs
+ * crash control to have been enabled once (the snapshots). */
+int astr_gpu_databakup(astr_ctx* ctx, int mode, long long* nstep);
+/* crashfix (src/mainloop.F90:1045-1198), one pass: every interior node with
+ * rho, p or T below its floor (1e-5, 1e-5, and p of those) takes the mean q
+ * of its neighbours with non-negative rho, p and T, node by node in the
+ * reference's loop order; *wiped (may be NULL) receives the nodes replaced. */
+int astr_gpu_crashfix(astr_ctx* ctx, long long* wiped);
+/* Counters of crash control: out6 = {rollbacks, backups, nodes wiped by
+ * crashfix, critical nodes (crinod), nstep, next backup step or -1}. */
+int astr_gpu_crash_report(astr_ctx* ctx, long long* out6);
+
 /* cflcal (src/commcal.F90:27-87) on the resident state: *cfl = deltat *
  * (Di + Dj + Dk), D the largest of 0 and the contravariant velocity plus
  * sound speed (sqrt(T)/mach) along each computational direction over the
