@@ -139,14 +139,53 @@ __global__ void k_sigma(Geo g, DevT<T> d, Phys ph) {
   sigma_point(g, d, ph, idx, hidx(g, i, j, k));
 }
 
+// RK3 update of the five variables at one point (and q2fvar): every
+// operand is read before anything is written, so the loads of the point
+// are in flight together; the primitives come from the stored (storage
+// precision) values, as q2fvar_store reads them.
 template <typename T>
 __global__ void k_rkupdate(Geo g, DevT<T> d, Phys ph, int q2f) {
   int i, j, k;
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (!point_of(g, idx, i, j, k)) return;
-  const long long p = hidx(g, i, j, k);
-  for (int m = 0; m < 5; ++m) rk_update(g, d, ph, p, idx, m, (double)d.qrhs[m * g.n0 + idx]);
-  if (q2f) q2fvar_store(g, d, ph, p);
+  const long long p = hidx(g, i, j, k), nh = g.nh, n0 = g.n0;
+  T rhs[5];
+  double qs[5], qv[5];
+#pragma unroll
+  for (int m = 0; m < 5; ++m) {
+    rhs[m] = d.qrhs[m * n0 + idx];
+    qs[m] = d.qsave[m * n0 + idx];
+    qv[m] = q64(d, p, idx, m, nh, n0);
+  }
+  const double J = d.jac64[p], rj = d.rjac64[p];
+  T qn[5];
+  // FP32 storage: the same update with fewer FP64 operations (the FP64
+  // pipe bounds this kernel on GB300): rk2*J once per point, rk3*dt folded
+  // on the host, the small term rk3*dt*rhs (rhs is stored in FP32) formed
+  // in FP32, multiply-adds; the FP64 form keeps the reference's order
+  const double c2J = ph.rk2 * J;
+#pragma unroll
+  for (int m = 0; m < 5; ++m) {
+    double v;
+    if (sizeof(T) == 4 && !ph.mini && !d.chan)
+      v = fma(ph.rk1, qs[m], fma(c2J, qv[m], (double)((float)ph.rk3dt * (float)rhs[m]))) * rj;
+    else
+      v = rk_value(ph, d.chan, m, qs[m], qv[m], (double)rhs[m], J, rj);
+    qn[m] = (T)v;
+    d.q[m * nh + p] = qn[m];
+    if (d.qm) d.qm[m * n0 + idx] = v;
+  }
+  if (q2f) {
+    T ro, u, v, w, pp, tt;
+    q2fvar_pt<T>(ph, qn[0], qn[1], qn[2], qn[3], qn[4], ro, u, v, w, pp, tt);
+    d.pr[p] = ro;
+    d.pr[p + nh] = u;
+    d.pr[p + 2 * nh] = v;
+    d.pr[p + 3 * nh] = w;
+    d.pr[p + 4 * nh] = pp;
+    d.pr[p + 5 * nh] = tt;
+    if (!(ro > T(0))) atomicOr(d.flag, 1);
+  }
 }
 
 // RK3 base at stage 1 (src/mainloop.F90:427-433): q*J (mini-app: q), in
@@ -1408,6 +1447,7 @@ void set_stage(astr_ctx* c, int s) {
   c->ph.rk1 = rk[s][0];
   c->ph.rk2 = rk[s][1];
   c->ph.rk3 = rk[s][2];
+  c->ph.rk3dt = rk[s][2] * c->ph.dt;
 }
 
 template <typename T>

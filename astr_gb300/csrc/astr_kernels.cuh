@@ -138,6 +138,7 @@ struct Phys {
   double tempconst, tempconst1, rreynolds;
   double dt;
   double rk1, rk2, rk3;
+  double rk3dt;   // rk3 * dt (the FP32-storage form's update)
   double rdx[3];  // mini-app reciprocal spacings
   // the same constants rounded to FP32 once, for the FP32 sweeps
   float f_const2, f_rconst6, f_hcc_scale, f_tempconst, f_tempconst1, f_rreynolds;
@@ -744,25 +745,29 @@ __device__ __forceinline__ double q64(const DevT<float>& d, long long p, long lo
 // RK3 stage update (src/mainloop.F90:441-451) of variable m at one point.
 // Main ordering: q = (rk1*qsave + rk2*q*J + rk3*dt*rhs)/J, the division a
 // multiplication by the stored 1/J; mini-app ordering: no Jacobian.
-template <typename T>
-__device__ __forceinline__ void rk_update(const Geo& g, const DevT<T>& d, const Phys& ph,
-                                          long long p, long long z, int m, double rhs) {
-  const long long nh = g.nh, n0 = g.n0;
-  const double J = d.jac64[p], rj = d.rjac64[p];
-  const double qv = q64(d, p, z, m, nh, n0);
-  const double qs = d.qsave[m * n0 + z];
-  double v;
-  if (d.chan) {
+// The updated value from its operands (qs: RK3 base, qv: current q, rhs:
+// residual, J and 1/J; chan: the channel controller or null).
+__device__ __forceinline__ double rk_value(const Phys& ph, const double* chan, int m, double qs,
+                                           double qv, double rhs, double J, double rj) {
+  if (chan) {
     // src_chan (src/solver.F90:335-346): body force and its work, times J
-    const double* C = d.chan;
+    const double* C = chan;
     const double f = m == 0 ? 0.0
                    : (m < 4 ? C[CHAN_FORCE + m - 1]
                             : C[CHAN_FORCE] * C[CHAN_UBULK] + C[CHAN_FORCE + 1] * C[CHAN_UBULK + 1] +
                                   C[CHAN_FORCE + 2] * C[CHAN_UBULK + 2]);
     rhs = rhs + f * J;
   }
-  if (ph.mini) v = ph.rk1 * qs + ph.rk2 * qv + ph.rk3 * rhs * ph.dt;
-  else v = (ph.rk1 * qs + ph.rk2 * qv * J + ph.rk3 * rhs * ph.dt) * rj;
+  if (ph.mini) return ph.rk1 * qs + ph.rk2 * qv + ph.rk3 * rhs * ph.dt;
+  return (ph.rk1 * qs + ph.rk2 * qv * J + ph.rk3 * rhs * ph.dt) * rj;
+}
+
+template <typename T>
+__device__ __forceinline__ void rk_update(const Geo& g, const DevT<T>& d, const Phys& ph,
+                                          long long p, long long z, int m, double rhs) {
+  const long long nh = g.nh, n0 = g.n0;
+  const double J = d.jac64[p], rj = d.rjac64[p];
+  const double v = rk_value(ph, d.chan, m, d.qsave[m * n0 + z], q64(d, p, z, m, nh, n0), rhs, J, rj);
   d.q[m * nh + p] = (T)v;
   if (d.qm) d.qm[m * n0 + z] = v;
 }
