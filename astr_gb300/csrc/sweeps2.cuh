@@ -480,7 +480,7 @@ k2_filter(Geo g, DevT<T> d, DScheme<T> S, UCo<T, CH> U, FTab<T> Tb, int P) {
 #pragma unroll
       for (int k = 0; k < CH; ++k) {
         const int node = slot_node(k);
-        am[k] = (node >= 0 && M) ? M[zs * node] : 0.0;
+        am[delta ? k : 0] = (node >= 0 && M) ? M[zs * node] : 0.0;
       }
     }
     solve2<CH>(y, S, U, c, scan, uni);
@@ -565,14 +565,14 @@ k2_convgrad(Geo g, DevT<T> d, DScheme<T> S, UCo<T, CH> U, CGFlags fl, int P) {
       const int row = sm_.row0 + 32 * k;
       const int nd = first - R + row;
       T A = T(0), B = T(0), C = T(0);
-      if (sok && row < NRT && nd >= -HMD && nd <= dim + HMD) {
+      if (sok && (k < E - 1 || row < NRT) && nd >= -HMD && nd <= dim + HMD) {
         const int p = shb + hs * nd;
         const T u = ud[p], pv = pp[p], x = xdd[p], J = jj[p];
         A = J * (x * u);
         B = J * (x * pv);
         C = pv * A;
       }
-      if (row < NRT) {
+      if (k < E - 1 || row < NRT) {
         const int w = tw<DIR, NL>(sm_.line, row, P);
         tA[w] = A;
         tB[w] = B;
@@ -594,7 +594,7 @@ k2_convgrad(Geo g, DevT<T> d, DScheme<T> S, UCo<T, CH> U, CGFlags fl, int P) {
       const int row = sm_.row0 + 32 * k;
       const int nd = first - R + row;
       const bool ok = sok && nd >= -HMD && nd <= dim + HMD;
-      if (row < NRT) cp_async_elem(bf + tw<DIR, NL>(sm_.line, row, P), ok ? v + hs * nd : v, ok);
+      if (k < E - 1 || row < NRT) cp_async_elem(bf + tw<DIR, NL>(sm_.line, row, P), ok ? v + hs * nd : v, ok);
     }
     cp_async_commit();
   };
@@ -606,7 +606,7 @@ k2_convgrad(Geo g, DevT<T> d, DScheme<T> S, UCo<T, CH> U, CGFlags fl, int P) {
 #pragma unroll
       for (int k = 0; k < E; ++k) {
         const int row = sm_.row0 + 32 * k;
-        if (row < NRT) {
+        if (k < E - 1 || row < NRT) {
           const int w = tw<DIR, NL>(sm_.line, row, P);
           const T v = bf[w];
           if (t == 1 + DIR) bf[w] = fma(v, tA[w], tB[w]);
@@ -729,11 +729,11 @@ k2_visc(Geo g, DevT<T> d, DScheme<T> S, UCo<T, CH> U, int P) {
       const int row = sm_.row0 + 32 * k;
       const int nd = first - R + row;
       T F = T(0);
-      if (sok && row < NRT && nd >= -HMD && nd <= dim + HMD) {
+      if (sok && (k < E - 1 || row < NRT) && nd >= -HMD && nd <= dim + HMD) {
         const int p = shb + hs * nd;
         F = xdd[p] * d.jac[p];
       }
-      if (row < NRT) tF[tw<DIR, NL>(sm_.line, row, P)] = F;
+      if (k < E - 1 || row < NRT) tF[tw<DIR, NL>(sm_.line, row, P)] = F;
     }
   }
   constexpr int s0 = DIR == 0 ? 0 : (DIR == 1 ? 1 : 2);
@@ -750,7 +750,7 @@ k2_visc(Geo g, DevT<T> d, DScheme<T> S, UCo<T, CH> U, int P) {
       int nd = first - R + row;
       if (per) nd = nd < 0 ? nd + dim : (nd > dim ? nd - dim : nd);
       const bool ok = sok && nd >= 0 && nd <= dim;
-      if (row < NRT) cp_async_elem(bf + tw<DIR, NL>(sm_.line, row, P), ok ? v + zs * nd : v, ok);
+      if (k < E - 1 || row < NRT) cp_async_elem(bf + tw<DIR, NL>(sm_.line, row, P), ok ? v + zs * nd : v, ok);
     }
     cp_async_commit();
   };
@@ -760,7 +760,7 @@ k2_visc(Geo g, DevT<T> d, DScheme<T> S, UCo<T, CH> U, int P) {
 #pragma unroll
     for (int k = 0; k < E; ++k) {
       const int row = sm_.row0 + 32 * k;
-      if (row < NRT) {
+      if (k < E - 1 || row < NRT) {
         const int w = tw<DIR, NL>(sm_.line, row, P);
         bf[w] = bf[w] * tF[w];
       }
@@ -791,10 +791,17 @@ k2_visc(Geo g, DevT<T> d, DScheme<T> S, UCo<T, CH> U, int P) {
     // the residual the fluxes add to, read before the solve
     T* dst = d.qrhs + (size_t)(t + 1) * n0 + obz;
     T ar[CH];
+    const int n0c = first + c * CH;
+    const bool full = DIR != 0 && ook && n0c >= lo && c * CH + CH - 1 < S.n && n0c + CH - 1 <= hi;
+    if (full) {
 #pragma unroll
-    for (int k = 0; k < CH; ++k) {
-      const int node = slot_node(k);
-      ar[k] = node >= 0 ? dst[zs * node] : T(0);
+      for (int k = 0; k < CH; ++k) ar[k] = dst[zs * (n0c + k)];
+    } else {
+#pragma unroll
+      for (int k = 0; k < CH; ++k) {
+        const int node = slot_node(k);
+        ar[k] = node >= 0 ? dst[zs * node] : T(0);
+      }
     }
     solve2<CH>(y, S, U, c, scan, uni);
     if (DIR == 0) {
@@ -802,13 +809,18 @@ k2_visc(Geo g, DevT<T> d, DScheme<T> S, UCo<T, CH> U, int P) {
       for (int k = 0; k < CH; ++k) bc[tw<DIR, NL>(ol, c * CH + k, P)] = y[k];
       __syncthreads();
     }
+    if (full) {
 #pragma unroll
-    for (int k = 0; k < CH; ++k) {
-      const int node = slot_node(k);
-      if (node >= 0) {
-        const T val = DIR == 0 ? bc[tw<DIR, NL>(sm_.line, node - first, P)] : y[k];
-        const bool in = node >= lo && node <= hi;
-        dst[zs * node] = ar[k] + (in ? val : T(0));
+      for (int k = 0; k < CH; ++k) dst[zs * (n0c + k)] = ar[k] + y[k];
+    } else {
+#pragma unroll
+      for (int k = 0; k < CH; ++k) {
+        const int node = slot_node(k);
+        if (node >= 0) {
+          const T val = DIR == 0 ? bc[tw<DIR, NL>(sm_.line, node - first, P)] : y[k];
+          const bool in = node >= lo && node <= hi;
+          dst[zs * node] = ar[k] + (in ? val : T(0));
+        }
       }
     }
     if (more) finish(buf0 + (cur ^ 1) * TWd);
