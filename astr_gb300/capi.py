@@ -22,6 +22,8 @@ ASTR_ERR_CUDA = -3
 ASTR_ERR_UNSUPPORTED = -4
 ASTR_ERR_NONFINITE = -5
 ASTR_ERR_STATE = -6
+ASTR_ERR_TIMEOUT = -7
+ASTR_ERR_CANCELLED = -8
 
 ORDER_MAIN = 0
 ORDER_MINIAPP = 1
@@ -43,6 +45,10 @@ EXPORTS = [
     "astr_gpu_boucon", "astr_gpu_step_async", "astr_gpu_poll", "astr_gpu_crashcheck",
     "astr_gpu_cflcal", "astr_gpu_upload_q", "astr_gpu_set_crash_control", "astr_gpu_databakup",
     "astr_gpu_crashfix", "astr_gpu_crash_report",
+    "astr_batch_create", "astr_batch_destroy", "astr_batch_add", "astr_batch_remove",
+    "astr_batch_size", "astr_batch_step_async", "astr_batch_poll", "astr_batch_wait",
+    "astr_batch_cancel", "astr_batch_step", "astr_batch_last_error", "astr_batch_launch_count",
+    "astr_batch_set_share",
 ]
 NOALLOC_STATS_MAX_BLOCKS = 65536
 KERNEL_CLASSES = ["filter", "halo", "convgrad", "visc", "pointwise", "stats", "mp"]
@@ -151,6 +157,28 @@ def load(path: str = LIB_PATH):
     L.astr_gpu_set_grid.restype = ip
     L.astr_gpu_channel_state.argtypes = [vp, dp]
     L.astr_gpu_channel_state.restype = ip
+    L.astr_batch_create.argtypes = [ip, ctypes.POINTER(vp)]
+    L.astr_batch_create.restype = ip
+    L.astr_batch_destroy.argtypes = [vp]
+    L.astr_batch_destroy.restype = None
+    for n in ("astr_batch_add", "astr_batch_remove"):
+        getattr(L, n).argtypes = [vp, vp]
+        getattr(L, n).restype = ip
+    for n in ("astr_batch_size", "astr_batch_poll", "astr_batch_cancel"):
+        getattr(L, n).argtypes = [vp]
+        getattr(L, n).restype = ip
+    L.astr_batch_set_share.argtypes = [vp, ctypes.c_double]
+    L.astr_batch_set_share.restype = ip
+    L.astr_batch_step_async.argtypes = [vp, ip, ctypes.c_double]
+    L.astr_batch_step_async.restype = ip
+    L.astr_batch_wait.argtypes = [vp, ctypes.POINTER(ip)]
+    L.astr_batch_wait.restype = ip
+    L.astr_batch_step.argtypes = [vp, ip, ctypes.c_double, ctypes.POINTER(ip)]
+    L.astr_batch_step.restype = ip
+    L.astr_batch_last_error.argtypes = [vp, ctypes.c_char_p, ip]
+    L.astr_batch_last_error.restype = ip
+    L.astr_batch_launch_count.argtypes = [vp]
+    L.astr_batch_launch_count.restype = ctypes.c_longlong
     for n in ("astr_gpu_set_metrics", "astr_gpu_upload_state", "astr_gpu_download_state",
               "astr_gpu_download_rhs", "astr_gpu_rk3_step", "astr_gpu_reduce_stats"):
         getattr(L, n).restype = ip
@@ -202,3 +230,88 @@ def check(h, rc: int):
     if rc != ASTR_OK:
         raise AstrError(rc, last_error(h))
     return rc
+
+
+def batch_error(b) -> str:
+    L = load()
+    buf = ctypes.create_string_buffer(1024)
+    L.astr_batch_last_error(b, buf, 1024)
+    return buf.value.decode(errors="replace")
+
+
+class Batch:
+    """A batch of cases stepped together (astr_batch_*): one launch per phase
+    of an RK3 stage covers every case; each case advances as it would alone.
+
+    Cases are GpuSolver objects (or anything with a context handle ``h``)."""
+
+    def __init__(self, precision: int = FP32_STORAGE):
+        L = load()
+        self.L = L
+        h = ctypes.c_void_p()
+        rc = L.astr_batch_create(precision, ctypes.byref(h))
+        if rc != ASTR_OK:
+            raise AstrError(rc, last_error(None))
+        self.h = h
+        self.members = []
+
+    def _c(self, rc: int):
+        if rc != ASTR_OK:
+            raise AstrError(rc, batch_error(self.h))
+        return rc
+
+    def add(self, case):
+        self._c(self.L.astr_batch_add(self.h, case.h))
+        self.members.append(case)
+
+    def remove(self, case):
+        self._c(self.L.astr_batch_remove(self.h, case.h))
+        self.members.remove(case)
+
+    def __len__(self):
+        return self.L.astr_batch_size(self.h)
+
+    def set_share(self, share: float):
+        """Fraction (0, 1] of the GPU's resident blocks a launch takes."""
+        self._c(self.L.astr_batch_set_share(self.h, float(share)))
+
+    def step_async(self, nsteps: int, budget_ms: float = 0.0):
+        self._c(self.L.astr_batch_step_async(self.h, nsteps, budget_ms))
+
+    def poll(self) -> bool:
+        rc = self.L.astr_batch_poll(self.h)
+        if rc < 0:
+            self._c(rc)
+        return rc == 1
+
+    def wait(self):
+        """(code, steps_done): code is ASTR_OK, ASTR_ERR_TIMEOUT or
+        ASTR_ERR_CANCELLED; other errors raise."""
+        n = ctypes.c_int(0)
+        rc = self.L.astr_batch_wait(self.h, ctypes.byref(n))
+        if rc not in (ASTR_OK, ASTR_ERR_TIMEOUT, ASTR_ERR_CANCELLED):
+            self._c(rc)
+        return rc, n.value
+
+    def step(self, nsteps: int, budget_ms: float = 0.0):
+        self.step_async(nsteps, budget_ms)
+        return self.wait()
+
+    def cancel(self):
+        self._c(self.L.astr_batch_cancel(self.h))
+
+    @property
+    def launches(self) -> int:
+        return self.L.astr_batch_launch_count(self.h)
+
+    def close(self):
+        if self.h:
+            self.L.astr_batch_destroy(self.h)
+            self.h = None
+            self.members = []
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -39,10 +39,9 @@ namespace {
 // Halo kernels
 // ---------------------------------------------------------------------------
 template <int DIR>
-__device__ __forceinline__ bool face_line(const Geo& g, int& dim, long long& base, long long& hs,
-                                          long long* zbase = nullptr, long long* zs = nullptr) {
-  const int a = blockIdx.x * blockDim.x + threadIdx.x;
-  const int b = blockIdx.y;
+__device__ __forceinline__ bool face_line_at(const Geo& g, int a, int b, int& dim, long long& base,
+                                             long long& hs, long long* zbase = nullptr,
+                                             long long* zs = nullptr) {
   const int na = DIR == 0 ? g.jm : g.im;
   if (a > na) return false;
   dim = DIR == 0 ? g.im : (DIR == 1 ? g.jm : g.km);
@@ -54,14 +53,19 @@ __device__ __forceinline__ bool face_line(const Geo& g, int& dim, long long& bas
   if (zs) *zs = zstride<DIR>(g);
   return true;
 }
+template <int DIR>
+__device__ __forceinline__ bool face_line(const Geo& g, int& dim, long long& base, long long& hs,
+                                          long long* zbase = nullptr, long long* zs = nullptr) {
+  return face_line_at<DIR>(g, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y, dim, base, hs, zbase, zs);
+}
 
 // qswap single-rank periodic branch of one direction (src/parallel.F90:
 // 4876-4920, 5018-5065, 5159-5206).
 template <typename T, int DIR>
-__global__ void k_qswap(Geo g, DevT<T> d, Phys ph) {
+__device__ __forceinline__ void qswap_line(const Geo& g, const DevT<T>& d, const Phys& ph, int a, int b) {
   int dim;
   long long base, hs, zb, zs;
-  if (!face_line<DIR>(g, dim, base, hs, &zb, &zs)) return;
+  if (!face_line_at<DIR>(g, a, b, dim, base, hs, &zb, &zs)) return;
   for (int n = 0; n < 5; ++n) {
     T* v = d.q + n * g.nh + base;
     if (dim == 0) {
@@ -87,6 +91,10 @@ __global__ void k_qswap(Geo g, DevT<T> d, Phys ph) {
   }
   for (int l = -HMD; l <= 0; ++l) q2fvar_store(g, d, ph, base + hs * l);
   for (int l = dim; l <= dim + HMD; ++l) q2fvar_store(g, d, ph, base + hs * l);
+}
+template <typename T, int DIR>
+__global__ void k_qswap(Geo g, DevT<T> d, Phys ph) {
+  qswap_line<T, DIR>(g, d, ph, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y);
 }
 
 // bchomo of the mini-app, one direction (tgvsolver.F90:271-369).
@@ -144,9 +152,9 @@ __global__ void k_sigma(Geo g, DevT<T> d, Phys ph) {
 // are in flight together; the primitives come from the stored (storage
 // precision) values, as q2fvar_store reads them.
 template <typename T>
-__global__ void k_rkupdate(Geo g, DevT<T> d, Phys ph, int q2f) {
+__device__ __forceinline__ void rk_point(const Geo& g, const DevT<T>& d, const Phys& ph, int q2f,
+                                         long long idx) {
   int i, j, k;
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (!point_of(g, idx, i, j, k)) return;
   const long long p = hidx(g, i, j, k), nh = g.nh, n0 = g.n0;
   T rhs[5];
@@ -187,19 +195,107 @@ __global__ void k_rkupdate(Geo g, DevT<T> d, Phys ph, int q2f) {
     if (!(ro > T(0))) atomicOr(d.flag, 1);
   }
 }
+template <typename T>
+__global__ void k_rkupdate(Geo g, DevT<T> d, Phys ph, int q2f) {
+  rk_point(g, d, ph, q2f, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // RK3 base at stage 1 (src/mainloop.F90:427-433): q*J (mini-app: q), in
 // FP64 from the FP64 state or master.
 template <typename T>
-__global__ void k_qsave(Geo g, DevT<T> d, Phys ph) {
+__device__ __forceinline__ void qsave_point(const Geo& g, const DevT<T>& d, const Phys& ph, long long idx) {
   int i, j, k;
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (!point_of(g, idx, i, j, k)) return;
   const long long p = hidx(g, i, j, k);
   const double J = d.jac64[p];
   for (int m = 0; m < 5; ++m) {
     const double qv = q64(d, p, idx, m, g.nh, g.n0);
     d.qsave[m * g.n0 + idx] = ph.mini ? qv : qv * J;
+  }
+}
+template <typename T>
+__global__ void k_qsave(Geo g, DevT<T> d, Phys ph) {
+  qsave_point(g, d, ph, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// Shu-Osher RK3 coefficients of the three stages (src/mainloop.F90:350-366).
+__constant__ double c_rk[3][3] = {{1.0, 0.0, 1.0}, {0.75, 0.25, 0.25}, {1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0}};
+
+// The point and face kernels of a batched step, persistent over a work list
+// of (case, block) items: kind 0-2 qswap of direction kind (item: a block
+// of 256 face lines, line index), 3 RK3 base, 4 stress and heat flux, 5 RK3
+// update of stage `stage` with the primitives (item: KB_PPT x 256 points).
+// Same bodies as the single-case kernels.
+constexpr int KB_THREADS = 256;
+constexpr int KB_PPT = 8;
+constexpr int KB_PTS = KB_PPT * KB_THREADS;
+template <typename T>
+__global__ void __launch_bounds__(KB_THREADS)
+kb_point(const BCase<T>* cases, const int4* items, int nitems, int kind, int stage, BatchCtl ctl) {
+  __shared__ int stop;
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const int4 w = items[it];
+    if (threadIdx.x == 0) stop = batch_stopped(ctl);
+    __syncthreads();
+    if (stop) break;
+    const BCase<T>* C = cases + w.x;
+    const Geo g = C->g;
+    const DevT<T> d = C->d;
+    Phys ph = C->ph;
+    if (kind <= 2) {
+      const int a = w.y * KB_THREADS + threadIdx.x;
+      if (kind == 0) qswap_line<T, 0>(g, d, ph, a, w.z);
+      else if (kind == 1) qswap_line<T, 1>(g, d, ph, a, w.z);
+      else qswap_line<T, 2>(g, d, ph, a, w.z);
+    } else {
+      if (kind == 5) {
+        ph.rk1 = c_rk[stage][0];
+        ph.rk2 = c_rk[stage][1];
+        ph.rk3 = c_rk[stage][2];
+        ph.rk3dt = c_rk[stage][2] * ph.dt;
+      }
+      const long long base = (long long)w.y * KB_PTS + threadIdx.x;
+#pragma unroll 1
+      for (int r = 0; r < KB_PPT; ++r) {
+        const long long idx = base + r * KB_THREADS;
+        if (kind == 3) {
+          qsave_point(g, d, ph, idx);
+        } else if (kind == 4) {
+          int i, j, k;
+          if (point_of(g, idx, i, j, k)) sigma_point(g, d, ph, idx, hidx(g, i, j, k));
+        } else {
+          rk_point(g, d, ph, 1, idx);
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Start of a batched call: the deadline (budget_ns after now on the GPU's
+// global timer; 0: none), a clear status word and no steps started.
+__global__ void k_batch_start(BatchCtl ctl, unsigned long long* deadline, unsigned long long budget_ns) {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  *deadline = budget_ns ? t + budget_ns : 0ULL;
+  *ctl.status = 0;
+  *ctl.started = 0;
+}
+
+// Gate of one batched step: stop on the cancel word or a passed deadline,
+// else count the step as started.
+__global__ void k_batch_gate(BatchCtl ctl) {
+  int s = *(volatile int*)ctl.status;
+  if (!s) {
+    if (ctl.cancel && *ctl.cancel) s |= 1;
+    const unsigned long long dl = *ctl.deadline_ns;
+    if (dl) {
+      unsigned long long t;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+      if (t > dl) s |= 2;
+    }
+    if (s) *ctl.status = s;
+    else *ctl.started += 1;
   }
 }
 
@@ -1061,6 +1157,9 @@ thread_local std::string g_create_err;
 // ---------------------------------------------------------------------------
 // Context
 // ---------------------------------------------------------------------------
+struct astr_batch;
+static void batch_forget(astr_batch* b, astr_ctx* c);
+
 struct astr_ctx {
   astr_dims dm;
   astr_params pm;
@@ -1145,6 +1244,8 @@ struct astr_ctx {
   bool mp = false;
   MPDev mpd{};
   MPSchemes mps{};
+  // the batch this case belongs to (astr_batch_add), or none
+  astr_batch* batch = nullptr;
   // one RK3 step captured as a CUDA graph (asynchronous stepping)
   cudaGraphExec_t step_graph = nullptr;
   long long graph_kernels = 0;  // kernel launches in one captured step
@@ -2187,6 +2288,7 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
 
 void astr_gpu_destroy(astr_ctx* c) {
   if (!c) return;
+  if (c->batch) batch_forget(c->batch, c);
   if (c->st) cudaStreamSynchronize(c->st);
   if (c->step_graph) cudaGraphExecDestroy(c->step_graph);
   if (c->cst) cudaStreamSynchronize(c->cst);
@@ -2895,5 +2997,414 @@ int astr_gpu_measure_fp64_peak(double* tflops) {
   *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (best * 1e-3) / 1e12;
   return ASTR_OK;
 }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batches of cases (continuous batching; no counterpart in the reference)
+// ---------------------------------------------------------------------------
+// A batch steps many independent cases with one launch per phase of an RK3
+// stage: each persistent kernel walks a work list of (case, block) items
+// drawn from every case of the batch.  A case runs exactly the kernels, in
+// the order and with the arithmetic, that its own context issues for a step
+// on the tiled sweeps, so it advances bit for bit as it would alone.
+struct astr_batch {
+  int prec = ASTR_FP64;
+  int nsm = 152;
+  double share = 1.0;  // fraction of the GPU's resident blocks a launch takes
+  std::vector<astr_ctx*> cases;
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev_desc = nullptr;  // the descriptors of the last call copied
+  cudaEvent_t ev_done = nullptr;  // end of the last call
+  cudaEvent_t ev_in = nullptr;    // joins a case's stream into the batch stream
+  void* dcases = nullptr;         // BCase<T>[cases]
+  void* hcases = nullptr;         // page-locked staging of the descriptors
+  size_t desc_cap = 0;            // bytes of both
+  int4* ditems = nullptr;
+  size_t items_cap = 0;
+  // One launch of a step: op (filter, convective + gradient, viscous
+  // sweeps; qswap, RK3 base, stress, RK3 update point kernels), its
+  // direction and chunk length, and its items.
+  struct Phase {
+    int op, dir, CH;
+    int rep;      // a case whose uniform-chunk constants the launch takes
+    size_t off;
+    int n;
+    bool stage0;  // first stage only
+  };
+  std::vector<Phase> phases;
+  bool dirty = true;
+  int* dctl = nullptr;                  // device: status, steps started
+  unsigned long long* ddeadline = nullptr;
+  int* hword = nullptr;                 // mapped page-locked: cancel, status, started
+  int* hword_dev = nullptr;             // its device address
+  bool pending = false;
+  int result = ASTR_OK, result_steps = 0;
+  long long launches = 0;
+  std::string err;
+};
+
+namespace {
+
+enum { BOP_FILTER = 0, BOP_CONVGRAD = 1, BOP_VISC = 2, BOP_QSWAP, BOP_QSAVE, BOP_SIGMA, BOP_RK };
+
+int bfail(astr_batch* b, int code, const std::string& msg) {
+  b->err = msg;
+  return code;
+}
+
+#define BCK(call)                                                                          \
+  do {                                                                                     \
+    const cudaError_t _e = (call);                                                         \
+    if (_e != cudaSuccess)                                                                 \
+      return bfail(b, _e == cudaErrorMemoryAllocation ? ASTR_ERR_OOM : ASTR_ERR_CUDA,       \
+                   std::string(#call) + ": " + cudaGetErrorString(_e));                   \
+  } while (0)
+
+// Why a context cannot join a batch (empty: it can).
+std::string batch_refusal(const astr_ctx* c, int prec) {
+  if (c->prec != prec) return "the case's precision differs from the batch's";
+  if (c->pm.order != ASTR_ORDER_MAIN) return "batches run the main ordering only";
+  if (!use_v2(c))
+    return "the case does not run the tiled sweeps (general metrics, the MP scheme, FP64 without "
+           "ASTR_V2=2, or a line outside the tiled chunk lengths)";
+  if (c->channel) return "a channel step depends on host counters";
+  if (c->has_bc) return "batches run periodic cases only (boundary routines set)";
+  if (c->cracon) return "crash control decides on the host before each step";
+  if (c->prof) return "profiling is on";
+  if (!c->metrics_set || !c->state_set) return "metrics or state not set";
+  return std::string();
+}
+
+// The work lists of one step, every phase's items of all cases in a row.
+template <typename T>
+void batch_plan(astr_batch* b, std::vector<int4>& items) {
+  items.clear();
+  b->phases.clear();
+  const int NL = v2_nl<T>();
+  const int nc = (int)b->cases.size();
+  auto push = [&](int op, int dir, int CH, int rep, bool stage0, size_t off) {
+    const int n = (int)(items.size() - off);
+    if (n > 0) b->phases.push_back(astr_batch::Phase{op, dir, CH, rep, off, n, stage0});
+  };
+  // sweeps of one op and direction, one launch per chunk length and set of
+  // uniform-chunk constants (cases of one scheme share them)
+  auto sweep = [&](int op, int dir) {
+    auto takes = [&](const astr_ctx* c) {
+      return dir < c->g.ndims && (op != BOP_FILTER || c->pm.lfilter) && (op != BOP_VISC || c->pm.diffterm);
+    };
+    auto same = [&](const astr_ctx* a, const astr_ctx* c) {
+      const bool f = op == BOP_FILTER;
+      if ((f ? a->CHf[dir] : a->CH[dir]) != (f ? c->CHf[dir] : c->CH[dir])) return false;
+      const astr_ctx::V2U& ua = f ? a->v2uf[dir] : a->v2ud[dir];
+      const astr_ctx::V2U& uc = f ? c->v2uf[dir] : c->v2ud[dir];
+      return std::memcmp(&ua, &uc, sizeof(ua)) == 0;
+    };
+    std::vector<int> reps;
+    for (int i = 0; i < nc; ++i) {
+      if (!takes(b->cases[i])) continue;
+      bool found = false;
+      for (int r : reps) found = found || same(b->cases[r], b->cases[i]);
+      if (!found) reps.push_back(i);
+    }
+    for (int r : reps) {
+      const size_t off = items.size();
+      const int ch = op == BOP_FILTER ? b->cases[r]->CHf[dir] : b->cases[r]->CH[dir];
+      for (int i = 0; i < nc; ++i) {
+        const astr_ctx* c = b->cases[i];
+        if (!takes(c) || !same(b->cases[r], c)) continue;
+        int gx, gy;
+        v2_blocks(c->g, dir, NL, gx, gy);
+        const int nz = !c->vsplit ? 1 : (op == BOP_FILTER ? 5 : (op == BOP_CONVGRAD ? 9 : 4));
+        for (int z = 0; z < nz; ++z)
+          for (int y = 0; y < gy; ++y)
+            for (int x = 0; x < gx; ++x) items.push_back(make_int4(i, x, y, z));
+      }
+      push(op, dir, ch, r, false, off);
+    }
+  };
+  auto points = [&](int op, bool stage0) {
+    const size_t off = items.size();
+    for (int i = 0; i < nc; ++i) {
+      const astr_ctx* c = b->cases[i];
+      if (op == BOP_SIGMA && !c->pm.diffterm) continue;
+      const long long nb = (c->g.n0 + KB_PTS - 1) / KB_PTS;
+      for (long long x = 0; x < nb; ++x) items.push_back(make_int4(i, (int)x, 0, 0));
+    }
+    push(op, 0, 0, 0, stage0, off);
+  };
+  for (int dir = 0; dir < 3; ++dir) sweep(BOP_FILTER, dir);
+  for (int dir = 0; dir < 3; ++dir) {
+    const size_t off = items.size();
+    for (int i = 0; i < nc; ++i) {
+      const astr_ctx* c = b->cases[i];
+      if (!c->g.per[dir]) continue;
+      const Geo& g = c->g;
+      const int na = dir == 0 ? g.jm : g.im, nb = dir == 2 ? g.jm : g.km;
+      const int nx = (na + KB_THREADS) / KB_THREADS;
+      for (int y = 0; y <= nb; ++y)
+        for (int x = 0; x < nx; ++x) items.push_back(make_int4(i, x, y, 0));
+    }
+    push(BOP_QSWAP, dir, 0, 0, false, off);
+  }
+  points(BOP_QSAVE, true);
+  for (int dir = 0; dir < 3; ++dir) sweep(BOP_CONVGRAD, dir);
+  points(BOP_SIGMA, false);
+  for (int dir = 0; dir < 3; ++dir) sweep(BOP_VISC, dir);
+  points(BOP_RK, false);
+}
+
+template <typename T>
+void batch_desc(astr_ctx* c, BCase<T>& o) {
+  std::memset((void*)&o, 0, sizeof(o));
+  o.g = c->g;
+  o.d = dev<T>(c);
+  o.ph = c->ph;
+  o.Tb = ftab<T>(c);
+  for (int dir = 0; dir < 3; ++dir) {
+    o.Sd[dir] = v2_sd<T>(c, dir);
+    o.Sf[dir] = v2_sf<T>(c, dir);
+  }
+  o.vsplit = c->vsplit ? 1 : 0;
+}
+
+template <typename T>
+int batch_launch(astr_batch* b, const astr_batch::Phase& p, int stage, const BatchCtl& ctl) {
+  const BCase<T>* cs = (const BCase<T>*)b->dcases;
+  const int4* it = b->ditems + p.off;
+  cudaError_t e = cudaSuccess;
+  if (p.op <= BOP_VISC) {
+    const V2Args<T> a = v2_args<T>(b->cases[p.rep], p.dir, p.op == BOP_FILTER);
+    const int nsm = std::max(1, (int)(b->nsm * b->share + 0.5));
+    e = p.dir == 0 ? astr::launch2_batch<T, 0>(p.op, p.CH, a, cs, it, p.n, ctl, nsm, b->st)
+                   : (p.dir == 1 ? astr::launch2_batch<T, 1>(p.op, p.CH, a, cs, it, p.n, ctl, nsm, b->st)
+                                 : astr::launch2_batch<T, 2>(p.op, p.CH, a, cs, it, p.n, ctl, nsm, b->st));
+  } else {
+    const int kind = p.op == BOP_QSWAP ? p.dir : (p.op == BOP_QSAVE ? 3 : (p.op == BOP_SIGMA ? 4 : 5));
+    const unsigned grid = (unsigned)std::min(p.n, std::max(1, (int)(b->nsm * b->share * 8 + 0.5)));
+    kb_point<T><<<grid, KB_THREADS, 0, b->st>>>(cs, it, p.n, kind, stage, ctl);
+    e = cudaGetLastError();
+  }
+  ++b->launches;
+  if (e != cudaSuccess) return bfail(b, ASTR_ERR_CUDA, std::string("batched launch: ") + cudaGetErrorString(e));
+  return ASTR_OK;
+}
+
+template <typename T>
+int batch_enqueue(astr_batch* b, int nsteps, double budget_ms) {
+  const size_t nc = b->cases.size();
+  if (b->dirty) {
+    std::vector<int4> items;
+    batch_plan<T>(b, items);
+    BCK(cudaStreamSynchronize(b->st));
+    if (items.size() > b->items_cap) {
+      if (b->ditems) BCK(cudaFree(b->ditems));
+      b->ditems = nullptr;
+      b->items_cap = 0;
+      BCK(cudaMalloc(&b->ditems, items.size() * sizeof(int4)));
+      b->items_cap = items.size();
+    }
+    if (!items.empty())
+      BCK(cudaMemcpy(b->ditems, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    const size_t bytes = std::max<size_t>(nc, 1) * sizeof(BCase<T>);
+    if (bytes > b->desc_cap) {
+      if (b->dcases) BCK(cudaFree(b->dcases));
+      if (b->hcases) BCK(cudaFreeHost(b->hcases));
+      b->dcases = b->hcases = nullptr;
+      b->desc_cap = 0;
+      BCK(cudaMalloc(&b->dcases, bytes));
+      BCK(cudaMallocHost(&b->hcases, bytes));
+      b->desc_cap = bytes;
+    }
+    b->dirty = false;
+  }
+  // descriptors (time step, constants) as the contexts hold them now
+  BCK(cudaEventSynchronize(b->ev_desc));
+  BCase<T>* h = (BCase<T>*)b->hcases;
+  for (size_t i = 0; i < nc; ++i) batch_desc<T>(b->cases[i], h[i]);
+  BCK(cudaMemcpyAsync(b->dcases, b->hcases, nc * sizeof(BCase<T>), cudaMemcpyHostToDevice, b->st));
+  BCK(cudaEventRecord(b->ev_desc, b->st));
+  // after the work already queued on every case
+  for (astr_ctx* c : b->cases) {
+    BCK(cudaEventRecord(b->ev_in, c->st));
+    BCK(cudaStreamWaitEvent(b->st, b->ev_in, 0));
+  }
+  ((volatile int*)b->hword)[0] = 0;
+  BatchCtl ctl{b->hword_dev, b->ddeadline, b->dctl, b->dctl + 1};
+  const unsigned long long budget = budget_ms > 0 ? (unsigned long long)(budget_ms * 1e6) : 0ULL;
+  k_batch_start<<<1, 1, 0, b->st>>>(ctl, b->ddeadline, budget < 1 && budget_ms > 0 ? 1ULL : budget);
+  BCK(cudaGetLastError());
+  ++b->launches;
+  for (int s = 0; s < nsteps; ++s) {
+    k_batch_gate<<<1, 1, 0, b->st>>>(ctl);
+    BCK(cudaGetLastError());
+    ++b->launches;
+    for (int stage = 0; stage < 3; ++stage)
+      for (const astr_batch::Phase& p : b->phases)
+        if (!p.stage0 || stage == 0) RC(batch_launch<T>(b, p, stage, ctl));
+  }
+  BCK(cudaMemcpyAsync(b->hword + 1, b->dctl, 2 * sizeof(int), cudaMemcpyDeviceToHost, b->st));
+  BCK(cudaEventRecord(b->ev_done, b->st));
+  // later work on each case waits for the batch
+  for (astr_ctx* c : b->cases) BCK(cudaStreamWaitEvent(c->st, b->ev_done, 0));
+  b->pending = true;
+  return ASTR_OK;
+}
+
+// The call's outcome, once its work has finished.
+void batch_finish(astr_batch* b) {
+  const int status = ((volatile int*)b->hword)[1];
+  const int started = ((volatile int*)b->hword)[2];
+  for (astr_ctx* c : b->cases) c->nstep += started;
+  b->result_steps = started;
+  b->result = (status & 1) ? ASTR_ERR_CANCELLED : ((status & 2) ? ASTR_ERR_TIMEOUT : ASTR_OK);
+  if (b->result == ASTR_ERR_CANCELLED) b->err = "cancelled";
+  if (b->result == ASTR_ERR_TIMEOUT) b->err = "deadline passed";
+  b->pending = false;
+}
+
+}  // namespace
+
+static void batch_forget(astr_batch* b, astr_ctx* c) {
+  if (b->pending) {
+    cudaEventSynchronize(b->ev_done);
+    batch_finish(b);
+  }
+  auto it = std::find(b->cases.begin(), b->cases.end(), c);
+  if (it != b->cases.end()) b->cases.erase(it);
+  c->batch = nullptr;
+  b->dirty = true;
+}
+
+extern "C" {
+
+int astr_batch_create(int precision, astr_batch** out) {
+  if (!out) return ASTR_ERR_ARG;
+  *out = nullptr;
+  if (precision != ASTR_FP64 && precision != ASTR_FP32_STORAGE) return ASTR_ERR_ARG;
+  astr_batch* b = new astr_batch();
+  b->prec = precision;
+  int dev = 0;
+  auto bad = [&](cudaError_t e) {
+    if (e == cudaSuccess) return false;
+    g_create_err = std::string("astr_batch_create: ") + cudaGetErrorString(e);
+    astr_batch_destroy(b);
+    return true;
+  };
+  if (bad(cudaGetDevice(&dev))) return ASTR_ERR_CUDA;
+  if (bad(cudaDeviceGetAttribute(&b->nsm, cudaDevAttrMultiProcessorCount, dev))) return ASTR_ERR_CUDA;
+  if (bad(cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking))) return ASTR_ERR_CUDA;
+  if (bad(cudaEventCreateWithFlags(&b->ev_desc, cudaEventDisableTiming))) return ASTR_ERR_CUDA;
+  if (bad(cudaEventCreateWithFlags(&b->ev_done, cudaEventDisableTiming))) return ASTR_ERR_CUDA;
+  if (bad(cudaEventCreateWithFlags(&b->ev_in, cudaEventDisableTiming))) return ASTR_ERR_CUDA;
+  if (bad(cudaMalloc(&b->dctl, 2 * sizeof(int)))) return ASTR_ERR_OOM;
+  if (bad(cudaMalloc(&b->ddeadline, sizeof(unsigned long long)))) return ASTR_ERR_OOM;
+  if (bad(cudaHostAlloc(&b->hword, 4 * sizeof(int), cudaHostAllocMapped))) return ASTR_ERR_OOM;
+  std::memset(b->hword, 0, 4 * sizeof(int));
+  if (bad(cudaHostGetDevicePointer((void**)&b->hword_dev, b->hword, 0))) return ASTR_ERR_CUDA;
+  *out = b;
+  return ASTR_OK;
+}
+
+void astr_batch_destroy(astr_batch* b) {
+  if (!b) return;
+  if (b->st) cudaStreamSynchronize(b->st);
+  for (astr_ctx* c : b->cases) c->batch = nullptr;
+  if (b->ev_desc) cudaEventDestroy(b->ev_desc);
+  if (b->ev_done) cudaEventDestroy(b->ev_done);
+  if (b->ev_in) cudaEventDestroy(b->ev_in);
+  if (b->dcases) cudaFree(b->dcases);
+  if (b->hcases) cudaFreeHost(b->hcases);
+  if (b->ditems) cudaFree(b->ditems);
+  if (b->dctl) cudaFree(b->dctl);
+  if (b->ddeadline) cudaFree(b->ddeadline);
+  if (b->hword) cudaFreeHost(b->hword);
+  if (b->st) cudaStreamDestroy(b->st);
+  delete b;
+}
+
+int astr_batch_add(astr_batch* b, astr_ctx* c) {
+  if (!b) return ASTR_ERR_ARG;
+  if (!c) return bfail(b, ASTR_ERR_ARG, "null context");
+  const std::string why = batch_refusal(c, b->prec);
+  if (!why.empty()) return bfail(b, ASTR_ERR_UNSUPPORTED, why);
+  if (c->batch) return bfail(b, ASTR_ERR_STATE, "the case is already in a batch");
+  if (b->pending) return bfail(b, ASTR_ERR_STATE, "a batched call is in flight (astr_batch_wait)");
+  b->cases.push_back(c);
+  c->batch = b;
+  b->dirty = true;
+  return ASTR_OK;
+}
+
+int astr_batch_remove(astr_batch* b, astr_ctx* c) {
+  if (!b) return ASTR_ERR_ARG;
+  if (!c || c->batch != b) return bfail(b, ASTR_ERR_ARG, "the case is not in this batch");
+  if (b->pending) return bfail(b, ASTR_ERR_STATE, "a batched call is in flight (astr_batch_wait)");
+  batch_forget(b, c);
+  return ASTR_OK;
+}
+
+int astr_batch_size(astr_batch* b) { return b ? (int)b->cases.size() : ASTR_ERR_ARG; }
+
+int astr_batch_set_share(astr_batch* b, double share) {
+  if (!b) return ASTR_ERR_ARG;
+  if (!(share > 0.0 && share <= 1.0)) return bfail(b, ASTR_ERR_ARG, "share outside (0, 1]");
+  b->share = share;
+  return ASTR_OK;
+}
+
+int astr_batch_step_async(astr_batch* b, int nsteps, double budget_ms) {
+  if (!b) return ASTR_ERR_ARG;
+  if (nsteps < 0) return bfail(b, ASTR_ERR_ARG, "nsteps < 0");
+  if (b->pending) return bfail(b, ASTR_ERR_STATE, "a batched call is in flight (astr_batch_wait)");
+  for (astr_ctx* c : b->cases) {
+    const std::string why = batch_refusal(c, b->prec);
+    if (!why.empty()) return bfail(b, ASTR_ERR_UNSUPPORTED, why);
+  }
+  return b->prec == ASTR_FP64 ? batch_enqueue<double>(b, nsteps, budget_ms)
+                              : batch_enqueue<float>(b, nsteps, budget_ms);
+}
+
+int astr_batch_poll(astr_batch* b) {
+  if (!b) return ASTR_ERR_ARG;
+  if (!b->pending) return 1;
+  const cudaError_t e = cudaEventQuery(b->ev_done);
+  if (e == cudaErrorNotReady) return 0;
+  if (e != cudaSuccess) return bfail(b, ASTR_ERR_CUDA, std::string("astr_batch_poll: ") + cudaGetErrorString(e));
+  batch_finish(b);
+  return 1;
+}
+
+int astr_batch_wait(astr_batch* b, int* steps_done) {
+  if (!b) return ASTR_ERR_ARG;
+  if (b->pending) {
+    BCK(cudaEventSynchronize(b->ev_done));
+    batch_finish(b);
+  }
+  if (steps_done) *steps_done = b->result_steps;
+  return b->result;
+}
+
+int astr_batch_cancel(astr_batch* b) {
+  if (!b) return ASTR_ERR_ARG;
+  ((volatile int*)b->hword)[0] = 1;
+  return ASTR_OK;
+}
+
+int astr_batch_step(astr_batch* b, int nsteps, double budget_ms, int* steps_done) {
+  RC(astr_batch_step_async(b, nsteps, budget_ms));
+  return astr_batch_wait(b, steps_done);
+}
+
+int astr_batch_last_error(astr_batch* b, char* buf, int len) {
+  const std::string& m = b ? b->err : g_create_err;
+  if (buf && len > 0) {
+    std::strncpy(buf, m.c_str(), (size_t)len - 1);
+    buf[len - 1] = 0;
+  }
+  return (int)m.size();
+}
+
+long long astr_batch_launch_count(astr_batch* b) { return b ? b->launches : 0; }
 
 }  // extern "C"

@@ -36,19 +36,11 @@
 
 namespace astr {
 
-// Lines per block (FP32 storage / FP64) and resident blocks per SM asked of
-// the compiler.
-#ifndef ASTR_V2_NL32
-#define ASTR_V2_NL32 8
-#endif
-#ifndef ASTR_V2_NL64
-#define ASTR_V2_NL64 4
-#endif
+// Resident blocks per SM asked of the compiler (the lines per block,
+// v2_nl, are in launch2.cuh).
 #ifndef ASTR_V2_MINB
 #define ASTR_V2_MINB 2
 #endif
-template <typename T>
-constexpr int v2_nl() { return sizeof(T) == 4 ? ASTR_V2_NL32 : ASTR_V2_NL64; }
 template <typename T>
 constexpr int v2_nt() { return 32 * v2_nl<T>(); }
 // The filter and viscous sweeps hold fewer tiles and fit more blocks per SM;
@@ -118,20 +110,30 @@ __device__ __forceinline__ void cp_async_elem(T* dst, const T* src, bool valid) 
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
-// Halo-array offset of node 0 of line l of this block (or of the last line
+// The block a sweep body works on: the launch's own block, or an item of
+// a batch work list (nz > 1: the variables of a line spread over z blocks).
+struct VB {
+  int x, y, z, nz;
+};
+__device__ __forceinline__ VB vb_grid() {
+  return VB{(int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z, (int)gridDim.z};
+}
+
+// Halo-array offset of node 0 of line l of block vb (or of the last line
 // when l is past the end), and the interior-array offset of that node.
 template <int DIR, int NL>
-__device__ __forceinline__ bool v2_line(const Geo& g, int l, int& hb, int& zb, int& la, int& lb) {
+__device__ __forceinline__ bool v2_line(const Geo& g, const VB& vb, int l, int& hb, int& zb, int& la,
+                                        int& lb) {
   const int amax = DIR == 0 ? g.jm : g.im;
-  int a = (int)blockIdx.x * NL + l;
+  int a = vb.x * NL + l;
   const bool ok = a <= amax;
   if (!ok) a = amax;
   int i, j, k;
-  line_ijk<DIR>(a, (int)blockIdx.y, 0, i, j, k);
+  line_ijk<DIR>(a, vb.y, 0, i, j, k);
   hb = (int)hidx(g, i, j, k);
   zb = (int)zidx(g, i, j, k);
   la = a;
-  lb = (int)blockIdx.y;
+  lb = vb.y;
   return ok;
 }
 
@@ -387,7 +389,7 @@ inline size_t v2_smem_bytes(int CH, int R, int P, int ntile) {
 // Pitch of an x tile: at least nrt words, 32/NL mod 32 (FP32) or 16/NL mod
 // 16 (FP64).
 template <typename T>
-inline int v2_pitch(int CH, int R) {
+__host__ __device__ inline int v2_pitch(int CH, int R) {
   const int nrt = 32 * CH + 2 * R;
   const int m = sizeof(T) == 4 ? 32 : 16;
   const int want = (m / v2_nl<T>()) % m;
@@ -411,11 +413,11 @@ inline UCo<T, CH> make_uco(const V2Args<T>& a) {
 // variables in place.
 // ---------------------------------------------------------------------------
 template <typename T, int DIR, int CH>
-__global__ void __launch_bounds__(v2_nt<T>(), sizeof(T) == 4 ? V2_MINB_F : 2)
-k2_filter(Geo g, DevT<T> d, DScheme<T> S, UCo<T, CH> U, FTab<T> Tb, int P) {
+__device__ __forceinline__ void filter_body(const Geo& g, const DevT<T>& d, const DScheme<T>& S,
+                                            const UCo<T, CH>& U, const FTab<T>& Tb, int P, const VB vb,
+                                            unsigned char* v2_smem) {
   constexpr int NL = v2_nl<T>(), R = 5, NRT = 32 * CH + 2 * R, E = (NRT + 31) / 32;
   constexpr bool delta = sizeof(T) == 4;
-  extern __shared__ __align__(16) unsigned char v2_smem[];
   const int TWd = DIR == 0 ? NL * P : NRT * NL;
   T* buf0 = reinterpret_cast<T*>(v2_smem);
   T* scan = buf0 + 2 * TWd;
@@ -427,13 +429,13 @@ k2_filter(Geo g, DevT<T> d, DScheme<T> S, UCo<T, CH> U, FTab<T> Tb, int P) {
   const int nh = (int)g.nh;
   StageMap<DIR, NL> sm_;
   int shb, szb, sa, sb;
-  const bool sok = v2_line<DIR, NL>(g, sm_.line, shb, szb, sa, sb);
+  const bool sok = v2_line<DIR, NL>(g, vb, sm_.line, shb, szb, sa, sb);
   int ohb, ozb, oa, ob;
-  const bool ook = v2_line<DIR, NL>(g, ol, ohb, ozb, oa, ob);
+  const bool ook = v2_line<DIR, NL>(g, vb, ol, ohb, ozb, oa, ob);
   (void)sa; (void)sb; (void)oa; (void)ob;
 
   int t0 = 0, t1 = 5;
-  if (gridDim.z > 1) { t0 = blockIdx.z; t1 = t0 + 1; }
+  if (vb.nz > 1) { t0 = vb.z; t1 = t0 + 1; }
   // task t's input (q, periodic nodes wrapped) into tile bf, asynchronously
   auto issue = [&](int t, T* bf) {
     const T* v = d.q + (size_t)t * nh + shb;
@@ -517,10 +519,10 @@ k2_filter(Geo g, DevT<T> d, DScheme<T> S, UCo<T, CH> U, FTab<T> Tb, int P) {
 // (src/comsolver.F90:244-497), one direction, diagonal metrics.
 // ---------------------------------------------------------------------------
 template <typename T, int DIR, int CH>
-__global__ void __launch_bounds__(v2_nt<T>(), V2_MINB)
-k2_convgrad(Geo g, DevT<T> d, DScheme<T> S, UCo<T, CH> U, CGFlags fl, int P) {
+__device__ __forceinline__ void convgrad_body(const Geo& g, const DevT<T>& d, const DScheme<T>& S,
+                                              const UCo<T, CH>& U, const CGFlags fl, int P, const VB vb,
+                                              unsigned char* v2_smem) {
   constexpr int NL = v2_nl<T>(), R = 3, NRT = 32 * CH + 2 * R, E = (NRT + 31) / 32;
-  extern __shared__ __align__(16) unsigned char v2_smem[];
   const int TWd = DIR == 0 ? NL * P : NRT * NL;
   T* tA = reinterpret_cast<T*>(v2_smem);
   T* tB = tA + TWd;
@@ -535,9 +537,9 @@ k2_convgrad(Geo g, DevT<T> d, DScheme<T> S, UCo<T, CH> U, CGFlags fl, int P) {
   const size_t n0 = (size_t)g.n0;
   StageMap<DIR, NL> sm_;
   int shb, szb, sa, sb;
-  const bool sok = v2_line<DIR, NL>(g, sm_.line, shb, szb, sa, sb);
+  const bool sok = v2_line<DIR, NL>(g, vb, sm_.line, shb, szb, sa, sb);
   int ohb, ozb, oa, ob;
-  const bool ook = v2_line<DIR, NL>(g, ol, ohb, ozb, oa, ob);
+  const bool ook = v2_line<DIR, NL>(g, vb, ol, ohb, ozb, oa, ob);
   const int lo = g.lo[DIR], hi = g.hi[DIR];
   constexpr int ta = DIR == 0 ? 1 : 0, tb = DIR == 2 ? 1 : 2;
   // convrsdcal6's transverse ranges, for the line a thread writes
@@ -549,8 +551,8 @@ k2_convgrad(Geo g, DevT<T> d, DScheme<T> S, UCo<T, CH> U, CGFlags fl, int P) {
   const int nconv = fl.conv ? 5 : 0;
   const int ntask = nconv + (fl.grad ? 4 : 0);
   int t0 = 0, t1 = ntask;
-  if (gridDim.z > 1) {
-    t0 = blockIdx.z;
+  if (vb.nz > 1) {
+    t0 = vb.z;
     t1 = t0 + 1;
   }
   if (t0 >= ntask) return;  // whole block
@@ -696,10 +698,10 @@ k2_convgrad(Geo g, DevT<T> d, DScheme<T> S, UCo<T, CH> U, CGFlags fl, int P) {
 // update after the last one runs as a point kernel.
 // ---------------------------------------------------------------------------
 template <typename T, int DIR, int CH>
-__global__ void __launch_bounds__(v2_nt<T>(), sizeof(T) == 4 ? V2_MINB_V : 2)
-k2_visc(Geo g, DevT<T> d, DScheme<T> S, UCo<T, CH> U, int P) {
+__device__ __forceinline__ void visc_body(const Geo& g, const DevT<T>& d, const DScheme<T>& S,
+                                          const UCo<T, CH>& U, int P, const VB vb,
+                                          unsigned char* v2_smem) {
   constexpr int NL = v2_nl<T>(), R = 3, NRT = 32 * CH + 2 * R, E = (NRT + 31) / 32;
-  extern __shared__ __align__(16) unsigned char v2_smem[];
   const int TWd = DIR == 0 ? NL * P : NRT * NL;
   T* tF = reinterpret_cast<T*>(v2_smem);
   T* buf0 = tF + TWd;
@@ -713,14 +715,14 @@ k2_visc(Geo g, DevT<T> d, DScheme<T> S, UCo<T, CH> U, int P) {
   const size_t n0 = (size_t)g.n0;
   StageMap<DIR, NL> sm_;
   int shb, szb, sa, sb;
-  const bool sok = v2_line<DIR, NL>(g, sm_.line, shb, szb, sa, sb);
+  const bool sok = v2_line<DIR, NL>(g, vb, sm_.line, shb, szb, sa, sb);
   int ohb, ozb, oa, ob;
-  const bool ook = v2_line<DIR, NL>(g, ol, ohb, ozb, oa, ob);
+  const bool ook = v2_line<DIR, NL>(g, vb, ol, ohb, ozb, oa, ob);
   (void)sa; (void)sb; (void)oa; (void)ob; (void)ohb;
   const int lo = g.lo[DIR], hi = g.hi[DIR];
 
   int t0 = 0, t1 = 4;
-  if (gridDim.z > 1) { t0 = blockIdx.z; t1 = t0 + 1; }
+  if (vb.nz > 1) { t0 = vb.z; t1 = t0 + 1; }
   {
     // J dxi at every tile row (the flux factor of the four variables)
     const T* xdd = d.xd + (size_t)DIR * nh;
@@ -830,20 +832,46 @@ k2_visc(Geo g, DevT<T> d, DScheme<T> S, UCo<T, CH> U, int P) {
 }
 
 // ---------------------------------------------------------------------------
+// Single-case kernels: the bodies on the launch's own blocks
+// ---------------------------------------------------------------------------
+template <typename T, int DIR, int CH>
+__global__ void __launch_bounds__(v2_nt<T>(), sizeof(T) == 4 ? V2_MINB_F : 2)
+k2_filter(Geo g, DevT<T> d, DScheme<T> S, UCo<T, CH> U, FTab<T> Tb, int P) {
+  extern __shared__ __align__(16) unsigned char v2_smem[];
+  filter_body<T, DIR, CH>(g, d, S, U, Tb, P, vb_grid(), v2_smem);
+}
+template <typename T, int DIR, int CH>
+__global__ void __launch_bounds__(v2_nt<T>(), V2_MINB)
+k2_convgrad(Geo g, DevT<T> d, DScheme<T> S, UCo<T, CH> U, CGFlags fl, int P) {
+  extern __shared__ __align__(16) unsigned char v2_smem[];
+  convgrad_body<T, DIR, CH>(g, d, S, U, fl, P, vb_grid(), v2_smem);
+}
+template <typename T, int DIR, int CH>
+__global__ void __launch_bounds__(v2_nt<T>(), sizeof(T) == 4 ? V2_MINB_V : 2)
+k2_visc(Geo g, DevT<T> d, DScheme<T> S, UCo<T, CH> U, int P) {
+  extern __shared__ __align__(16) unsigned char v2_smem[];
+  visc_body<T, DIR, CH>(g, d, S, U, P, vb_grid(), v2_smem);
+}
+
+// ---------------------------------------------------------------------------
 // Launchers
 // ---------------------------------------------------------------------------
 template <int DIR>
 inline dim3 v2_grid(const Geo& g, int NL, int nz) {
-  const int amax = DIR == 0 ? g.jm : g.im;
-  const unsigned gx = (unsigned)((amax + NL) / NL);
-  return dim3(gx, DIR == 1 ? g.km + 1 : (DIR == 0 ? g.km + 1 : g.jm + 1), nz);
+  int gx, gy;
+  v2_blocks(g, DIR, NL, gx, gy);
+  return dim3((unsigned)gx, (unsigned)gy, nz);
 }
 
+// Raise a kernel's dynamic shared-memory limit.  Each launcher calls it once
+// per kernel instantiation (a function-local static: the size is fixed by
+// the template arguments), never per launch: the call is not a stream
+// operation, and made per launch it kept batches on separate streams from
+// running concurrently.
 template <class K>
 inline cudaError_t v2_allow_smem(K kern, size_t bytes) {
   return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
-
 #define ASTR_V2_CH_SWITCH(CHV, EXPR)                        \
   switch (CHV) {                                            \
     case 3: { constexpr int CHC = 3; EXPR; } break;         \
@@ -857,7 +885,7 @@ template <typename T, int DIR, int CHC>
 cudaError_t launch2_filter_ch(const V2Args<T>& a, cudaStream_t st, int vsplit) {
   const int P = v2_pitch<T>(CHC, 5);
   const size_t smem = v2_smem_bytes<T, DIR>(CHC, 5, P, 2);
-  cudaError_t e = v2_allow_smem(k2_filter<T, DIR, CHC>, smem);
+  static const cudaError_t e = v2_allow_smem(k2_filter<T, DIR, CHC>, smem);
   if (e != cudaSuccess) return e;
   const dim3 gr = v2_grid<DIR>(a.g, v2_nl<T>(), vsplit ? 5 : 1);
   k2_filter<T, DIR, CHC><<<gr, dim3(v2_nl<T>(), 32), smem, st>>>(a.g, a.d, a.S, make_uco<T, CHC>(a),
@@ -868,7 +896,7 @@ template <typename T, int DIR, int CHC>
 cudaError_t launch2_convgrad_ch(const V2Args<T>& a, cudaStream_t st, CGFlags f, int vsplit) {
   const int P = v2_pitch<T>(CHC, 3);
   const size_t smem = v2_smem_bytes<T, DIR>(CHC, 3, P, V2_CG_SINGLE ? 4 : 5);
-  cudaError_t e = v2_allow_smem(k2_convgrad<T, DIR, CHC>, smem);
+  static const cudaError_t e = v2_allow_smem(k2_convgrad<T, DIR, CHC>, smem);
   if (e != cudaSuccess) return e;
   const int ntask = (f.conv ? 5 : 0) + (f.grad ? 4 : 0);
   const dim3 gr = v2_grid<DIR>(a.g, v2_nl<T>(), vsplit && ntask > 1 ? ntask : 1);
@@ -880,7 +908,7 @@ template <typename T, int DIR, int CHC>
 cudaError_t launch2_visc_ch(const V2Args<T>& a, cudaStream_t st, int vsplit) {
   const int P = v2_pitch<T>(CHC, 3);
   const size_t smem = v2_smem_bytes<T, DIR>(CHC, 3, P, 3);
-  cudaError_t e = v2_allow_smem(k2_visc<T, DIR, CHC>, smem);
+  static const cudaError_t e = v2_allow_smem(k2_visc<T, DIR, CHC>, smem);
   if (e != cudaSuccess) return e;
   const dim3 gr = v2_grid<DIR>(a.g, v2_nl<T>(), vsplit ? 4 : 1);
   k2_visc<T, DIR, CHC><<<gr, dim3(v2_nl<T>(), 32), smem, st>>>(a.g, a.d, a.S, make_uco<T, CHC>(a), P);
@@ -903,9 +931,141 @@ cudaError_t launch2_visc(const V2Args<T>& a, cudaStream_t st, int CH, int vsplit
   return cudaSuccess;
 }
 
+// ---------------------------------------------------------------------------
+// Batches: persistent kernels that take (case, block) items of many cases
+// from a work list, every case with its own descriptor, so one launch runs a
+// sweep of all the cases of a batch; the bodies are the single-case ones.
+// The cases of one launch share the chunk length and the uniform-chunk
+// constants (they depend on the scheme, not on the grid), which stay kernel
+// parameters as in the single-case kernels.  Each item first reads the
+// batch's status word (set by the step gates).
+// ---------------------------------------------------------------------------
+// Copy of a descriptor into shared memory by the whole block (the bodies
+// then read its fields from there, as the single-case kernels read theirs
+// from the parameter bank, instead of holding them in registers).
+template <typename X>
+__device__ __forceinline__ void smem_copy(X* dst, const X* src) {
+  static_assert(sizeof(X) % 4 == 0, "descriptor of whole words");
+  const int nt = blockDim.x * blockDim.y, tid = threadIdx.x + blockDim.x * threadIdx.y;
+  for (int i = tid; i < (int)(sizeof(X) / 4); i += nt) ((int*)dst)[i] = ((const int*)src)[i];
+}
+
+template <typename T, int DIR, int CH>
+__global__ void __launch_bounds__(v2_nt<T>(), sizeof(T) == 4 ? V2_MINB_F : 2)
+kb_filter(const BCase<T>* cases, const int4* items, int nitems, UCo<T, CH> U, BatchCtl ctl) {
+  extern __shared__ __align__(16) unsigned char v2_smem[];
+  __shared__ int stop;
+  __shared__ Geo sg;
+  __shared__ DevT<T> sd;
+  __shared__ DScheme<T> sS;
+  __shared__ FTab<T> sT;
+  const int P = v2_pitch<T>(CH, 5);
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const int4 w = items[it];
+    const BCase<T>* C = cases + w.x;
+    if (threadIdx.x == 0 && threadIdx.y == 0) stop = batch_stopped(ctl);
+    smem_copy(&sg, &C->g);
+    smem_copy(&sd, &C->d);
+    smem_copy(&sS, &C->Sf[DIR]);
+    smem_copy(&sT, &C->Tb);
+    __syncthreads();
+    if (stop) break;
+    filter_body<T, DIR, CH>(sg, sd, sS, U, sT, P, VB{w.y, w.z, w.w, C->vsplit ? 5 : 1}, v2_smem);
+    __syncthreads();
+  }
+}
+template <typename T, int DIR, int CH>
+__global__ void __launch_bounds__(v2_nt<T>(), V2_MINB)
+kb_convgrad(const BCase<T>* cases, const int4* items, int nitems, UCo<T, CH> U, BatchCtl ctl) {
+  extern __shared__ __align__(16) unsigned char v2_smem[];
+  __shared__ int stop;
+  __shared__ Geo sg;
+  __shared__ DevT<T> sd;
+  __shared__ DScheme<T> sS;
+  const int P = v2_pitch<T>(CH, 3);
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const int4 w = items[it];
+    const BCase<T>* C = cases + w.x;
+    if (threadIdx.x == 0 && threadIdx.y == 0) stop = batch_stopped(ctl);
+    smem_copy(&sg, &C->g);
+    smem_copy(&sd, &C->d);
+    smem_copy(&sS, &C->Sd[DIR]);
+    __syncthreads();
+    if (stop) break;
+    CGFlags f{};
+    f.conv = 1;
+    f.grad = 1;
+    f.first = DIR == 0;
+    f.last = DIR == sg.ndims - 1;
+    convgrad_body<T, DIR, CH>(sg, sd, sS, U, f, P, VB{w.y, w.z, w.w, C->vsplit ? 9 : 1}, v2_smem);
+    __syncthreads();
+  }
+}
+template <typename T, int DIR, int CH>
+__global__ void __launch_bounds__(v2_nt<T>(), sizeof(T) == 4 ? V2_MINB_V : 2)
+kb_visc(const BCase<T>* cases, const int4* items, int nitems, UCo<T, CH> U, BatchCtl ctl) {
+  extern __shared__ __align__(16) unsigned char v2_smem[];
+  __shared__ int stop;
+  __shared__ Geo sg;
+  __shared__ DevT<T> sd;
+  __shared__ DScheme<T> sS;
+  const int P = v2_pitch<T>(CH, 3);
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const int4 w = items[it];
+    const BCase<T>* C = cases + w.x;
+    if (threadIdx.x == 0 && threadIdx.y == 0) stop = batch_stopped(ctl);
+    smem_copy(&sg, &C->g);
+    smem_copy(&sd, &C->d);
+    smem_copy(&sS, &C->Sd[DIR]);
+    __syncthreads();
+    if (stop) break;
+    visc_body<T, DIR, CH>(sg, sd, sS, U, P, VB{w.y, w.z, w.w, C->vsplit ? 4 : 1}, v2_smem);
+    __syncthreads();
+  }
+}
+
+// kind: 0 filter, 1 convective + gradient, 2 viscous; a: the launch's
+// uniform-chunk constants (its other fields are not used)
+template <typename T, int DIR, int CHC>
+cudaError_t launchb_ch(int kind, const V2Args<T>& a, const BCase<T>* cases, const int4* items, int nitems,
+                       BatchCtl ctl, int nsm, cudaStream_t st) {
+  const int R = kind == 0 ? 5 : 3;
+  const int P = v2_pitch<T>(CHC, R);
+  const int ntile = kind == 0 ? 2 : (kind == 1 ? (V2_CG_SINGLE ? 4 : 5) : 3);
+  const size_t smem = v2_smem_bytes<T, DIR>(CHC, R, P, ntile);
+  const int minb = kind == 0 ? (sizeof(T) == 4 ? V2_MINB_F : 2)
+                             : (kind == 1 ? V2_MINB : (sizeof(T) == 4 ? V2_MINB_V : 2));
+  const unsigned grid = (unsigned)std::min(nitems, nsm * minb);
+  const dim3 bl(v2_nl<T>(), 32);
+  const UCo<T, CHC> U = make_uco<T, CHC>(a);
+  if (kind == 0) {
+    static const cudaError_t e = v2_allow_smem(kb_filter<T, DIR, CHC>, smem);
+    if (e != cudaSuccess) return e;
+    kb_filter<T, DIR, CHC><<<grid, bl, smem, st>>>(cases, items, nitems, U, ctl);
+  } else if (kind == 1) {
+    static const cudaError_t e = v2_allow_smem(kb_convgrad<T, DIR, CHC>, smem);
+    if (e != cudaSuccess) return e;
+    kb_convgrad<T, DIR, CHC><<<grid, bl, smem, st>>>(cases, items, nitems, U, ctl);
+  } else {
+    static const cudaError_t e = v2_allow_smem(kb_visc<T, DIR, CHC>, smem);
+    if (e != cudaSuccess) return e;
+    kb_visc<T, DIR, CHC><<<grid, bl, smem, st>>>(cases, items, nitems, U, ctl);
+  }
+  return cudaGetLastError();
+}
+template <typename T, int DIR>
+cudaError_t launch2_batch(int kind, int CH, const V2Args<T>& a, const BCase<T>* cases, const int4* items,
+                          int nitems, BatchCtl ctl, int nsm, cudaStream_t st) {
+  if (nitems <= 0) return cudaSuccess;
+  ASTR_V2_CH_SWITCH(CH, return (launchb_ch<T, DIR, CHC>(kind, a, cases, items, nitems, ctl, nsm, st)));
+  return cudaSuccess;
+}
+
 #define ASTR_INSTANTIATE_SWEEPS2(T, DIR)                                                          \
   template cudaError_t launch2_filter<T, DIR>(const V2Args<T>&, cudaStream_t, int, int);         \
   template cudaError_t launch2_convgrad<T, DIR>(const V2Args<T>&, cudaStream_t, int, CGFlags, int); \
-  template cudaError_t launch2_visc<T, DIR>(const V2Args<T>&, cudaStream_t, int, int);
+  template cudaError_t launch2_visc<T, DIR>(const V2Args<T>&, cudaStream_t, int, int);          \
+  template cudaError_t launch2_batch<T, DIR>(int, int, const V2Args<T>&, const BCase<T>*, const int4*, \
+                                             int, BatchCtl, int, cudaStream_t);
 
 }  // namespace astr

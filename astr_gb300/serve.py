@@ -9,6 +9,9 @@ graph launches (astr_gpu_step_async), so the kernels of every admitted case
 run concurrently on the device, and a case that arrives while others run
 starts as soon as a slot and memory free up (continuous batching).  Finished
 cases are downloaded and their memory released at the next scheduling pass.
+BatchBackend instead steps the admitted cases together in one batch of
+persistent kernels (astr_batch_*), cases joining and leaving between calls
+of a few steps.
 
 Nothing here has a counterpart in the reference, which runs one case per
 MPI job; the cases themselves are the reference's TGV set-up (tgvini,
@@ -152,6 +155,136 @@ class GpuBackend:
         return out, launches
 
 
+class _BatchCase:
+    """A case of the BatchBackend: its solver, the steps it still needs, its
+    group (None: it runs on its own graphs) and whether it has finished."""
+
+    def __init__(self, g, points):
+        self.g = g
+        self.points = points
+        self.remaining = 0
+        self.group = None
+        self.finished = False
+
+
+class _Group:
+    """One batch, its stream and its call cycle: calls of up to `chunk`
+    steps; between calls, cases that reached their step count leave and
+    waiting cases join."""
+
+    def __init__(self, precision, chunk):
+        self.batch = capi.Batch(precision)
+        self.chunk = chunk
+        self.members: list = []
+        self.joining: list = []
+        self.inflight = 0
+        self.calls = 0
+
+    def load(self) -> float:
+        return sum(h.points for h in self.members + self.joining)
+
+    def tick(self):
+        if self.inflight:
+            if not self.batch.poll():
+                return
+            code, n = self.batch.wait()
+            if code != capi.ASTR_OK:
+                raise capi.AstrError(code, capi.batch_error(self.batch.h))
+            self.inflight = 0
+            for h in self.members:
+                h.remaining -= n
+            for h in [h for h in self.members if h.remaining <= 0]:
+                self.batch.remove(h.g)
+                self.members.remove(h)
+                h.finished = True
+        for h in self.joining:
+            self.batch.add(h.g)
+            self.members.append(h)
+        self.joining = []
+        if self.members:
+            k = min(self.chunk, min(h.remaining for h in self.members))
+            self.batch.step_async(k)
+            self.inflight = k
+            self.calls += 1
+
+
+class BatchBackend(GpuBackend):
+    """Cases step together in batches (astr_batch_*): every launch of a step
+    is a persistent kernel over the (case, block) items of all the cases of
+    a batch.  `groups` batches, each on its own stream, split the admitted
+    cases by points (timed on a 32-case mix, more than one batch gained
+    nothing: balanced batches run their phases in step).
+    Each batch runs calls of up to `chunk` steps; between calls, cases that
+    reached their step count leave and admitted cases join
+    (iteration-level continuous batching).  A case the batch kernels do not
+    take (a line longer than the tiled chunk lengths, for instance) runs on
+    its own context's graphs as in GpuBackend, and so does a case of more
+    than `max_points` points when that is set (large cases gain more from
+    running concurrently with the others than from sharing launches)."""
+
+    def __init__(self, precision=capi.FP32_STORAGE, chunk: int = 20, groups: int = 1,
+                 max_points=None):
+        super().__init__(precision)
+        self.groups = [_Group(precision, int(chunk)) for _ in range(max(1, int(groups)))]
+        self.max_points = max_points
+
+    def start(self, req: Request, inputs=None):
+        return _BatchCase(super().start(req, inputs), request_points(req))
+
+    def enqueue(self, h, nsteps: int):
+        h.remaining = int(nsteps)
+        if h.remaining <= 0:
+            h.finished = True
+            return
+        if self.max_points is not None and h.points > self.max_points:
+            h.g.step_async(nsteps)
+            return
+        grp = min(self.groups, key=lambda q: q.load())
+        try:
+            grp.batch.add(h.g)
+        except capi.AstrError as e:
+            if e.code == capi.ASTR_ERR_UNSUPPORTED:
+                h.g.step_async(nsteps)      # not batchable: own graphs
+                return
+            if e.code != capi.ASTR_ERR_STATE:
+                raise
+            h.group = grp
+            grp.joining.append(h)           # a call is in flight: join after it
+            return
+        h.group = grp
+        grp.members.append(h)
+
+    def tick(self):
+        """Harvest each batch's call in flight when it has finished and
+        start its next call."""
+        for grp in self.groups:
+            grp.tick()
+
+    def done(self, h) -> bool:
+        if h.group is None:
+            return h.finished or h.g.poll()
+        self.tick()
+        return h.finished
+
+    def finish(self, h):
+        out = h.g.download_state()
+        launches = h.g.launches
+        h.g.close()
+        return out, launches
+
+    @property
+    def calls(self) -> int:
+        return sum(q.calls for q in self.groups)
+
+    @property
+    def batch_launches(self) -> int:
+        return sum(q.batch.launches for q in self.groups)
+
+    def close(self):
+        for q in self.groups:
+            q.batch.close()
+
+
 @dataclass
 class _Slot:
     req: Request
@@ -241,6 +374,8 @@ class Server:
             self.peak_active = max(self.peak_active, len(self.active))
         if self.prefetch:
             self._prefetch()
+        if hasattr(self.b, "tick"):
+            self.b.tick()   # a batching backend starts its next call
         return done
 
 

@@ -16,6 +16,13 @@ the FP64 state q from page-locked host memory (the primitives are derived
 from it on the device), runs one RK3 step, and downloads q and the
 statistics.
 
+The line also carries "serve": the first --serve-cases (100) requests of a
+seeded Poisson stream of independent cases served through the batch kernels
+and through per-case streams (time-to-solution p50/p99, cases/s);
+--no-serve leaves it out, and --case serve runs that stream through the
+arms of --serve-arms (default: batch kernels, per-case streams, sequential
+FP64) instead.
+
 --impl reference times the CPU restatement of the reference (oracle/, a
 C++ port of the Fortran routines; the Fortran itself cannot be built on
 this image) on all host cores, on bounded 128^3 samples of the same case.
@@ -585,6 +592,12 @@ def run_gpu(args, rank, world, dist):
             "clocks": clocks[runs[-1][0]],
             "clocks_fp64": clocks.get("fp64"),
         }
+    # serving (the batch kernels) on the same GPU, after the TGV runs
+    if args.serve_in_line and args.serve_cases > 0:
+        srv = serve_summary(args, rank, world, dist, ("batched", "streams"))
+        if rank == 0:
+            line["serve"] = srv
+    if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
 
@@ -764,14 +777,41 @@ def run_channel(args, rank, world, dist):
     return 0
 
 
-def run_serve(args, rank, world, dist):
+SERVE_WORKLOAD = ("seeded Poisson stream (seed 20261203): TGV 3-D / vortex 2-D 50/50, edge "
+                  "log-U 32-192 / 64-1024, Re log-U 100-3000, Mach U(0.05,0.3), steps "
+                  "U{50..500}, CFL 0.5")
+
+
+def serve_arm(reqs, backend, budget, slots, dist, total):
+    """Serve `reqs` through `backend`; the summary with the makespan taken
+    over ranks and cases/s over all `total` requests."""
+    from astr_gb300 import serve
+    srv = serve.Server(backend, budget, max_active=slots)
+    barrier(dist)
+    recs = serve.serve(reqs, srv)
+    srv.close()
+    out = serve.summarize(reqs, recs)
+    out["makespan_s"] = round(max_over_ranks(dist, out["makespan_s"]), 3)
+    out["cases_per_s"] = round(total / out["makespan_s"], 3)
+    out.update({"peak_active": srv.peak_active, "peak_hbm_gb": round(srv.peak_used / 1e9, 2),
+                "gpu_launches": srv.launches + getattr(backend, "batch_launches", 0)})
+    if hasattr(backend, "calls"):
+        out["batched_calls"] = backend.calls
+    return out
+
+
+def serve_summary(args, rank, world, dist, arms):
     """Serving: a Poisson stream of independent cases (3-D TGV / 2-D vortex,
     50/50; edge log-uniform 32-192 / 64-1024; Re log-uniform 100-3000; Mach
     uniform 0.05-0.3; steps uniform 50-500) at args.serve_rate per second,
-    the first args.serve_cases requests of the stream.  FP32-storage cases
-    under continuous batching (admission by slots and free HBM, every
-    admitted case's steps as graph launches on its own stream) against the
-    same requests solved one at a time in plain FP64."""
+    the first args.serve_cases requests of the stream, through each arm:
+    "batched": FP32-storage cases stepped together by the batch kernels
+    (persistent kernels over (case, block) work lists; cases join and leave
+    between calls of a few steps; cases the batch kernels do not take run on
+    their own graphs), "hybrid": the same with the cases of more than
+    args.serve_hybrid_points points on their own graphs, "streams": every
+    case on its own stream and graphs, "sequential_fp64": one case at a time
+    in plain FP64."""
     import torch  # noqa: F401  (CUDA context for the memory query)
     from astr_gb300 import capi, serve
     allreqs = serve.make_requests(args.serve_cases, rate=args.serve_rate, seed=20261203)
@@ -779,40 +819,45 @@ def run_serve(args, rank, world, dist):
     reqs = serve.partition(allreqs, rank, world)
     free, total = torch.cuda.mem_get_info()
     budget = int(0.8 * free)
-    be = serve.GpuBackend(capi.FP32_STORAGE)
-    srv = serve.Server(be, budget, max_active=args.serve_slots)
-    barrier(dist)
-    recs = serve.serve(reqs, srv)
-    srv.close()
-    batched = serve.summarize(reqs, recs)
-    batched["makespan_s"] = round(max_over_ranks(dist, batched["makespan_s"]), 3)
-    batched["cases_per_s"] = round(len(allreqs) / batched["makespan_s"], 3)
-    batched.update({"peak_active": srv.peak_active, "peak_hbm_gb": round(srv.peak_used / 1e9, 2),
-                    "gpu_launches": srv.launches})
-    barrier(dist)
-    seq = serve.summarize(reqs, serve.serve_sequential(reqs, serve.GpuBackend(capi.FP64)))
-    seq["makespan_s"] = round(max_over_ranks(dist, seq["makespan_s"]), 3)
-    seq["cases_per_s"] = round(len(allreqs) / seq["makespan_s"], 3)
-    if rank != 0:
-        return 0
-    reqs = allreqs
-    work = sum(serve.request_points(q) * 3 * q.steps for q in reqs)
-    line = {
-        "case": "serve",
-        "workload": f"first {len(reqs)} requests of the seeded Poisson stream at "
-                    f"{args.serve_rate:g}/s (seed 20261203): TGV 3-D / vortex 2-D 50/50, edge "
-                    "log-U 32-192 / 64-1024, Re log-U 100-3000, Mach U(0.05,0.3), steps "
-                    "U{50..500}, CFL 0.5",
+    out = {}
+    for arm in arms:
+        if arm in ("batched", "hybrid"):
+            mp = args.serve_hybrid_points if arm == "hybrid" else None
+            be = serve.BatchBackend(capi.FP32_STORAGE, chunk=args.serve_chunk,
+                                    groups=args.serve_groups, max_points=mp)
+            out[arm] = serve_arm(reqs, be, budget, args.serve_slots, dist, len(allreqs))
+            out[arm]["chunk_steps"] = args.serve_chunk
+            out[arm]["batches"] = args.serve_groups
+            if mp is not None:
+                out[arm]["batched_up_to_points"] = mp
+            be.close()
+        elif arm == "streams":
+            out[arm] = serve_arm(reqs, serve.GpuBackend(capi.FP32_STORAGE), budget,
+                                 args.serve_slots, dist, len(allreqs))
+        else:
+            barrier(dist)
+            seq = serve.summarize(reqs, serve.serve_sequential(reqs, serve.GpuBackend(capi.FP64)))
+            seq["makespan_s"] = round(max_over_ranks(dist, seq["makespan_s"]), 3)
+            seq["cases_per_s"] = round(len(allreqs) / seq["makespan_s"], 3)
+            out[arm] = seq
+    work = sum(serve.request_points(q) * 3 * q.steps for q in allreqs)
+    out.update({
+        "workload": f"first {len(allreqs)} requests at {args.serve_rate:g}/s of the "
+                    + SERVE_WORKLOAD,
         "offered_mpts_stages": round(work / 1e6, 1),
-        "continuous_batching_fp32_storage": batched,
-        "sequential_fp64": seq,
         "hbm_budget_gb": round(budget / 1e9, 1), "slots": args.serve_slots, "n_gpus": world,
         "latency_note": "p50/p99 of rank 0's share when n_gpus > 1",
         "note": "time to solution = finish - arrival (wall clock, host-driven loop incl. case "
                 "set-up, upload and download); the offered load exceeds one GPU, so latency "
                 "includes queueing",
-    }
-    print(json.dumps(line), flush=True)
+    })
+    return out
+
+
+def run_serve(args, rank, world, dist):
+    out = serve_summary(args, rank, world, dist, tuple(args.serve_arms.split(",")))
+    if rank == 0:
+        print(json.dumps(dict(case="serve", **out)), flush=True)
     return 0
 
 
@@ -929,6 +974,12 @@ def main():
     ap.add_argument("--serve-cases", type=int, default=100)
     ap.add_argument("--serve-rate", type=float, default=50.0)
     ap.add_argument("--serve-slots", type=int, default=32)
+    ap.add_argument("--serve-chunk", type=int, default=20)
+    ap.add_argument("--serve-arms", default="batched,streams,sequential_fp64")
+    ap.add_argument("--serve-groups", type=int, default=1)
+    ap.add_argument("--serve-hybrid-points", type=float, default=2e5)
+    ap.add_argument("--no-serve", dest="serve_in_line", action="store_false",
+                    help="leave the serving key out of the TGV line")
     ap.add_argument("--channel-dims", type=int, nargs=3, default=[256, 192, 128])
     ap.add_argument("--channel-steps", type=int, default=500)
     ap.add_argument("--vortex-n", type=int, default=512)

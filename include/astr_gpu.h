@@ -33,6 +33,8 @@ extern "C" {
 #define ASTR_ERR_UNSUPPORTED -4 /* configuration outside what is built   */
 #define ASTR_ERR_NONFINITE -5  /* crash check: non-finite or rho <= 0     */
 #define ASTR_ERR_STATE -6      /* call out of order (e.g. no metrics)     */
+#define ASTR_ERR_TIMEOUT -7    /* batched call: deadline passed           */
+#define ASTR_ERR_CANCELLED -8  /* batched call: cancelled by the host     */
 
 /* Stage ordering. */
 #define ASTR_ORDER_MAIN 0     /* src/mainloop.F90:396-486                 */
@@ -149,6 +151,58 @@ int astr_gpu_step_async(astr_ctx* ctx, int nsteps);
 /* 1 when all work enqueued on the context has finished, 0 while it is in
  * flight, < 0 on a CUDA error. */
 int astr_gpu_poll(astr_ctx* ctx);
+
+/* Batches (continuous batching of independent cases; no counterpart in the
+ * reference).  A batch steps all its cases with one launch per phase of an
+ * RK3 stage (filter, qswap, RK3 base, convective + gradient, stress,
+ * viscous, update): persistent kernels walk a work list of (case, block)
+ * items of every case, each case with its own geometry, fields, schemes and
+ * time step.  A case advances exactly as astr_gpu_rk3_step would advance it
+ * alone (same kernels, same order, same arithmetic).  Cases join with
+ * astr_batch_add after their metrics and state are set; a batch takes cases
+ * of its own precision that run the tiled sweeps (main ordering, diagonal
+ * metrics, central scheme; FP64 only with ASTR_V2=2 set at create), are
+ * periodic (no boundary routines), not channels, without crash control.
+ * Each case keeps its own context: uploads, downloads and statistics go
+ * through it, ordered after the batch's work by stream events.  Destroying
+ * a context removes it from its batch. */
+typedef struct astr_batch astr_batch;
+int astr_batch_create(int precision, astr_batch** out);
+void astr_batch_destroy(astr_batch* batch);
+/* ASTR_ERR_UNSUPPORTED (with the reason in astr_batch_last_error) for a case
+ * outside what batches run, checked first; then ASTR_ERR_STATE when the case
+ * is already in a batch or a call of this batch is in flight. */
+int astr_batch_add(astr_batch* batch, astr_ctx* ctx);
+int astr_batch_remove(astr_batch* batch, astr_ctx* ctx);
+int astr_batch_size(astr_batch* batch);
+/* Grid of the batch's persistent kernels: share (0, 1] of the blocks the
+ * GPU holds resident at once (default 1: the whole GPU).  Batches that run
+ * concurrently on their own streams take a share each, so that the phases
+ * of one fill the GPU while another's end. */
+int astr_batch_set_share(astr_batch* batch, double share);
+/* Enqueue nsteps RK3 steps of every case and return at once.  budget_ms > 0
+ * sets a deadline that many milliseconds after the call's work starts on the
+ * GPU (its global timer).  Each step begins with a gate that reads the
+ * cancel word (astr_batch_cancel) and the timer: once either says stop, no
+ * later step starts, and a step that has started runs to its end, so every
+ * case is always left at a step boundary.  One call in flight at a time. */
+int astr_batch_step_async(astr_batch* batch, int nsteps, double budget_ms);
+/* 1 when the call in flight has finished (or none is), 0 while it runs,
+ * < 0 on a CUDA error. */
+int astr_batch_poll(astr_batch* batch);
+/* Wait for the call in flight; *steps_done (may be NULL) receives the steps
+ * every case advanced.  ASTR_OK when all ran, ASTR_ERR_TIMEOUT when the
+ * deadline stopped it, ASTR_ERR_CANCELLED when the cancel word did. */
+int astr_batch_wait(astr_batch* batch, int* steps_done);
+/* Set the batch's cancel word (page-locked host memory mapped into the
+ * GPU); the next step gate of the call in flight sees it.  Thread-safe
+ * against a concurrent astr_batch_wait. */
+int astr_batch_cancel(astr_batch* batch);
+/* astr_batch_step_async followed by astr_batch_wait. */
+int astr_batch_step(astr_batch* batch, int nsteps, double budget_ms, int* steps_done);
+int astr_batch_last_error(astr_batch* batch, char* buf, int len);
+/* Kernel launches issued by this batch since creation. */
+long long astr_batch_launch_count(astr_batch* batch);
 
 /* crashcheck (src/mainloop.F90:709-812): count the interior nodes whose
  * density is negative or not a number; ijk (may be NULL) receives the

@@ -11,7 +11,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def header_symbols():
     src = open(os.path.join(ROOT, "include", "astr_gpu.h")).read()
-    return sorted(set(re.findall(r"\b(astr_gpu_\w+)\s*\(", src)))
+    return sorted(set(re.findall(r"\b(astr_(?:gpu|batch)_\w+)\s*\(", src)))
 
 
 def test_exports_every_declared_symbol(gpu_lib):

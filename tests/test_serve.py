@@ -114,3 +114,63 @@ def test_scheduler_prefetches_inputs():
     # first come first served, every case prepared exactly once before it started
     assert be.started == sorted(be.started)
     assert sorted(be.prepared) == be.started
+
+
+class _FakeBatch:
+    """Stands in for capi.Batch: a call of k steps finishes at the next
+    poll; a case added while a call is in flight is refused as the C ABI
+    refuses it."""
+
+    def __init__(self, precision):
+        self.members = []
+        self.calls = []
+        self.inflight = None
+
+    def add(self, g):
+        from astr_gb300 import capi
+        if self.inflight is not None:
+            raise capi.AstrError(capi.ASTR_ERR_STATE, "a batched call is in flight")
+        self.members.append(g)
+
+    def remove(self, g):
+        self.members.remove(g)
+
+    def __len__(self):
+        return len(self.members)
+
+    def step_async(self, k):
+        assert self.inflight is None and k > 0
+        self.inflight = k
+        self.calls.append((k, list(self.members)))
+
+    def poll(self):
+        return True
+
+    def wait(self):
+        from astr_gb300 import capi
+        k, self.inflight = self.inflight, None
+        return capi.ASTR_OK, k
+
+
+def test_batch_group_joins_and_leaves_between_calls(monkeypatch):
+    """Calls of min(chunk, fewest remaining steps); a case leaves when its
+    steps are done and a case that arrives during a call joins after it."""
+    from astr_gb300 import capi
+    monkeypatch.setattr(capi, "Batch", _FakeBatch)
+    grp = serve._Group(capi.FP32_STORAGE, chunk=20)
+    a, b, c = (serve._BatchCase(name, 1.0) for name in ("a", "b", "c"))
+    a.remaining, b.remaining, c.remaining = 50, 7, 30
+    for h in (a, b):
+        grp.batch.add(h.g)
+        grp.members.append(h)
+    grp.tick()                                  # starts a call of 7 steps
+    assert grp.batch.calls[-1] == (7, ["a", "b"])
+    grp.joining.append(c)                       # arrives during the call
+    grp.tick()                                  # harvest: b done; c joins; next call
+    assert b.finished and not a.finished and (a.remaining, c.remaining) == (43, 30)
+    assert grp.batch.calls[-1] == (20, ["a", "c"])
+    for _ in range(4):
+        grp.tick()
+    assert a.finished and c.finished and a.remaining == 0 and c.remaining == 0
+    assert [k for k, _ in grp.batch.calls] == [7, 20, 10, 13]
+    assert grp.batch.members == []
