@@ -831,14 +831,39 @@ __device__ __forceinline__ void visc_body(const Geo& g, const DevT<T>& d, const 
   }
 }
 
+// Copy of a descriptor into shared memory by the whole block (the bodies
+// then read its fields from there, as the single-case kernels read theirs
+// from the parameter bank, instead of holding them in registers).
+template <typename X>
+__device__ __forceinline__ void smem_copy(X* dst, const X* src) {
+  static_assert(sizeof(X) % 4 == 0, "descriptor of whole words");
+  const int nt = blockDim.x * blockDim.y, tid = threadIdx.x + blockDim.x * threadIdx.y;
+  for (int i = tid; i < (int)(sizeof(X) / 4); i += nt) ((int*)dst)[i] = ((const int*)src)[i];
+}
+
 // ---------------------------------------------------------------------------
 // Single-case kernels: the bodies on the launch's own blocks
 // ---------------------------------------------------------------------------
+// The filter's descriptors go through shared memory (thread 0 copies them
+// from the parameter bank): read from there, its body holds fewer of their
+// fields in registers and stops spilling at CH = 17 (ptxas).  The other
+// sweeps spill less reading their descriptors from the parameter bank.
 template <typename T, int DIR, int CH>
 __global__ void __launch_bounds__(v2_nt<T>(), sizeof(T) == 4 ? V2_MINB_F : 2)
 k2_filter(Geo g, DevT<T> d, DScheme<T> S, UCo<T, CH> U, FTab<T> Tb, int P) {
   extern __shared__ __align__(16) unsigned char v2_smem[];
-  filter_body<T, DIR, CH>(g, d, S, U, Tb, P, vb_grid(), v2_smem);
+  __shared__ Geo sg;
+  __shared__ DevT<T> sd;
+  __shared__ DScheme<T> sS;
+  __shared__ FTab<T> sT;
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    sg = g;
+    sd = d;
+    sS = S;
+    sT = Tb;
+  }
+  __syncthreads();
+  filter_body<T, DIR, CH>(sg, sd, sS, U, sT, P, vb_grid(), v2_smem);
 }
 template <typename T, int DIR, int CH>
 __global__ void __launch_bounds__(v2_nt<T>(), V2_MINB)
@@ -940,16 +965,6 @@ cudaError_t launch2_visc(const V2Args<T>& a, cudaStream_t st, int CH, int vsplit
 // parameters as in the single-case kernels.  Each item first reads the
 // batch's status word (set by the step gates).
 // ---------------------------------------------------------------------------
-// Copy of a descriptor into shared memory by the whole block (the bodies
-// then read its fields from there, as the single-case kernels read theirs
-// from the parameter bank, instead of holding them in registers).
-template <typename X>
-__device__ __forceinline__ void smem_copy(X* dst, const X* src) {
-  static_assert(sizeof(X) % 4 == 0, "descriptor of whole words");
-  const int nt = blockDim.x * blockDim.y, tid = threadIdx.x + blockDim.x * threadIdx.y;
-  for (int i = tid; i < (int)(sizeof(X) / 4); i += nt) ((int*)dst)[i] = ((const int*)src)[i];
-}
-
 template <typename T, int DIR, int CH>
 __global__ void __launch_bounds__(v2_nt<T>(), sizeof(T) == 4 ? V2_MINB_F : 2)
 kb_filter(const BCase<T>* cases, const int4* items, int nitems, UCo<T, CH> U, BatchCtl ctl) {
