@@ -95,6 +95,14 @@ struct StageMap {
   }
 };
 
+// The block shape every tiled kernel assumes, NL lines x 32 chunks
+// (v2_block on the host): a launch of any other shape returns at once
+// instead of indexing its tiles out of range.
+template <typename T>
+__device__ __forceinline__ bool v2_shape_ok() {
+  return blockDim.x == (unsigned)v2_nl<T>() && blockDim.y == 32 && blockDim.z == 1;
+}
+
 // Asynchronous global -> shared copy of one element (cp.async, completed
 // by cp_async_wait_all); an invalid element is written as zero without a
 // read (source size 0).
@@ -852,6 +860,7 @@ template <typename T, int DIR, int CH>
 __global__ void __launch_bounds__(v2_nt<T>(), sizeof(T) == 4 ? V2_MINB_F : 2)
 k2_filter(Geo g, DevT<T> d, DScheme<T> S, UCo<T, CH> U, FTab<T> Tb, int P) {
   extern __shared__ __align__(16) unsigned char v2_smem[];
+  if (!v2_shape_ok<T>()) return;
   __shared__ Geo sg;
   __shared__ DevT<T> sd;
   __shared__ DScheme<T> sS;
@@ -869,12 +878,14 @@ template <typename T, int DIR, int CH>
 __global__ void __launch_bounds__(v2_nt<T>(), V2_MINB)
 k2_convgrad(Geo g, DevT<T> d, DScheme<T> S, UCo<T, CH> U, CGFlags fl, int P) {
   extern __shared__ __align__(16) unsigned char v2_smem[];
+  if (!v2_shape_ok<T>()) return;
   convgrad_body<T, DIR, CH>(g, d, S, U, fl, P, vb_grid(), v2_smem);
 }
 template <typename T, int DIR, int CH>
 __global__ void __launch_bounds__(v2_nt<T>(), sizeof(T) == 4 ? V2_MINB_V : 2)
 k2_visc(Geo g, DevT<T> d, DScheme<T> S, UCo<T, CH> U, int P) {
   extern __shared__ __align__(16) unsigned char v2_smem[];
+  if (!v2_shape_ok<T>()) return;
   visc_body<T, DIR, CH>(g, d, S, U, P, vb_grid(), v2_smem);
 }
 
@@ -893,6 +904,11 @@ inline dim3 v2_grid(const Geo& g, int NL, int nz) {
 // the template arguments), never per launch: the call is not a stream
 // operation, and made per launch it kept batches on separate streams from
 // running concurrently.
+template <typename T>
+inline dim3 v2_block() {
+  return dim3(v2_nl<T>(), 32);
+}
+
 template <class K>
 inline cudaError_t v2_allow_smem(K kern, size_t bytes) {
   return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
@@ -913,7 +929,7 @@ cudaError_t launch2_filter_ch(const V2Args<T>& a, cudaStream_t st, int vsplit) {
   static const cudaError_t e = v2_allow_smem(k2_filter<T, DIR, CHC>, smem);
   if (e != cudaSuccess) return e;
   const dim3 gr = v2_grid<DIR>(a.g, v2_nl<T>(), vsplit ? 5 : 1);
-  k2_filter<T, DIR, CHC><<<gr, dim3(v2_nl<T>(), 32), smem, st>>>(a.g, a.d, a.S, make_uco<T, CHC>(a),
+  k2_filter<T, DIR, CHC><<<gr, v2_block<T>(), smem, st>>>(a.g, a.d, a.S, make_uco<T, CHC>(a),
                                                                   a.Tb, P);
   return cudaGetLastError();
 }
@@ -925,7 +941,7 @@ cudaError_t launch2_convgrad_ch(const V2Args<T>& a, cudaStream_t st, CGFlags f, 
   if (e != cudaSuccess) return e;
   const int ntask = (f.conv ? 5 : 0) + (f.grad ? 4 : 0);
   const dim3 gr = v2_grid<DIR>(a.g, v2_nl<T>(), vsplit && ntask > 1 ? ntask : 1);
-  k2_convgrad<T, DIR, CHC><<<gr, dim3(v2_nl<T>(), 32), smem, st>>>(a.g, a.d, a.S,
+  k2_convgrad<T, DIR, CHC><<<gr, v2_block<T>(), smem, st>>>(a.g, a.d, a.S,
                                                                     make_uco<T, CHC>(a), f, P);
   return cudaGetLastError();
 }
@@ -936,7 +952,7 @@ cudaError_t launch2_visc_ch(const V2Args<T>& a, cudaStream_t st, int vsplit) {
   static const cudaError_t e = v2_allow_smem(k2_visc<T, DIR, CHC>, smem);
   if (e != cudaSuccess) return e;
   const dim3 gr = v2_grid<DIR>(a.g, v2_nl<T>(), vsplit ? 4 : 1);
-  k2_visc<T, DIR, CHC><<<gr, dim3(v2_nl<T>(), 32), smem, st>>>(a.g, a.d, a.S, make_uco<T, CHC>(a), P);
+  k2_visc<T, DIR, CHC><<<gr, v2_block<T>(), smem, st>>>(a.g, a.d, a.S, make_uco<T, CHC>(a), P);
   return cudaGetLastError();
 }
 
@@ -969,6 +985,7 @@ template <typename T, int DIR, int CH>
 __global__ void __launch_bounds__(v2_nt<T>(), sizeof(T) == 4 ? V2_MINB_F : 2)
 kb_filter(const BCase<T>* cases, const int4* items, int nitems, UCo<T, CH> U, BatchCtl ctl) {
   extern __shared__ __align__(16) unsigned char v2_smem[];
+  if (!v2_shape_ok<T>()) return;
   __shared__ int stop;
   __shared__ Geo sg;
   __shared__ DevT<T> sd;
@@ -993,6 +1010,7 @@ template <typename T, int DIR, int CH>
 __global__ void __launch_bounds__(v2_nt<T>(), V2_MINB)
 kb_convgrad(const BCase<T>* cases, const int4* items, int nitems, UCo<T, CH> U, BatchCtl ctl) {
   extern __shared__ __align__(16) unsigned char v2_smem[];
+  if (!v2_shape_ok<T>()) return;
   __shared__ int stop;
   __shared__ Geo sg;
   __shared__ DevT<T> sd;
@@ -1020,6 +1038,7 @@ template <typename T, int DIR, int CH>
 __global__ void __launch_bounds__(v2_nt<T>(), sizeof(T) == 4 ? V2_MINB_V : 2)
 kb_visc(const BCase<T>* cases, const int4* items, int nitems, UCo<T, CH> U, BatchCtl ctl) {
   extern __shared__ __align__(16) unsigned char v2_smem[];
+  if (!v2_shape_ok<T>()) return;
   __shared__ int stop;
   __shared__ Geo sg;
   __shared__ DevT<T> sd;
@@ -1051,7 +1070,7 @@ cudaError_t launchb_ch(int kind, const V2Args<T>& a, const BCase<T>* cases, cons
   const int minb = kind == 0 ? (sizeof(T) == 4 ? V2_MINB_F : 2)
                              : (kind == 1 ? V2_MINB : (sizeof(T) == 4 ? V2_MINB_V : 2));
   const unsigned grid = (unsigned)std::min(nitems, nsm * minb);
-  const dim3 bl(v2_nl<T>(), 32);
+  const dim3 bl = v2_block<T>();
   const UCo<T, CHC> U = make_uco<T, CHC>(a);
   if (kind == 0) {
     static const cudaError_t e = v2_allow_smem(kb_filter<T, DIR, CHC>, smem);
