@@ -48,7 +48,7 @@ EXPORTS = [
     "astr_batch_create", "astr_batch_destroy", "astr_batch_add", "astr_batch_remove",
     "astr_batch_size", "astr_batch_step_async", "astr_batch_poll", "astr_batch_wait",
     "astr_batch_cancel", "astr_batch_step", "astr_batch_last_error", "astr_batch_launch_count",
-    "astr_batch_set_share",
+    "astr_batch_set_share", "astr_gpu_set_inflow",
 ]
 NOALLOC_STATS_MAX_BLOCKS = 65536
 KERNEL_CLASSES = ["filter", "halo", "convgrad", "visc", "pointwise", "stats", "mp"]
@@ -155,6 +155,8 @@ def load(path: str = LIB_PATH):
     L.astr_gpu_poll.restype = ip
     L.astr_gpu_set_grid.argtypes = [vp, dp]
     L.astr_gpu_set_grid.restype = ip
+    L.astr_gpu_set_inflow.argtypes = [vp, dp, dp, dp]
+    L.astr_gpu_set_inflow.restype = ip
     L.astr_gpu_channel_state.argtypes = [vp, dp]
     L.astr_gpu_channel_state.restype = ip
     L.astr_batch_create.argtypes = [ip, ctypes.POINTER(vp)]

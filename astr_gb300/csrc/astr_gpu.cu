@@ -315,7 +315,10 @@ __global__ void k_batch_gate(BatchCtl ctl) {
 //      temperature on ymax only;
 //   60 symmetry (2664-2996): x faces and zmax remove the velocity along the
 //      metric row's unit vector, y faces and zmin zero the normal component;
-//      q with temperature on the x faces, ymax and zmax.
+//      q with temperature on the x faces, ymax and zmax;
+//   11 inflow (1366-1562, xmin): v, w, T from the inflow arrays, p from the
+//      incoming characteristic blended towards pinf, u from p; q with
+//      temperature.
 // extrapolate(v1, v2, 0) is (4 v1 - v2)/3 (extrapolate_2o,
 // src/commfunc.F90:277-285).
 __device__ __forceinline__ double bc_ex2(double v1, double v2) {
@@ -325,7 +328,7 @@ __device__ __forceinline__ double bc_ex2(double v1, double v2) {
 template <typename T>
 __global__ void k_face_bc(Geo g, DevT<T> d, Phys ph, int n, int type, double tw, double const1,
                           double const6, double pinf, double adt, double mach,
-                          const unsigned char* slip) {
+                          const unsigned char* slip, const double* inflow) {
   const int dir = n / 2, side = n % 2;
   const int na = (dir == 0 ? g.jm : g.im) + 1;
   const int nb = (dir == 2 ? g.jm : g.km) + 1;
@@ -382,6 +385,27 @@ __global__ void k_face_bc(Geo g, DevT<T> d, Phys ph, int n, int type, double tw,
     v = n == 3 ? (1.0 / 3.0) * (4.0 * prim(p1, 2) - prim(p2, 2)) : 0.0;
     w = 0.0;
     ro = pe / te * c2;
+  } else if (type == 11) {
+    // inflow xmin (1366-1562, its active subsonic branch): node (j, k) =
+    // (a, b) of the face; inflow = vel_in(0:jm,0:km,1:3), tmp_in(0:jm,0:km),
+    // tmp_prof(0:jm); rho_ref the first interior node; css the speed of
+    // sound of the profile temperature; blend -> 1 as the inflow Mach
+    // number passes 1
+    const long long nf = (long long)(g.jm + 1) * (g.km + 1), fj = (long long)a + (long long)(g.jm + 1) * b;
+    const double vin1 = inflow[fj], vin2 = inflow[fj + nf], vin3 = inflow[fj + 2 * nf];
+    const double rho_ref = prim(p1, 0);
+    const double css = sqrt(inflow[4 * nf + a]) / mach;
+    const double pex = bc_ex2(prim(p1, 4), prim(p2, 4));
+    const double ue = bc_ex2(prim(p1, 1), prim(p2, 1));
+    const double malo = vin1 / css;
+    const double blend = 0.5 * (tanh((malo - 1.0) * 6.0) + 1.0);
+    pe = (0.5 * (pinf + pex) + 0.5 * rho_ref * css * (vin1 - ue)) * (1.0 - blend) + pinf * blend;
+    u = vin1 + (pinf - pe) / rho_ref / css;
+    v = vin2;
+    w = vin3;
+    te = inflow[3 * nf + fj];
+    ro = pe / te * c2;
+    tform = true;
   } else if (type == 21 && n == 1) {
     // outflow xmax (3427-3532): the i-1 node copied (its supersonic branch
     // is taken unconditionally); q in temperature form
@@ -1195,6 +1219,8 @@ struct astr_ctx {
   int chan_nblk = 0;
   double* ycoord = nullptr;     // y coordinates, halo layout
   unsigned char* slip_mask = nullptr;  // 411 on ymin: node (i, k) at x <= xslip
+  // 11 on xmin: vel_in(0:jm,0:km,1:3), tmp_in(0:jm,0:km), tmp_prof(0:jm)
+  double* inflow = nullptr;
   double chan_ly = 0.0;         // ymax - ymin
   long long nstep = 0;          // completed time steps (statcal's nstep)
   bool rkfirst_called = false;  // rkfirst's firstcall flag
@@ -1606,13 +1632,13 @@ int run_boucon(astr_ctx* c) {
   for (int n = 0; n < 2 * g.ndims; ++n) {
     const int type = c->bct[n];
     if (type != 41 && type != 42 && type != 50 && type != 60 && type != 421 && type != 21 &&
-        type != 51 && type != 411)
+        type != 51 && type != 411 && type != 11)
       continue;
     const int dir = n / 2;
     const long long cnt = (long long)((dir == 0 ? g.jm : g.im) + 1) * ((dir == 2 ? g.jm : g.km) + 1);
     prof_begin(c, KC_HALO);
     k_face_bc<T><<<point_grid(cnt), 256, 0, c->st>>>(g, dev<T>(c), c->ph, n, type, c->btw[n], const1,
-                                                     const6, pinf, adt, mach, c->slip_mask);
+                                                     const6, pinf, adt, mach, c->slip_mask, c->inflow);
     prof_end(c);
     RC(after_launch(c, "k_face_bc"));
   }
@@ -1854,6 +1880,25 @@ int rhscal_t(astr_ctx* c) {
 // ---------------------------------------------------------------------------
 extern "C" {
 
+// The inflow arrays of bctype 11 into HBM: vel_in(0:jm,0:km,1:3),
+// tmp_in(0:jm,0:km), tmp_prof(0:jm); a NULL array takes freestreaminflow's
+// values (src/bc.F90:7950-8003: uinf = 1, vinf = winf = 0, tinf = 1).
+static int inflow_upload(astr_ctx* c, const double* vel_in, const double* tmp_in,
+                         const double* tmp_prof) {
+  const size_t nf = (size_t)(c->g.jm + 1) * (c->g.km + 1), nj = (size_t)c->g.jm + 1;
+  std::vector<double> h(4 * nf + nj);
+  for (size_t t = 0; t < 3 * nf; ++t) h[t] = vel_in ? vel_in[t] : (t < nf ? 1.0 : 0.0);
+  for (size_t t = 0; t < nf; ++t) h[3 * nf + t] = tmp_in ? tmp_in[t] : 1.0;
+  for (size_t t = 0; t < nj; ++t) h[4 * nf + t] = tmp_prof ? tmp_prof[t] : 1.0;
+  for (double v : h)
+    if (!std::isfinite(v)) return fail(c, ASTR_ERR_ARG, "inflow arrays: a non-finite value");
+  for (size_t t = 3 * nf; t < h.size(); ++t)
+    if (!(h[t] > 0.0)) return fail(c, ASTR_ERR_ARG, "inflow temperatures must be > 0");
+  CK(cudaMemcpyAsync(c->inflow, h.data(), h.size() * 8, cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return ASTR_OK;
+}
+
 size_t astr_gpu_footprint(const astr_dims* dims, const astr_params* params) {
   if (!dims) return 0;
   const size_t nh = (size_t)(dims->im + 2 * HMD + 1) * (dims->jm + 2 * HMD + 1) * (dims->km + 2 * HMD + 1);
@@ -1870,6 +1915,8 @@ size_t astr_gpu_footprint(const astr_dims* dims, const astr_params* params) {
   // flux 5, sensor 1 (halo arrays, FP64), the shock flags (bytes) and the
   // list of flagged interfaces (at most nh ints)
   if (params && params->conschm == ASTR_CONSCHM_MP) b += 8 * 26 * nh + n0 + 4 * nh;
+  if (params && params->bctype[0] == 11)  // inflow arrays
+    b += 8 * (4 * (size_t)(dims->jm + 1) * (dims->km + 1) + (size_t)(dims->jm + 1));
   return b;
 }
 
@@ -1896,9 +1943,11 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
     if (params->channel && (n == 2 || n == 3) && (bct[n] == 0 || bct[n] == 1)) bct[n] = 41;
     if (bct[n] == 0 || bct[n] == 1) continue;
     if (bct[n] != 41 && bct[n] != 42 && bct[n] != 50 && bct[n] != 60 && bct[n] != 421 &&
-        bct[n] != 21 && bct[n] != 51 && bct[n] != 411)
+        bct[n] != 21 && bct[n] != 51 && bct[n] != 411 && bct[n] != 11)
       return fail(nullptr, ASTR_ERR_UNSUPPORTED,
-                  "bctype: 21, 41, 42, 411, 421, 50, 51 and 60 are built (0/1: none)");
+                  "bctype: 11, 21, 41, 42, 411, 421, 50, 51 and 60 are built (0/1: none)");
+    if (bct[n] == 11 && n != 0)
+      return fail(nullptr, ASTR_ERR_UNSUPPORTED, "bctype 11 exists for the xmin face only");
     if (bct[n] == 51 && n < 2)
       return fail(nullptr, ASTR_ERR_UNSUPPORTED, "bctype 51 exists for the y and z faces only");
     if (bct[n] == 21 && n != 1 && n != 3)
@@ -2066,6 +2115,8 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
     c->ycoord = (double*)alloc(nh * 8);
   }
   if (bct[2] == 411) c->slip_mask = (unsigned char*)alloc((size_t)(g.im + 1) * (g.km + 1));
+  const size_t n_inflow = 4 * (size_t)(g.jm + 1) * (g.km + 1) + (size_t)(g.jm + 1);
+  if (bct[0] == 11) c->inflow = (double*)alloc(n_inflow * 8);
   // schemes: per direction derivative + filter, in both precisions
   std::vector<HostScheme> hs;
   for (int dd = 0; dd < 3; ++dd) {
@@ -2282,6 +2333,14 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
     }
     c->mp = true;
   }
+  if (c->inflow) {
+    const int rc = inflow_upload(c, nullptr, nullptr, nullptr);
+    if (rc != ASTR_OK) {
+      std::string msg = c->err;
+      astr_gpu_destroy(c);
+      return fail(nullptr, rc, msg);
+    }
+  }
   *out = c;
   return ASTR_OK;
 }
@@ -2393,6 +2452,12 @@ int astr_gpu_set_grid(astr_ctx* c, const double* x) {
   CK(cudaStreamSynchronize(c->st));
   c->grid_set = true;
   return ASTR_OK;
+}
+
+int astr_gpu_set_inflow(astr_ctx* c, const double* vel_in, const double* tmp_in, const double* tmp_prof) {
+  if (!c) return fail(c, ASTR_ERR_ARG, "null context");
+  if (!c->inflow) return fail(c, ASTR_ERR_STATE, "no inflow face (bctype 11 on xmin)");
+  return inflow_upload(c, vel_in, tmp_in, tmp_prof);
 }
 
 int astr_gpu_channel_state(astr_ctx* c, double* out) {

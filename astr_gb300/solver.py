@@ -119,6 +119,21 @@ class GpuSolver:
         x = _f(x, halo_shape(self.im, self.jm, self.km, 3))
         self._c(self.L.astr_gpu_set_grid(self.h, capi.dptr(x)))
 
+    def set_inflow(self, vel_in=None, tmp_in=None, tmp_prof=None):
+        """Inflow arrays of bctype 11 on xmin: vel_in (jm+1, km+1, 3),
+        tmp_in (jm+1, km+1), tmp_prof (jm+1); None keeps the freestream."""
+        nj, nk = self.jm + 1, self.km + 1
+        args = []
+        for a, shape in ((vel_in, (nj, nk, 3)), (tmp_in, (nj, nk)), (tmp_prof, (nj,))):
+            if a is None:
+                args.append(None)
+                continue
+            a = np.asarray(a, dtype=np.float64)
+            if a.shape != shape:
+                raise ValueError(f"inflow array of shape {a.shape}, want {shape}")
+            args.append(np.asfortranarray(a))
+        self._c(self.L.astr_gpu_set_inflow(self.h, *(capi.dptr(a) for a in args)))
+
     def channel_state(self):
         """(force(1), mass flux, target mass flux, wall friction, steps)."""
         out = np.zeros(5)

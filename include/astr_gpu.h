@@ -139,6 +139,16 @@ int astr_gpu_set_metrics(astr_ctx* ctx, const double* dxi, const double* jacob);
  * which of that face's nodes lie at x <= xslip; others ignore the call. */
 int astr_gpu_set_grid(astr_ctx* ctx, const double* x);
 
+/* Inflow arrays of bctype 11 on xmin (inflow, src/bc.F90:1366-1562):
+ * vel_in(0:jm,0:km,1:3), tmp_in(0:jm,0:km) and tmp_prof(0:jm) in Fortran
+ * layout, the values alloinflow's arrays hold after the profile routine
+ * (freestreaminflow, profileinflow, ...).  A NULL array takes
+ * freestreaminflow's values (u = 1, v = w = 0, T = 1), which a context
+ * with bctype 11 starts from.  The turbulent inflow fluctuations (turbinf)
+ * are not applied.  ASTR_ERR_STATE without an inflow face. */
+int astr_gpu_set_inflow(astr_ctx* ctx, const double* vel_in, const double* tmp_in,
+                        const double* tmp_prof);
+
 /* Asynchronous stepping (no counterpart in the reference; used by the
  * request loop that serves many independent cases on one GPU): enqueue
  * nsteps RK3 steps on the context's stream and return at once, without

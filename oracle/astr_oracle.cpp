@@ -79,6 +79,10 @@ struct orc_ctx {
   std::vector<double> qrhs, qsave, dvel, dtmp;
   std::vector<double> ssf;              // shock-sensor function (halo array)
   std::vector<unsigned char> lshock;    // lshock(0:im,0:jm,0:km)
+  // inflow (bctype 11 on xmin): vel_in(0:jm,0:km,1:3), tmp_in(0:jm,0:km),
+  // tmp_prof(0:jm) (alloinflow, src/bc.F90:69-83; freestreaminflow's
+  // values, src/bc.F90:7950-8003, until the host sets a profile)
+  std::vector<double> vel_in, tmp_in, tmp_prof;
   bool sson = false;                    // allocated(lshock)
   double force[3] = {0, 0, 0};
   double massflux_target = 0.0;
@@ -852,6 +856,11 @@ orc_ctx* orc_create(const orc_config* cfg) {
   // they hold zero
   c->ssf.assign(c->nh, 0.0);
   c->lshock.assign(c->n0, 0);
+  const size_t nf = (size_t)(c->jm + 1) * (c->km + 1);
+  c->vel_in.assign(3 * nf, 0.0);
+  for (size_t t = 0; t < nf; ++t) c->vel_in[t] = c->uinf;  // (uinf, vinf = 0, winf = 0)
+  c->tmp_in.assign(nf, c->tinf);
+  c->tmp_prof.assign((size_t)c->jm + 1, c->tinf);
   return c;
 }
 
@@ -865,6 +874,9 @@ double* orc_field(orc_ctx* c, const char* name) {
   if (s == "prs") return c->prs.data();
   if (s == "tmp") return c->tmp.data();
   if (s == "x") return c->x.data();
+  if (s == "vel_in") return c->vel_in.data();
+  if (s == "tmp_in") return c->tmp_in.data();
+  if (s == "tmp_prof") return c->tmp_prof.data();
   if (s == "dxi") return c->dxi.data();
   if (s == "jacob") return c->jacob.data();
   if (s == "sigma") return c->sigma.data();
@@ -1435,6 +1447,28 @@ void face_node(orc_ctx& c, int n, int type, double tw, int i, int j, int k) {
     }
     T[p] = P[p] / R[p] * c.const2;
     fvar2q_prs_node(c, p);
+  } else if (type == 11) {  // inflow xmin, src/bc.F90:1366-1562 (its active, subsonic branch)
+    // v, w and T from the inflow arrays; p from the incoming characteristic
+    // against pinf blended towards pinf by the local inflow Mach number
+    // (the speed of sound of the profile temperature); u from p; rho from
+    // p and T; q in temperature form.  rho_ref is the first interior node.
+    const size_t fj = (size_t)j + (size_t)(c.jm + 1) * (size_t)k;
+    const size_t nf = (size_t)(c.jm + 1) * (c.km + 1);
+    const double vin1 = c.vel_in[fj], vin2 = c.vel_in[fj + nf], vin3 = c.vel_in[fj + 2 * nf];
+    const double rho_ref = R[p1];
+    const double css = std::sqrt(c.tmp_prof[j]) / c.cfg.mach;
+    V[p + nh] = vin2;
+    V[p + 2 * nh] = vin3;
+    T[p] = c.tmp_in[fj];
+    const double pe = ex2(P[p1], P[p2]);
+    const double ue = ex2(V[p1], V[p2]);
+    const double pwave_in = c.pinf;
+    const double malo = vin1 / css;
+    const double blend = 0.5 * (std::tanh((malo - 1.0) * 6.0) + 1.0);
+    P[p] = (0.5 * (pwave_in + pe) + 0.5 * rho_ref * css * (vin1 - ue)) * (1.0 - blend) + pwave_in * blend;
+    V[p] = vin1 + (c.pinf - P[p]) / rho_ref / css;
+    R[p] = P[p] / T[p] * c.const2;
+    fvar2q_tmp_node(c, p);
   } else if (type == 50) {  // zeroextrap, src/bc.F90:2356-2652
     const double ue = ex2(V[p1], V[p2]), ve = ex2(V[p1 + nh], V[p2 + nh]);
     const double we = ex2(V[p1 + 2 * nh], V[p2 + 2 * nh]);
@@ -1502,11 +1536,11 @@ void orc_boucon(orc_ctx* c) {
   for (int n = 0; n < 2 * c->ndims; ++n) {
     const int type = face_bctype(*c, n);
     if (type != 41 && type != 42 && type != 50 && type != 60 && type != 421 && type != 21 &&
-        type != 51 && type != 411)
+        type != 51 && type != 411 && type != 11)
       continue;
     const int d = n / 2;
     if (c->npdc(d) != 4 || ((type == 421 || type == 411) && d != 1) ||
-        (type == 21 && n != 1 && n != 3) || (type == 51 && d == 0))
+        (type == 21 && n != 1 && n != 3) || (type == 51 && d == 0) || (type == 11 && n != 0))
       continue;
     const double tw = face_twall(*c, n);
     const int a1 = d == 0 ? c->jm : c->im, b1 = d == 2 ? c->jm : c->km;

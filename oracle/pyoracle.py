@@ -171,6 +171,17 @@ class Oracle:
         buf = np.ctypeslib.as_array(p, shape=(count,))
         return buf.reshape(shape, order="F")
 
+    def inflow(self):
+        """Views of the inflow arrays of bctype 11 (freestream values until
+        set): vel_in (jm+1, km+1, 3), tmp_in (jm+1, km+1), tmp_prof (jm+1)."""
+        nj, nk = self.jm + 1, self.km + 1
+        out = {}
+        for name, shape in (("vel_in", (nj, nk, 3)), ("tmp_in", (nj, nk)), ("tmp_prof", (nj,))):
+            p = self.L.orc_field(self.h, name.encode())
+            buf = np.ctypeslib.as_array(p, shape=(int(np.prod(shape)),))
+            out[name] = buf.reshape(shape, order="F")
+        return out
+
     def scheme(self, d: int, kind: int):
         first = ctypes.c_int()
         out = np.zeros(5 * 4200)

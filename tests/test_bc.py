@@ -1,7 +1,7 @@
 """Boundary routines of boucon (src/bc.F90:327-409) in the oracle, on CPU:
 the face values each routine sets (41 isothermal no-slip, 42 adiabatic
 no-slip, 411 isothermal slip/no-slip wall, 421 adiabatic slip wall, 21
-outflow, 51 farfield, 50
+outflow, 51 farfield, 11 inflow, 50
 zero-gradient extrapolation, 60 symmetry), and a closed box
 stepping stably with walls on every face."""
 import numpy as np
@@ -224,3 +224,57 @@ def test_closed_box_steps():
     vel = o.field("vel")
     assert np.all(_face(vel, 0) == 0.0) and np.all(_face(vel, 1) == 0.0)
     assert np.all(_face(vel[..., 1], 3) == 0.0)
+
+
+def _inflow_profile(o):
+    """A non-uniform inflow (vel_in, tmp_in, tmp_prof) in the oracle's
+    arrays, returned as copies."""
+    f = o.inflow()
+    nj, nk = f["tmp_in"].shape
+    J = np.arange(nj).reshape(-1, 1) * (2 * np.pi / (nj - 1))
+    K = np.arange(nk).reshape(1, -1) * (2 * np.pi / max(nk - 1, 1))
+    f["vel_in"][..., 0] = 1.0 + 0.1 * np.sin(J) * np.cos(K)
+    f["vel_in"][..., 1] = 0.05 * np.cos(K) * np.ones_like(J)
+    f["vel_in"][..., 2] = 0.02 * np.sin(J + K)
+    f["tmp_in"][...] = 1.0 + 0.05 * np.sin(J + 0.3) * np.ones_like(K)
+    f["tmp_prof"][...] = 1.0 + 0.03 * np.cos(np.arange(nj) * 0.4)
+    return {k: v.copy() for k, v in f.items()}
+
+
+@pytest.mark.parametrize("profile", [False, True])
+def test_inflow_face_values(profile):
+    """11 (inflow, src/bc.F90:1366-1562) on xmin: v, w, T from the inflow
+    arrays; p from the incoming characteristic against pinf, blended towards
+    pinf by tanh of the inflow Mach number (speed of sound of the profile
+    temperature); u = u_in + (pinf - p)/(rho_1 css); rho from p and T; q in
+    temperature form.  Freestream arrays (u 1, T 1) or a profile."""
+    o = bc_oracle((24, 20, 16), (4, 3, 3), (11, 21, 0, 0, 0, 0), deltat=2e-3)
+    if profile:
+        f = _inflow_profile(o)
+    else:
+        f = {k: v.copy() for k, v in o.inflow().items()}
+        assert np.all(f["vel_in"][..., 0] == 1.0) and np.all(f["vel_in"][..., 1:] == 0.0)
+        assert np.all(f["tmp_in"] == 1.0) and np.all(f["tmp_prof"] == 1.0)
+    before = {k: o.field(k).copy() for k in ("vel", "prs", "tmp", "rho")}
+    o.call("boucon")
+    c = cases.refcal(MACH, 400.0)
+    const1, const2, pinf = c["const1"], c["const2"], c["pinf"]
+    sl0 = (H, slice(H, H + o.jm + 1), slice(H, H + o.km + 1))
+    sl1 = (H + 1,) + sl0[1:]
+    sl2 = (H + 2,) + sl0[1:]
+    ex = lambda a: (4.0 * a[sl1] - a[sl2]) / 3.0
+    vin = f["vel_in"]
+    css = (np.sqrt(f["tmp_prof"]) / MACH).reshape(-1, 1)
+    rho_ref = before["rho"][sl1]
+    pe, ue = ex(before["prs"]), ex(before["vel"][..., 0])
+    blend = 0.5 * (np.tanh((vin[..., 0] / css - 1.0) * 6.0) + 1.0)
+    p = (0.5 * (pinf + pe) + 0.5 * rho_ref * css * (vin[..., 0] - ue)) * (1.0 - blend) + pinf * blend
+    vel, prs, tmp, rho, q = (o.field(k) for k in ("vel", "prs", "tmp", "rho", "q"))
+    np.testing.assert_allclose(prs[sl0], p, rtol=1e-14)
+    np.testing.assert_allclose(vel[sl0 + (0,)], vin[..., 0] + (pinf - p) / rho_ref / css, rtol=1e-14)
+    assert np.array_equal(vel[sl0 + (1,)], vin[..., 1]) and np.array_equal(vel[sl0 + (2,)], vin[..., 2])
+    assert np.array_equal(tmp[sl0], f["tmp_in"])
+    np.testing.assert_allclose(rho[sl0], p / f["tmp_in"] * const2, rtol=1e-15)
+    e = rho[sl0] * (tmp[sl0] * const1 + 0.5 * (vel[sl0] ** 2).sum(axis=-1))
+    np.testing.assert_allclose(q[sl0 + (4,)], e, rtol=1e-14)
+    assert blend.max() < 1e-3  # subsonic inflow: the characteristic branch dominates

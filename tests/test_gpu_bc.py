@@ -4,7 +4,8 @@ no-slip, symmetry, zero-gradient extrapolation), slip walls (isothermal with
 a slip region, adiabatic) on the y faces, outflow on xmax and ymax, farfield on the y and z faces, the
 viscous terms and the
 filter; a skewed curvilinear box where the symmetry faces project on the
-metric normal; and the FP32-storage form against FP64."""
+metric normal; inflow on xmin (freestream and a profile) with outflow on
+xmax; and the FP32-storage form against FP64."""
 import numpy as np
 import pytest
 
@@ -176,5 +177,39 @@ def test_boundary_routine_checks(gpu_lib):
         GpuSolver(16, 16, 16, bctype=(41, 0, 0, 0, 0, 0))
     with pytest.raises(capi.AstrError):   # adiabatic no-slip exists for x and y faces only
         GpuSolver(16, 16, 16, npdc=(3, 3, 4), bctype=(0, 0, 0, 0, 42, 0))
-    with pytest.raises(capi.AstrError):   # not built
-        GpuSolver(16, 16, 16, npdc=(4, 3, 3), bctype=(11, 21, 0, 0, 0, 0))
+    with pytest.raises(capi.AstrError):   # not built (inflow_nscbc)
+        GpuSolver(16, 16, 16, npdc=(4, 3, 3), bctype=(12, 21, 0, 0, 0, 0))
+
+
+@pytest.mark.parametrize("profile", [False, True])
+def test_inflow_outflow_match_oracle(gpu_lib, profile):
+    """11 on xmin (freestream arrays, or a profile through
+    astr_gpu_set_inflow), 21 on xmax, y and z periodic, viscous with the
+    filter."""
+    from test_bc import _inflow_profile
+    o = bc_oracle((24, 20, 16), (4, 3, 3), (11, 21, 0, 0, 0, 0), deltat=2e-3, lfilter=True)
+    g = _gpu_from(o)
+    if profile:
+        f = _inflow_profile(o)
+        g.set_inflow(f["vel_in"], f["tmp_in"], f["tmp_prof"])
+    o.rk3_steps(4)
+    g.time_integration_rk(4)
+    s = g.download_state()
+    g.close()
+    _cmp(o, s)
+
+
+def test_inflow_arguments(gpu_lib):
+    """bctype 11 exists on xmin only; set_inflow needs an inflow face and
+    positive temperatures."""
+    from astr_gb300.solver import GpuSolver
+    with pytest.raises(capi.AstrError, match="xmin"):
+        GpuSolver(16, 16, 16, npdc=(4, 4, 3), bctype=(0, 0, 11, 0, 0, 0))
+    g = GpuSolver(16, 16, 16, npdc=(4, 3, 3), bctype=(11, 21, 0, 0, 0, 0))
+    with pytest.raises(capi.AstrError, match="> 0"):
+        g.set_inflow(tmp_prof=np.zeros(17))
+    g.close()
+    g = GpuSolver(16, 16, 16)
+    with pytest.raises(capi.AstrError, match="no inflow face"):
+        g.set_inflow()
+    g.close()
