@@ -318,7 +318,10 @@ __global__ void k_batch_gate(BatchCtl ctl) {
 //      q with temperature on the x faces, ymax and zmax;
 //   11 inflow (1366-1562, xmin): v, w, T from the inflow arrays, p from the
 //      incoming characteristic blended towards pinf, u from p; q with
-//      temperature.
+//      temperature;
+//   23 gcnscbc (8024-8254, xmax and ymax): LODI at node dim-1 relaxed
+//      towards pinf (ymax inflow: towards the free stream), extrapolated
+//      over 2 dx; q with pressure.
 // extrapolate(v1, v2, 0) is (4 v1 - v2)/3 (extrapolate_2o,
 // src/commfunc.F90:277-285).
 __device__ __forceinline__ double bc_ex2(double v1, double v2) {
@@ -328,7 +331,8 @@ __device__ __forceinline__ double bc_ex2(double v1, double v2) {
 template <typename T>
 __global__ void k_face_bc(Geo g, DevT<T> d, Phys ph, int n, int type, double tw, double const1,
                           double const6, double pinf, double adt, double mach,
-                          const unsigned char* slip, const double* inflow) {
+                          const unsigned char* slip, const double* inflow, const double* gcd,
+                          double gce) {
   const int dir = n / 2, side = n % 2;
   const int na = (dir == 0 ? g.jm : g.im) + 1;
   const int nb = (dir == 2 ? g.jm : g.km) + 1;
@@ -384,6 +388,63 @@ __global__ void k_face_bc(Geo g, DevT<T> d, Phys ph, int n, int type, double tw,
     u = (1.0 / 3.0) * (4.0 * prim(p1, 1) - prim(p2, 1));
     v = n == 3 ? (1.0 / 3.0) * (4.0 * prim(p1, 2) - prim(p2, 2)) : 0.0;
     w = 0.0;
+    ro = pe / te * c2;
+  } else if (type == 23) {
+    // gcnscbc xmax (8041-8148) / ymax (8150-8252), prs_t = pinf: gcd is
+    // the face's x(dim-1) - x(dim-2) along the normal, gce the grid's
+    // extent along it.  css, css2 and vnorm are INTEGER in the reference
+    // (src/bc.F90:8035): truncated, mavg an integer division, and
+    // lambda(5:numq) = vnorm leaves lambda(5) = vnorm.
+    const int on = dir, ot = dir == 0 ? 1 : 0;
+    const int css = (int)(sqrt(prim(p1, 5)) / mach);
+    const int css2 = css * css;
+    const int vnorm = (int)prim(p1, 1 + on);
+    const double mavg = css != 0 ? (double)(vnorm / css) : 0.0;
+    double lam[5] = {(double)(vnorm - css), (double)vnorm, (double)vnorm, (double)vnorm, (double)vnorm};
+    for (int m = 0; m < 5; ++m) lam[m] = lam[m] + 1e-10;
+    const double dx = gcd[idx];
+    // every product and sum rounded on its own (no contracted multiply-
+    // adds): the one-sided differences cancel, and the restatement the
+    // parity tests hold this to rounds each operation
+    auto M = [](double x, double y) { return __dmul_rn(x, y); };
+    auto A = [](double x, double y) { return __dadd_rn(x, y); };
+    auto S = [](double x, double y) { return __dsub_rn(x, y); };
+    const double r1 = prim(p1, 0), t1 = prim(p1, 5), pr1 = prim(p1, 4), cs = (double)css;
+    double dvel[3], dprs;
+    for (int m = 0; m < 3; ++m) dvel[m] = -S(prim(p2, 1 + m), prim(p1, 1 + m)) / dx;
+    dprs = -S(prim(p2, 4), pr1) / dx;
+    const double drho = -S(prim(p2, 0), r1) / dx;
+    double lodi[5];
+    lodi[0] = M(lam[0], S(dprs, M(M(r1, cs), dvel[on])));
+    lodi[1] = M(lam[1], S(M((double)css2, drho), dprs));
+    lodi[2] = M(lam[2], dvel[ot]);
+    lodi[3] = M(lam[3], dvel[2]);
+    lodi[4] = M(lam[4], A(dprs, M(M(r1, cs), dvel[on])));
+    const double m2 = S(1.0, M(mavg, mavg));
+    if (dir == 0 || vnorm >= 0) {
+      const double kamma = M(M(0.25, cs), m2) / gce;
+      lodi[0] = M(kamma, S(pr1, pinf));
+    } else {
+      // the free stream: uinf = 1, vinf = winf = 0, tinf = 1
+      const double eta = 0.25;
+      lodi[0] = M(M(M(M(eta, r1), (double)css2), m2) / gce, S(prim(p1, 1 + on), 0.0));
+      lodi[1] = M(M(M(eta, r1), (double)css2) / 1.4 / gce, S(t1, 1.0));
+      lodi[2] = M(M(eta, cs) / gce, S(prim(p1, 1 + ot), 1.0));
+      lodi[3] = M(M(eta, cs) / gce, S(prim(p1, 3), 0.0));
+    }
+    for (int m = 0; m < 5; ++m) lodi[m] = lodi[m] / lam[m];
+    const double l05 = A(lodi[0], lodi[4]);
+    const double dtmp = M(t1 / r1 / cs, A(-lodi[1], M(0.5 * (1.4 - 1.0), l05)));
+    dprs = M(0.5, l05);
+    dvel[on] = M(1.0 / M(M(2.0, r1), cs), S(lodi[4], lodi[0]));
+    dvel[ot] = lodi[2];
+    dvel[2] = lodi[3];
+    const double dx2 = M(2.0, dx);  // rho follows from p and T
+    te = A(t1, M(dx2, dtmp));
+    pe = A(pr1, M(dx2, dprs));
+    u = A(prim(p1, 1), M(dx2, dvel[0]));
+    v = A(prim(p1, 2), M(dx2, dvel[1]));
+    w = A(prim(p1, 3), M(dx2, dvel[2]));
     ro = pe / te * c2;
   } else if (type == 11) {
     // inflow xmin (1366-1562, its active subsonic branch): node (j, k) =
@@ -1221,6 +1282,10 @@ struct astr_ctx {
   unsigned char* slip_mask = nullptr;  // 411 on ymin: node (i, k) at x <= xslip
   // 11 on xmin: vel_in(0:jm,0:km,1:3), tmp_in(0:jm,0:km), tmp_prof(0:jm)
   double* inflow = nullptr;
+  // 23 on xmax / ymax (index 0 / 1): the face's normal spacing
+  // x(dim-1) - x(dim-2) per node and the grid's extent, from the grid
+  double* gc_dx[2] = {nullptr, nullptr};
+  double gc_ext[2] = {0.0, 0.0};
   double chan_ly = 0.0;         // ymax - ymin
   long long nstep = 0;          // completed time steps (statcal's nstep)
   bool rkfirst_called = false;  // rkfirst's firstcall flag
@@ -1632,13 +1697,15 @@ int run_boucon(astr_ctx* c) {
   for (int n = 0; n < 2 * g.ndims; ++n) {
     const int type = c->bct[n];
     if (type != 41 && type != 42 && type != 50 && type != 60 && type != 421 && type != 21 &&
-        type != 51 && type != 411 && type != 11)
+        type != 51 && type != 411 && type != 11 && type != 23)
       continue;
     const int dir = n / 2;
+    const int gi = n == 3 ? 1 : 0;
     const long long cnt = (long long)((dir == 0 ? g.jm : g.im) + 1) * ((dir == 2 ? g.jm : g.km) + 1);
     prof_begin(c, KC_HALO);
     k_face_bc<T><<<point_grid(cnt), 256, 0, c->st>>>(g, dev<T>(c), c->ph, n, type, c->btw[n], const1,
-                                                     const6, pinf, adt, mach, c->slip_mask, c->inflow);
+                                                     const6, pinf, adt, mach, c->slip_mask, c->inflow,
+                                                     c->gc_dx[gi], c->gc_ext[gi]);
     prof_end(c);
     RC(after_launch(c, "k_face_bc"));
   }
@@ -1943,9 +2010,11 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
     if (params->channel && (n == 2 || n == 3) && (bct[n] == 0 || bct[n] == 1)) bct[n] = 41;
     if (bct[n] == 0 || bct[n] == 1) continue;
     if (bct[n] != 41 && bct[n] != 42 && bct[n] != 50 && bct[n] != 60 && bct[n] != 421 &&
-        bct[n] != 21 && bct[n] != 51 && bct[n] != 411 && bct[n] != 11)
+        bct[n] != 21 && bct[n] != 51 && bct[n] != 411 && bct[n] != 11 && bct[n] != 23)
       return fail(nullptr, ASTR_ERR_UNSUPPORTED,
-                  "bctype: 11, 21, 41, 42, 411, 421, 50, 51 and 60 are built (0/1: none)");
+                  "bctype: 11, 21, 23, 41, 42, 411, 421, 50, 51 and 60 are built (0/1: none)");
+    if (bct[n] == 23 && n != 1 && n != 3)
+      return fail(nullptr, ASTR_ERR_UNSUPPORTED, "bctype 23 exists for the xmax and ymax faces only");
     if (bct[n] == 11 && n != 0)
       return fail(nullptr, ASTR_ERR_UNSUPPORTED, "bctype 11 exists for the xmin face only");
     if (bct[n] == 51 && n < 2)
@@ -2117,6 +2186,8 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
   if (bct[2] == 411) c->slip_mask = (unsigned char*)alloc((size_t)(g.im + 1) * (g.km + 1));
   const size_t n_inflow = 4 * (size_t)(g.jm + 1) * (g.km + 1) + (size_t)(g.jm + 1);
   if (bct[0] == 11) c->inflow = (double*)alloc(n_inflow * 8);
+  if (bct[1] == 23) c->gc_dx[0] = (double*)alloc((size_t)(g.jm + 1) * (g.km + 1) * 8);
+  if (bct[3] == 23) c->gc_dx[1] = (double*)alloc((size_t)(g.im + 1) * (g.km + 1) * 8);
   // schemes: per direction derivative + filter, in both precisions
   std::vector<HostScheme> hs;
   for (int dd = 0; dd < 3; ++dd) {
@@ -2427,7 +2498,7 @@ int astr_gpu_set_metrics(astr_ctx* c, const double* dxi, const double* jacob) {
 
 int astr_gpu_set_grid(astr_ctx* c, const double* x) {
   if (!c || !x) return fail(c, ASTR_ERR_ARG, "null argument");
-  if (!c->channel && !c->slip_mask) return ASTR_OK;
+  if (!c->channel && !c->slip_mask && !c->gc_dx[0] && !c->gc_dx[1]) return ASTR_OK;
   const size_t nh = (size_t)c->g.nh;
   const long long NI = c->g.NI, NJ = c->g.NJ;
   auto h = [&](int i, int j, int k) {
@@ -2443,6 +2514,30 @@ int astr_gpu_set_grid(astr_ctx* c, const double* x) {
       for (int i = 0; i <= im; ++i)
         mask[(size_t)i + (size_t)(im + 1) * k] = x[h(i, 0, k)] <= c->pm.xslip ? 1 : 0;
     CK(cudaMemcpyAsync(c->slip_mask, mask.data(), mask.size(), cudaMemcpyHostToDevice, c->st));
+  }
+  for (int f = 0; f < 2; ++f) {
+    // gcnscbc's spacing x(dim-1) - x(dim-2) along the face normal at every
+    // face node (the face kernel's order: j + (jm+1) k on xmax, i + (im+1) k
+    // on ymax) and the grid's extent along it (xmax - xmin, ymax - ymin)
+    if (!c->gc_dx[f]) continue;
+    const int im = c->g.im, jm = c->g.jm, km = c->g.km;
+    const double* xc = x + (size_t)f * nh;
+    double lo = 1e300, hi = -1e300;
+    for (int k = 0; k <= km; ++k)
+      for (int j = 0; j <= jm; ++j)
+        for (int i = 0; i <= im; ++i) {
+          lo = std::min(lo, xc[h(i, j, k)]);
+          hi = std::max(hi, xc[h(i, j, k)]);
+        }
+    c->gc_ext[f] = hi - lo;
+    const int na = f == 0 ? jm : im;
+    std::vector<double> dxv((size_t)(na + 1) * (km + 1));
+    for (int k = 0; k <= km; ++k)
+      for (int a = 0; a <= na; ++a)
+        dxv[(size_t)a + (size_t)(na + 1) * k] =
+            f == 0 ? xc[h(im - 1, a, k)] - xc[h(im - 2, a, k)] : xc[h(a, jm - 1, k)] - xc[h(a, jm - 2, k)];
+    CK(cudaMemcpyAsync(c->gc_dx[f], dxv.data(), dxv.size() * 8, cudaMemcpyHostToDevice, c->st));
+    CK(cudaStreamSynchronize(c->st));
   }
   if (c->channel) {
     const double* y = x + nh;  // x(..,2)
@@ -2659,8 +2754,8 @@ static int ready(astr_ctx* c) {
   if (!c->metrics_set && c->pm.order == ASTR_ORDER_MAIN)
     return fail(c, ASTR_ERR_STATE, "metrics not set (astr_gpu_set_metrics)");
   if (!c->state_set) return fail(c, ASTR_ERR_STATE, "state not uploaded (astr_gpu_upload_state)");
-  if ((c->channel || c->slip_mask) && !c->grid_set)
-    return fail(c, ASTR_ERR_STATE, "grid not set (astr_gpu_set_grid): a channel or bctype 411");
+  if ((c->channel || c->slip_mask || c->gc_dx[0] || c->gc_dx[1]) && !c->grid_set)
+    return fail(c, ASTR_ERR_STATE, "grid not set (astr_gpu_set_grid): a channel or bctype 411 or 23");
   return ASTR_OK;
 }
 

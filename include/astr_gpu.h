@@ -136,7 +136,9 @@ int astr_gpu_set_metrics(astr_ctx* ctx, const double* dxi, const double* jacob);
 /* Node coordinates x(-hm:..,1:3) in Fortran layout (gridgeom's x after its
  * halo fill).  A channel context keeps the y coordinates for the bulk
  * integrals of src_chan and massfluxchan; a context with 411 on ymin keeps
- * which of that face's nodes lie at x <= xslip; others ignore the call. */
+ * which of that face's nodes lie at x <= xslip; a context with 23 (gcnscbc)
+ * on xmax or ymax keeps that face's normal spacing and the grid's extent
+ * along it; others ignore the call. */
 int astr_gpu_set_grid(astr_ctx* ctx, const double* x);
 
 /* Inflow arrays of bctype 11 on xmin (inflow, src/bc.F90:1366-1562):

@@ -1321,7 +1321,21 @@ inline void bnorm(const orc_ctx& c, int d, long p, double* nv) {
   nv[0] = a / var1; nv[1] = b / var1; nv[2] = e / var1;
 }
 
-void face_node(orc_ctx& c, int n, int type, double tw, int i, int j, int k) {
+// Extent of the grid along direction d (xmax - xmin, ymax - ymin, ...:
+// gridgeom's maxval / minval over the interior nodes, src/geom.F90:684-696).
+double grid_extent(const orc_ctx& c, int d) {
+  double lo = 1e300, hi = -1e300;
+  for (int k = 0; k <= c.km; ++k)
+    for (int j = 0; j <= c.jm; ++j)
+      for (int i = 0; i <= c.im; ++i) {
+        const double v = c.x[c.h(i, j, k) + d * c.nh];
+        lo = std::min(lo, v);
+        hi = std::max(hi, v);
+      }
+  return hi - lo;
+}
+
+void face_node(orc_ctx& c, int n, int type, double tw, int i, int j, int k, double extent) {
   const int d = n / 2, side = n % 2;
   const int dim = c.dimof(d);
   const long nh = c.nh;
@@ -1447,6 +1461,60 @@ void face_node(orc_ctx& c, int n, int type, double tw, int i, int j, int k) {
     }
     T[p] = P[p] / R[p] * c.const2;
     fvar2q_prs_node(c, p);
+  } else if (type == 23) {  // gcnscbc xmax 8041-8148, ymax 8150-8252 (prs_t = pinf)
+    // LODI at node dim-1 with one-sided differences, the outgoing wave
+    // relaxed towards pinf (ymax: and, where the normal velocity is
+    // negative, the incoming waves towards the free stream), projected
+    // back and extrapolated over 2 dx.  css, css2 and vnorm are INTEGER in
+    // the reference's declarations (src/bc.F90:8035): sos and the velocity
+    // are truncated, mavg = vnorm/css is an integer division, and
+    // lambda(5:numq) = vnorm leaves lambda(5) = vnorm with numq = 5.
+    const long vn_off = d * nh;                       // normal velocity component
+    const long t1_off = (d == 0 ? 1 : 0) * nh;        // the other in-plane one
+    const int css = (int)(std::sqrt(T[p1]) / c.cfg.mach);
+    const int css2 = css * css;
+    const int vnorm = (int)V[p1 + vn_off];
+    // (css = 0, sos below 1, would divide by zero in the reference; 0 here)
+    const double mavg = css != 0 ? (double)(vnorm / css) : 0.0;
+    double lambda[5] = {(double)(vnorm - css), (double)vnorm, (double)vnorm, (double)vnorm,
+                        (double)vnorm};
+    for (int m = 0; m < 5; ++m) lambda[m] = lambda[m] + 1e-10;
+    const double* X = c.x.data() + d * nh;
+    const double dx = X[p1] - X[p2];
+    auto dr = [&](double v0, double v1) { return -(-v0 + v1) / dx; };  // -deriv(v0, v1)/dx
+    double dvel[3] = {dr(V[p1], V[p2]), dr(V[p1 + nh], V[p2 + nh]), dr(V[p1 + 2 * nh], V[p2 + 2 * nh])};
+    double dprs = dr(P[p1], P[p2]), drho = dr(R[p1], R[p2]), dtmp;
+    const int dn = d, dt1 = d == 0 ? 1 : 0;
+    double lodi[5];
+    lodi[0] = lambda[0] * (dprs - R[p1] * css * dvel[dn]);
+    lodi[1] = lambda[1] * (css2 * drho - dprs);
+    lodi[2] = lambda[2] * dvel[dt1];
+    lodi[3] = lambda[3] * dvel[2];
+    lodi[4] = lambda[4] * (dprs + R[p1] * css * dvel[dn]);
+    if (d == 0 || vnorm >= 0) {
+      const double sigma = 0.25;
+      const double kamma = sigma * css * (1.0 - mavg * mavg) / extent;
+      lodi[0] = kamma * (P[p1] - c.pinf);
+    } else {
+      const double eta = 0.25, vinf = 0.0, winf = 0.0;
+      lodi[0] = eta * R[p1] * css2 * (1.0 - mavg * mavg) / extent * (V[p1 + vn_off] - vinf);
+      lodi[1] = eta * R[p1] * css2 / GAMMA / extent * (T[p1] - c.tinf);
+      lodi[2] = eta * css / extent * (V[p1 + t1_off] - c.uinf);
+      lodi[3] = eta * css / extent * (V[p1 + 2 * nh] - winf);
+    }
+    for (int m = 0; m < 5; ++m) lodi[m] = lodi[m] / lambda[m];
+    drho = 1.0 / (double)(css * css) * (lodi[1] + 0.5 * (lodi[0] + lodi[4]));
+    dtmp = T[p1] / R[p1] / css * (-lodi[1] + 0.5 * (GAMMA - 1.0) * (lodi[0] + lodi[4]));
+    dprs = 0.5 * (lodi[0] + lodi[4]);
+    dvel[dn] = 1.0 / (2.0 * R[p1] * css) * (lodi[4] - lodi[0]);
+    dvel[dt1] = lodi[2];
+    dvel[2] = lodi[3];
+    T[p] = T[p1] + 2.0 * dx * dtmp;
+    R[p] = R[p1] + 2.0 * dx * drho;
+    P[p] = P[p1] + 2.0 * dx * dprs;
+    for (int m = 0; m < 3; ++m) V[p + m * nh] = V[p1 + m * nh] + 2.0 * dx * dvel[m];
+    R[p] = P[p] / T[p] * c.const2;
+    fvar2q_prs_node(c, p);
   } else if (type == 11) {  // inflow xmin, src/bc.F90:1366-1562 (its active, subsonic branch)
     // v, w and T from the inflow arrays; p from the incoming characteristic
     // against pinf blended towards pinf by the local inflow Mach number
@@ -1536,18 +1604,20 @@ void orc_boucon(orc_ctx* c) {
   for (int n = 0; n < 2 * c->ndims; ++n) {
     const int type = face_bctype(*c, n);
     if (type != 41 && type != 42 && type != 50 && type != 60 && type != 421 && type != 21 &&
-        type != 51 && type != 411 && type != 11)
+        type != 51 && type != 411 && type != 11 && type != 23)
       continue;
     const int d = n / 2;
     if (c->npdc(d) != 4 || ((type == 421 || type == 411) && d != 1) ||
-        (type == 21 && n != 1 && n != 3) || (type == 51 && d == 0) || (type == 11 && n != 0))
+        ((type == 21 || type == 23) && n != 1 && n != 3) || (type == 51 && d == 0) ||
+        (type == 11 && n != 0))
       continue;
     const double tw = face_twall(*c, n);
+    const double extent = type == 23 ? grid_extent(*c, d) : 0.0;
     const int a1 = d == 0 ? c->jm : c->im, b1 = d == 2 ? c->jm : c->km;
     for (int b = 0; b <= b1; ++b)
       for (int a = 0; a <= a1; ++a) {
         const int i = d == 0 ? 0 : a, j = d == 0 ? a : (d == 1 ? 0 : b), k = d == 2 ? 0 : b;
-        face_node(*c, n, type, tw, i, j, k);
+        face_node(*c, n, type, tw, i, j, k, extent);
       }
   }
 }

@@ -1,7 +1,7 @@
 """Boundary routines of boucon (src/bc.F90:327-409) in the oracle, on CPU:
 the face values each routine sets (41 isothermal no-slip, 42 adiabatic
 no-slip, 411 isothermal slip/no-slip wall, 421 adiabatic slip wall, 21
-outflow, 51 farfield, 11 inflow, 50
+outflow, 51 farfield, 11 inflow, 23 gcnscbc, 50
 zero-gradient extrapolation, 60 symmetry), and a closed box
 stepping stably with walls on every face."""
 import numpy as np
@@ -278,3 +278,71 @@ def test_inflow_face_values(profile):
     e = rho[sl0] * (tmp[sl0] * const1 + 0.5 * (vel[sl0] ** 2).sum(axis=-1))
     np.testing.assert_allclose(q[sl0 + (4,)], e, rtol=1e-14)
     assert blend.max() < 1e-3  # subsonic inflow: the characteristic branch dominates
+
+
+def _gcnscbc_expected(before, x, n, mach, pinf, const2, extent):
+    """gcnscbc (src/bc.F90:8024-8254) on face n (1 xmax, 3 ymax) restated in
+    numpy from the state before the call, with the reference's INTEGER css,
+    css2 and vnorm (truncated; mavg an integer division; lambda(5) = vnorm
+    since lambda(5:numq) = vnorm follows lambda(5) = vnorm + css)."""
+    d = n // 2
+    on, ot = d, 1 - d
+    f1 = lambda a: _face(a, n, 1)
+    f2 = lambda a: _face(a, n, 2)
+    r1, t1, p1 = f1(before["rho"]), f1(before["tmp"]), f1(before["prs"])
+    v1, v2 = f1(before["vel"]), f2(before["vel"])
+    css = np.trunc(np.sqrt(t1) / mach).astype(np.int64)
+    css2 = css * css
+    vnorm = np.trunc(v1[..., on]).astype(np.int64)
+    mavg = np.trunc(vnorm / css).astype(np.float64)
+    lam = [(vnorm - css) + 1e-10] + [vnorm + 1e-10] * 4
+    dx = f1(x[..., d]) - f2(x[..., d])
+    dr = lambda a, b: -(-a + b) / dx
+    dvel = [dr(v1[..., m], v2[..., m]) for m in range(3)]
+    dprs = dr(p1, f2(before["prs"]))
+    drho = dr(r1, f2(before["rho"]))
+    lodi = [lam[0] * (dprs - r1 * css * dvel[on]), lam[1] * (css2 * drho - dprs), lam[2] * dvel[ot],
+            lam[3] * dvel[2], lam[4] * (dprs + r1 * css * dvel[on])]
+    soft = 0.25 * css * (1.0 - mavg * mavg) / extent * (p1 - pinf)
+    if d == 0:
+        lodi[0] = soft
+    else:
+        eta, inflow = 0.25, vnorm < 0
+        lodi[0] = np.where(inflow, eta * r1 * css2 * (1.0 - mavg * mavg) / extent * v1[..., 1], soft)
+        lodi[1] = np.where(inflow, eta * r1 * css2 / 1.4 / extent * (t1 - 1.0), lodi[1])
+        lodi[2] = np.where(inflow, eta * css / extent * (v1[..., 0] - 1.0), lodi[2])
+        lodi[3] = np.where(inflow, eta * css / extent * v1[..., 2], lodi[3])
+    lodi = [lodi[m] / lam[m] for m in range(5)]
+    dtmp = t1 / r1 / css * (-lodi[1] + 0.5 * (1.4 - 1.0) * (lodi[0] + lodi[4]))
+    dprs = 0.5 * (lodi[0] + lodi[4])
+    dv = [None] * 3
+    dv[on] = 1.0 / (2.0 * r1 * css) * (lodi[4] - lodi[0])
+    dv[ot], dv[2] = lodi[2], lodi[3]
+    t = t1 + 2.0 * dx * dtmp
+    p = p1 + 2.0 * dx * dprs
+    vel = np.stack([v1[..., m] + 2.0 * dx * dv[m] for m in range(3)], axis=-1)
+    return {"tmp": t, "prs": p, "vel": vel, "rho": p / t * const2}
+
+
+def test_gcnscbc_face_values():
+    """23 (gcnscbc) on xmax and ymax against a numpy restatement; a bulk v
+    of -1 puts both of ymax's branches (vnorm >= 0: soft outflow towards
+    pinf; vnorm < 0: the waves relaxed towards the free stream) on the
+    face."""
+    o = bc_oracle((24, 20, 16), (4, 4, 3), (41, 23, 42, 23, 0, 0), twall6=(1.2, 0, 0, 0, 0, 0),
+                  vbulk=-1.0, deltat=2e-3)
+    before = {k: o.field(k).copy() for k in ("vel", "prs", "tmp", "rho")}
+    x = o.field("x").copy()
+    o.call("boucon")
+    c = cases.refcal(MACH, 400.0)
+    extent = 2.0 * np.pi
+    vnorm_y = np.trunc(_face(before["vel"], 3, 1)[..., 1])
+    assert 0.05 < (vnorm_y < 0).mean() < 0.95
+    for n in (1, 3):
+        want = _gcnscbc_expected(before, x, n, MACH, c["pinf"], c["const2"], extent)
+        for k in ("prs", "tmp", "rho"):
+            np.testing.assert_allclose(_face(o.field(k), n), want[k], rtol=1e-13, err_msg=(n, k))
+        np.testing.assert_allclose(_face(o.field("vel"), n), want["vel"], rtol=1e-12, atol=1e-13)
+        q, rho, vel, prs = (o.field(k) for k in ("q", "rho", "vel", "prs"))
+        e = _face(prs, n) * 2.5 + 0.5 * _face(rho, n) * (_face(vel, n) ** 2).sum(axis=-1)
+        np.testing.assert_allclose(_face(q[..., 4], n), e, rtol=1e-12)
