@@ -155,7 +155,7 @@ def load(path: str = LIB_PATH):
     L.astr_gpu_poll.restype = ip
     L.astr_gpu_set_grid.argtypes = [vp, dp]
     L.astr_gpu_set_grid.restype = ip
-    L.astr_gpu_set_inflow.argtypes = [vp, dp, dp, dp]
+    L.astr_gpu_set_inflow.argtypes = [vp, dp, dp, dp, dp]
     L.astr_gpu_set_inflow.restype = ip
     L.astr_gpu_channel_state.argtypes = [vp, dp]
     L.astr_gpu_channel_state.restype = ip

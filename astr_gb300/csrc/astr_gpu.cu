@@ -92,6 +92,22 @@ __device__ __forceinline__ void qswap_line(const Geo& g, const DevT<T>& d, const
   for (int l = -HMD; l <= 0; ++l) q2fvar_store(g, d, ph, base + hs * l);
   for (int l = dim; l <= dim + HMD; ++l) q2fvar_store(g, d, ph, base + hs * l);
 }
+// dataswap of q along a periodic direction (the halo copy filterq makes
+// before filtering that direction, src/comsolver.F90:530-575 with
+// src/parallel.F90:4169-4303, single rank): the halo layers take the
+// periodic images of the current interior; no averaging, no primitives.
+template <typename T, int DIR>
+__global__ void k_qhalo(Geo g, DevT<T> d) {
+  int dim;
+  long long base, hs;
+  if (!face_line<DIR>(g, dim, base, hs)) return;
+  for (int n = 0; n < 5; ++n) {
+    T* v = d.q + n * g.nh + base;
+    for (int h = 1; h <= HMD; ++h) v[-hs * h] = v[hs * (dim - h)];
+    for (int h = 1; h <= HMD; ++h) v[hs * (dim + h)] = v[hs * h];
+  }
+}
+
 template <typename T, int DIR>
 __global__ void k_qswap(Geo g, DevT<T> d, Phys ph) {
   qswap_line<T, DIR>(g, d, ph, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y);
@@ -599,6 +615,194 @@ __global__ void k_face_bc(Geo g, DevT<T> d, Phys ph, int n, int type, double tw,
     d.qm[z + 3 * n0] = ro * w;
     d.qm[z + 4 * n0] = e;
   }
+}
+
+// inflow_nscbc (src/bc.F90:2114-2344), bctype 12 on xmin with periodic y
+// and z.  Three kernels: the domain-wide maximum of |u|^2/c^2 (gmachmax2);
+// per face node (j, k) the residual the routine adds to qrhs at i = 0 --
+// the LODI residual (the outgoing wave kept, the incoming waves relaxed
+// towards the inflow arrays at the rate kin) and the face's tangential flux
+// derivatives (ddfc '222e' with periodic ends: 0.5 (f(j+1) - f(j-1))) --
+// in FP64 into B; and, after the convective sweeps (which leave qrhs at
+// i = 0 zero: the face lies outside convrsdcal6's ranges), qrhs(0) -= B,
+// the sign rhscal's negation gives the routine's additions.
+__device__ __forceinline__ double nscbc_dxi(const Geo& g, const double* xg64, const void* xgv, const void* xdv,
+                                            bool f32, int d, int m, long long p) {
+  (void)g;
+  (void)xg64;
+  const long long nh = g.nh;
+  if (xgv) return f32 ? (double)((const float*)xgv)[(3 * d + m) * nh + p] : ((const double*)xgv)[(3 * d + m) * nh + p];
+  if (d != m) return 0.0;
+  return f32 ? (double)((const float*)xdv)[d * nh + p] : ((const double*)xdv)[d * nh + p];
+}
+
+template <typename T>
+__device__ __forceinline__ double nscbc_x(const Geo& g, const DevT<T>& d, int r, int m, long long p) {
+  return nscbc_dxi(g, nullptr, (const void*)d.xg, (const void*)d.xd, sizeof(T) == 4, r, m, p);
+}
+
+// J (q u_r + dxi(r,:) p) at node p, every product and sum rounded on its own
+template <typename T>
+__device__ __forceinline__ void nscbc_flux(const Geo& g, const DevT<T>& d, int r, long long p, double* f) {
+  const long long nh = g.nh;
+  const double x1 = nscbc_x(g, d, r, 0, p), x2 = nscbc_x(g, d, r, 1, p), x3 = nscbc_x(g, d, r, 2, p);
+  const double u = (double)d.pr[p + nh], v = (double)d.pr[p + 2 * nh], w = (double)d.pr[p + 3 * nh];
+  const double pr = (double)d.pr[p + 4 * nh], J = d.jac64[p];
+  const double uu = __dadd_rn(__dadd_rn(__dmul_rn(x1, u), __dmul_rn(x2, v)), __dmul_rn(x3, w));
+  f[0] = __dmul_rn(__dmul_rn(J, (double)d.q[p]), uu);
+  f[1] = __dmul_rn(J, __dadd_rn(__dmul_rn((double)d.q[p + nh], uu), __dmul_rn(x1, pr)));
+  f[2] = __dmul_rn(J, __dadd_rn(__dmul_rn((double)d.q[p + 2 * nh], uu), __dmul_rn(x2, pr)));
+  f[3] = __dmul_rn(J, __dadd_rn(__dmul_rn((double)d.q[p + 3 * nh], uu), __dmul_rn(x3, pr)));
+  f[4] = __dmul_rn(__dmul_rn(J, __dadd_rn((double)d.q[p + 4 * nh], pr)), uu);
+}
+
+template <typename T>
+__global__ void k_nscbc_gmach(Geo g, DevT<T> d, double mach, unsigned long long* out) {
+  __shared__ double sh[256];
+  double mx = 0.0;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < g.n0;
+       idx += (long long)gridDim.x * blockDim.x) {
+    int i, j, k;
+    point_of(g, idx, i, j, k);
+    const long long p = hidx(g, i, j, k), nh = g.nh;
+    const double u = (double)d.pr[p + nh], v = (double)d.pr[p + 2 * nh], w = (double)d.pr[p + 3 * nh];
+    const double var1 = __dadd_rn(__dadd_rn(__dmul_rn(u, u), __dmul_rn(v, v)), __dmul_rn(w, w));
+    const double css = sqrt((double)d.pr[p + 5 * nh]) / mach;
+    mx = fmax(mx, var1 / css / css);
+  }
+  sh[threadIdx.x] = mx;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + s]);
+    __syncthreads();
+  }
+  // non-negative doubles order as their bit patterns
+  if (threadIdx.x == 0) atomicMax(out, (unsigned long long)__double_as_longlong(sh[0]));
+}
+
+template <typename T>
+__global__ void k_nscbc_inflow(Geo g, DevT<T> d, double mach, const double* inflow, double extent,
+                               const unsigned long long* gmach, double* B) {
+  const long long nf = (long long)(g.jm + 1) * (g.km + 1);
+  const long long fj = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (fj >= nf) return;
+  const int j = (int)(fj % (g.jm + 1)), k = (int)(fj / (g.jm + 1));
+  auto M = [](double x, double y) { return __dmul_rn(x, y); };
+  auto A = [](double x, double y) { return __dadd_rn(x, y); };
+  auto S = [](double x, double y) { return __dsub_rn(x, y); };
+  const long long nh = g.nh, p = hidx(g, 0, j, k), pa = hidx(g, 1, j, k);
+  const double gm2 = __longlong_as_double((long long)*gmach);
+  const double rho = (double)d.pr[p], u = (double)d.pr[p + nh], v = (double)d.pr[p + 2 * nh];
+  const double w = (double)d.pr[p + 3 * nh], pr = (double)d.pr[p + 4 * nh], t = (double)d.pr[p + 5 * nh];
+  const double J = d.jac64[p];
+  double q[5];
+  for (int m = 0; m < 5; ++m) q[m] = (double)d.q[p + m * nh];
+  const double ddi[3] = {nscbc_x(g, d, 0, 0, p), nscbc_x(g, d, 0, 1, p), nscbc_x(g, d, 0, 2, p)};
+  // pmatrix (src/bc.F90:5516-5611)
+  const double c = sqrt(t) / mach;
+  const double vr = 1.0 / sqrt(A(A(M(ddi[0], ddi[0]), M(ddi[1], ddi[1])), M(ddi[2], ddi[2])));
+  const double nx = M(ddi[0], vr), ny = M(ddi[1], vr), nz = M(ddi[2], vr);
+  const double phi = M(0.5 * (1.4 - 1.0), A(A(M(u, u), M(v, v)), M(w, w)));
+  const double VV = A(A(M(nx, u), M(ny, v)), M(nz, w));
+  const double a1 = 1.4 - 1.0, cc = M(c, c);
+  const double a2 = 1.0 / M(M(sqrt(2.0), rho), c);
+  const double a3 = rho / M(c, sqrt(2.0));
+  const double a4 = A(phi, cc) / (1.4 - 1.0);
+  const double a5 = S(1.0, phi / cc);
+  const double a6 = phi / (1.4 - 1.0);
+  const double n3[3] = {nx, ny, nz};
+  double Pi[5][5], Pn[5][5];
+  Pi[0][0] = S(M(nx, a5), S(M(nz, v), M(ny, w)) / rho);
+  Pi[0][1] = M(M(nx, a1), u) / cc;
+  Pi[0][2] = A(M(M(nx, a1), v) / cc, nz / rho);
+  Pi[0][3] = S(M(M(nx, a1), w) / cc, ny / rho);
+  Pi[1][0] = S(M(ny, a5), S(M(nx, w), M(nz, u)) / rho);
+  Pi[1][1] = S(M(M(ny, a1), u) / cc, nz / rho);
+  Pi[1][2] = M(M(ny, a1), v) / cc;
+  Pi[1][3] = A(M(M(ny, a1), w) / cc, nx / rho);
+  Pi[2][0] = S(M(nz, a5), S(M(ny, u), M(nx, v)) / rho);
+  Pi[2][1] = A(M(M(nz, a1), u) / cc, ny / rho);
+  Pi[2][2] = S(M(M(nz, a1), v) / cc, nx / rho);
+  Pi[2][3] = M(M(nz, a1), w) / cc;
+  for (int r = 0; r < 3; ++r) Pi[r][4] = -(M(n3[r], a1) / cc);
+  Pi[3][0] = M(a2, S(phi, M(c, VV)));
+  Pi[3][1] = -M(a2, S(M(a1, u), M(nx, c)));
+  Pi[3][2] = -M(a2, S(M(a1, v), M(ny, c)));
+  Pi[3][3] = -M(a2, S(M(a1, w), M(nz, c)));
+  Pi[3][4] = M(a1, a2);
+  Pi[4][0] = M(a2, A(phi, M(c, VV)));
+  Pi[4][1] = -M(a2, A(M(a1, u), M(nx, c)));
+  Pi[4][2] = -M(a2, A(M(a1, v), M(ny, c)));
+  Pi[4][3] = -M(a2, A(M(a1, w), M(nz, c)));
+  Pi[4][4] = M(a1, a2);
+  Pn[0][0] = nx; Pn[0][1] = ny; Pn[0][2] = nz; Pn[0][3] = a3; Pn[0][4] = a3;
+  Pn[1][0] = M(nx, u); Pn[1][1] = S(M(ny, u), M(nz, rho)); Pn[1][2] = A(M(nz, u), M(ny, rho));
+  Pn[1][3] = M(a3, A(u, M(nx, c))); Pn[1][4] = M(a3, S(u, M(nx, c)));
+  Pn[2][0] = A(M(nx, v), M(nz, rho)); Pn[2][1] = M(ny, v); Pn[2][2] = S(M(nz, v), M(nx, rho));
+  Pn[2][3] = M(a3, A(v, M(ny, c))); Pn[2][4] = M(a3, S(v, M(ny, c)));
+  Pn[3][0] = S(M(nx, w), M(ny, rho)); Pn[3][1] = A(M(ny, w), M(nx, rho)); Pn[3][2] = M(nz, w);
+  Pn[3][3] = M(a3, A(w, M(nz, c))); Pn[3][4] = M(a3, S(w, M(nz, c)));
+  Pn[4][0] = A(M(nx, a6), M(rho, S(M(nz, v), M(ny, w))));
+  Pn[4][1] = A(M(ny, a6), M(rho, S(M(nx, w), M(nz, u))));
+  Pn[4][2] = A(M(nz, a6), M(rho, S(M(ny, u), M(nx, v))));
+  Pn[4][3] = M(a3, A(a4, M(c, VV))); Pn[4][4] = M(a3, S(a4, M(c, VV)));
+  // normal flux difference, E/F/G at the node, metric derivatives
+  double e0[5], e1[5];
+  nscbc_flux(g, d, 0, p, e0);
+  nscbc_flux(g, d, 0, pa, e1);
+  const double E[5] = {q[1], A(M(q[1], u), pr), M(q[2], u), M(q[3], u), M(A(q[4], pr), u)};
+  const double F[5] = {q[2], M(q[1], v), A(M(q[2], v), pr), M(q[3], v), M(A(q[4], pr), v)};
+  const double G[5] = {q[3], M(q[1], w), M(q[2], w), A(M(q[3], w), pr), M(A(q[4], pr), w)};
+  double jcbi[3];
+  for (int m = 0; m < 3; ++m) jcbi[m] = A(-M(ddi[m], J), M(nscbc_x(g, d, 0, m, pa), d.jac64[pa]));
+  double rest[5], l1[5], lodi[5];
+  for (int n = 0; n < 5; ++n) {
+    rest[n] = A(A(M(E[n], jcbi[0]), M(F[n], jcbi[1])), M(G[n], jcbi[2]));
+    l1[n] = S(A(-e0[n], e1[n]), rest[n]);
+  }
+  for (int r = 0; r < 5; ++r) {
+    double acc = 0.0;
+    for (int m = 0; m < 5; ++m) acc = A(acc, M(Pi[r][m], l1[m]));
+    lodi[r] = acc / J;
+  }
+  const double kin = M(M(0.25, S(1.0, gm2)), c) / extent;
+  const long long fo = fj;
+  const double ui = inflow[fo], vi = inflow[fo + nf], wi = inflow[fo + 2 * nf];
+  const double pin = inflow[4 * nf + (g.jm + 1) + fo];
+  const double x1 = M(ddi[0], vr), x2 = M(ddi[1], vr), x3 = M(ddi[2], vr);
+  lodi[0] = 0.0;
+  lodi[1] = M(M(kin, 0.5), S(M(x1, S(w, wi)), M(x3, S(u, ui))));
+  lodi[2] = M(M(kin, 0.5), A(-M(x1, S(v, vi)), M(x2, S(u, ui))));
+  lodi[3] = M(kin, A(A(A(M(x1, S(u, ui)), M(x2, S(v, vi))), M(x3, S(w, wi))), S(pr, pin) / rho / c));
+  double b[5];
+  for (int r = 0; r < 5; ++r) {
+    double acc = 0.0;
+    for (int m = 0; m < 5; ++m) acc = A(acc, M(Pn[r][m], lodi[m]));
+    b[r] = A(0.0, A(M(acc, J), rest[r]));
+  }
+  // tangential derivatives of the face (y, and z in 3-D)
+  double fp[5], fm[5];
+  nscbc_flux(g, d, 1, hidx(g, 0, j + 1, k), fp);
+  nscbc_flux(g, d, 1, hidx(g, 0, j - 1, k), fm);
+  for (int n = 0; n < 5; ++n) b[n] = A(b[n], M(0.5, S(fp[n], fm[n])));
+  if (g.ndims == 3) {
+    nscbc_flux(g, d, 2, hidx(g, 0, j, k + 1), fp);
+    nscbc_flux(g, d, 2, hidx(g, 0, j, k - 1), fm);
+    for (int n = 0; n < 5; ++n) b[n] = A(b[n], M(0.5, S(fp[n], fm[n])));
+  }
+  for (int n = 0; n < 5; ++n) B[n * nf + fj] = b[n];
+}
+
+template <typename T>
+__global__ void k_nscbc_apply(Geo g, DevT<T> d, const double* B) {
+  const long long nf = (long long)(g.jm + 1) * (g.km + 1);
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 5 * nf) return;
+  const int n = (int)(t / nf);
+  const long long fj = t % nf;
+  const int j = (int)(fj % (g.jm + 1)), k = (int)(fj / (g.jm + 1));
+  T* r = d.qrhs + (long long)n * g.n0 + zidx(g, 0, j, k);
+  *r = (T)__dsub_rn((double)*r, B[t]);
 }
 
 // Channel volume sums, one thread per (i, k) column, i = 1..im, k = 1..km
@@ -1280,8 +1484,16 @@ struct astr_ctx {
   int chan_nblk = 0;
   double* ycoord = nullptr;     // y coordinates, halo layout
   unsigned char* slip_mask = nullptr;  // 411 on ymin: node (i, k) at x <= xslip
-  // 11 on xmin: vel_in(0:jm,0:km,1:3), tmp_in(0:jm,0:km), tmp_prof(0:jm)
+  // 11 or 12 on xmin: vel_in(0:jm,0:km,1:3), tmp_in(0:jm,0:km),
+  // tmp_prof(0:jm), prs_in(0:jm,0:km)
   double* inflow = nullptr;
+  // 12 on xmin (inflow_nscbc): the residual it adds at i = 0 (5 arrays of
+  // the face), the domain-wide Mach-number word, the grid's x extent, and
+  // whether a boucon call has left B to be applied after the convection
+  double* nscbc_b = nullptr;
+  unsigned long long* nscbc_gm = nullptr;
+  double nscbc_ext = 0.0;
+  bool nscbc_pending = false;
   // 23 on xmax / ymax (index 0 / 1): the face's normal spacing
   // x(dim-1) - x(dim-2) per node and the grid's extent, from the grid
   double* gc_dx[2] = {nullptr, nullptr};
@@ -1480,6 +1692,17 @@ int launch_face(astr_ctx* c, bool mini) {
 
 dim3 point_grid(long long n) { return dim3((unsigned)((n + 255) / 256)); }
 
+template <typename T, int DIR>
+int launch_qhalo(astr_ctx* c) {
+  const Geo& g = c->g;
+  const int na = DIR == 0 ? g.jm : g.im;
+  const int nb = DIR == 2 ? g.jm : g.km;
+  prof_begin(c, KC_HALO);
+  k_qhalo<T, DIR><<<dim3((na + 128) / 128, nb + 1), 128, 0, c->st>>>(g, dev<T>(c));
+  prof_end(c);
+  return after_launch(c, "k_qhalo");
+}
+
 // The tiled sweeps run where the context built them and the metrics are
 // diagonal (the compact MP path keeps the register-window sweeps).
 bool use_v2(const astr_ctx* c) { return c->v2 && !c->gen && !c->mp; }
@@ -1535,14 +1758,25 @@ int launch2_visc_c(astr_ctx* c) {
 template <typename T>
 int run_filter(astr_ctx* c, bool q2f_last) {
   const int nd = c->g.ndims;
+  // filterq refreshes the q halos of each periodic direction before
+  // filtering it; the sweeps read wrapped interior nodes instead, so the
+  // copy is made only where a routine reads those halos before the next
+  // qswap: inflow_nscbc's tangential derivatives on the xmin face
+  const bool halos = c->nscbc_b != nullptr;
   if (use_v2(c) && !q2f_last) {
+    if (halos && c->g.per[0]) RC((launch_qhalo<T, 0>(c)));
     RC((launch2_filter_c<T, 0>(c)));
+    if (halos && c->g.per[1]) RC((launch_qhalo<T, 1>(c)));
     RC((launch2_filter_c<T, 1>(c)));
+    if (halos && nd == 3 && c->g.per[2]) RC((launch_qhalo<T, 2>(c)));
     if (nd == 3) RC((launch2_filter_c<T, 2>(c)));
     return ASTR_OK;
   }
+  if (halos && c->g.per[0]) RC((launch_qhalo<T, 0>(c)));
   RC((launch_filter<T, 0>(c, 0)));
+  if (halos && c->g.per[1]) RC((launch_qhalo<T, 1>(c)));
   RC((launch_filter<T, 1>(c, (q2f_last && nd == 2) ? 1 : 0)));
+  if (halos && nd == 3 && c->g.per[2]) RC((launch_qhalo<T, 2>(c)));
   if (nd == 3) RC((launch_filter<T, 2>(c, q2f_last ? 1 : 0)));
   return ASTR_OK;
 }
@@ -1696,6 +1930,21 @@ int run_boucon(astr_ctx* c) {
   const double pinf = 1.0 / c->ph.const2, adt = 0.25 * c->pm.deltat;
   for (int n = 0; n < 2 * g.ndims; ++n) {
     const int type = c->bct[n];
+    if (type == 12 && n == 0) {
+      // inflow_nscbc: the state is read, the residual B kept for rhscal
+      prof_begin(c, KC_HALO);
+      CK(cudaMemsetAsync(c->nscbc_gm, 0, 8, c->st));
+      k_nscbc_gmach<T><<<std::min<long long>((g.n0 + 255) / 256, 4096), 256, 0, c->st>>>(g, dev<T>(c), mach,
+                                                                                      c->nscbc_gm);
+      RC(after_launch(c, "k_nscbc_gmach"));
+      const long long nf = (long long)(g.jm + 1) * (g.km + 1);
+      k_nscbc_inflow<T><<<point_grid(nf), 256, 0, c->st>>>(g, dev<T>(c), mach, c->inflow, c->nscbc_ext,
+                                                           c->nscbc_gm, c->nscbc_b);
+      prof_end(c);
+      RC(after_launch(c, "k_nscbc_inflow"));
+      c->nscbc_pending = true;
+      continue;
+    }
     if (type != 41 && type != 42 && type != 50 && type != 60 && type != 421 && type != 21 &&
         type != 51 && type != 411 && type != 11 && type != 23)
       continue;
@@ -1710,6 +1959,18 @@ int run_boucon(astr_ctx* c) {
     RC(after_launch(c, "k_face_bc"));
   }
   return ASTR_OK;
+}
+
+// inflow_nscbc's residual into qrhs at i = 0, after the convective part and
+// its negation (rhscal), so that qrhs(0) = -(B + the convective part)
+template <typename T>
+int nscbc_apply(astr_ctx* c) {
+  const long long n = 5LL * (c->g.jm + 1) * (c->g.km + 1);
+  prof_begin(c, KC_POINT);
+  k_nscbc_apply<T><<<point_grid(n), 256, 0, c->st>>>(c->g, dev<T>(c), c->nscbc_b);
+  prof_end(c);
+  c->nscbc_pending = false;
+  return after_launch(c, "k_nscbc_apply");
 }
 
 // Channel bulk sums and controller for one stage; statcal at stage 1 from
@@ -1826,6 +2087,7 @@ int one_step(astr_ctx* c, double* stats) {
       if (pt_stats && st1 && stats) RC(stats_pointwise<T>(c));
       if (split_sig) RC(sigma_pointwise<T>(c));
       if (c->mp) RC(run_mpconv(c));
+      if (c->nscbc_pending) RC(nscbc_apply<T>(c));
       if (c->channel) RC(run_chan<T>(c, st1));
       if (visc) RC(run_visc<T>(c, !split_rk, !split_rk));
       if (!visc || split_rk) RC(rk_pointwise<T>(c, 1));
@@ -1924,6 +2186,7 @@ template <typename T>
 int rhscal_t(astr_ctx* c) {
   if (c->mp) RC(run_mpconv(c));
   else RC(run_convgrad<T>(c, true, false, false, false, false));
+  if (c->nscbc_pending) RC(nscbc_apply<T>(c));
   if (c->pm.diffterm) {
     prof_begin(c, KC_POINT);
     k_sigma<T><<<point_grid(c->g.n0), 256, 0, c->st>>>(c->g, dev<T>(c), c->ph);
@@ -1947,20 +2210,23 @@ int rhscal_t(astr_ctx* c) {
 // ---------------------------------------------------------------------------
 extern "C" {
 
-// The inflow arrays of bctype 11 into HBM: vel_in(0:jm,0:km,1:3),
-// tmp_in(0:jm,0:km), tmp_prof(0:jm); a NULL array takes freestreaminflow's
-// values (src/bc.F90:7950-8003: uinf = 1, vinf = winf = 0, tinf = 1).
+// The inflow arrays of bctypes 11 and 12 into HBM: vel_in(0:jm,0:km,1:3),
+// tmp_in(0:jm,0:km), tmp_prof(0:jm), prs_in(0:jm,0:km); a NULL array takes
+// freestreaminflow's values (src/bc.F90:7950-8003: uinf = 1, vinf = winf
+// = 0, tinf = 1, prs_in = thermal(roinf, tinf) = pinf).
 static int inflow_upload(astr_ctx* c, const double* vel_in, const double* tmp_in,
-                         const double* tmp_prof) {
+                         const double* tmp_prof, const double* prs_in) {
   const size_t nf = (size_t)(c->g.jm + 1) * (c->g.km + 1), nj = (size_t)c->g.jm + 1;
-  std::vector<double> h(4 * nf + nj);
+  const double pinf = 1.0 * 1.0 / c->ph.const2;
+  std::vector<double> h(5 * nf + nj);
   for (size_t t = 0; t < 3 * nf; ++t) h[t] = vel_in ? vel_in[t] : (t < nf ? 1.0 : 0.0);
   for (size_t t = 0; t < nf; ++t) h[3 * nf + t] = tmp_in ? tmp_in[t] : 1.0;
   for (size_t t = 0; t < nj; ++t) h[4 * nf + t] = tmp_prof ? tmp_prof[t] : 1.0;
+  for (size_t t = 0; t < nf; ++t) h[4 * nf + nj + t] = prs_in ? prs_in[t] : pinf;
   for (double v : h)
     if (!std::isfinite(v)) return fail(c, ASTR_ERR_ARG, "inflow arrays: a non-finite value");
   for (size_t t = 3 * nf; t < h.size(); ++t)
-    if (!(h[t] > 0.0)) return fail(c, ASTR_ERR_ARG, "inflow temperatures must be > 0");
+    if (!(h[t] > 0.0)) return fail(c, ASTR_ERR_ARG, "inflow temperatures and pressures must be > 0");
   CK(cudaMemcpyAsync(c->inflow, h.data(), h.size() * 8, cudaMemcpyHostToDevice, c->st));
   CK(cudaStreamSynchronize(c->st));
   return ASTR_OK;
@@ -1982,8 +2248,9 @@ size_t astr_gpu_footprint(const astr_dims* dims, const astr_params* params) {
   // flux 5, sensor 1 (halo arrays, FP64), the shock flags (bytes) and the
   // list of flagged interfaces (at most nh ints)
   if (params && params->conschm == ASTR_CONSCHM_MP) b += 8 * 26 * nh + n0 + 4 * nh;
-  if (params && params->bctype[0] == 11)  // inflow arrays
-    b += 8 * (4 * (size_t)(dims->jm + 1) * (dims->km + 1) + (size_t)(dims->jm + 1));
+  if (params && (params->bctype[0] == 11 || params->bctype[0] == 12))  // inflow arrays (+ B)
+    b += 8 * ((params->bctype[0] == 12 ? 10 : 5) * (size_t)(dims->jm + 1) * (dims->km + 1) +
+              (size_t)(dims->jm + 1) + 1);
   return b;
 }
 
@@ -2010,13 +2277,17 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
     if (params->channel && (n == 2 || n == 3) && (bct[n] == 0 || bct[n] == 1)) bct[n] = 41;
     if (bct[n] == 0 || bct[n] == 1) continue;
     if (bct[n] != 41 && bct[n] != 42 && bct[n] != 50 && bct[n] != 60 && bct[n] != 421 &&
-        bct[n] != 21 && bct[n] != 51 && bct[n] != 411 && bct[n] != 11 && bct[n] != 23)
+        bct[n] != 21 && bct[n] != 51 && bct[n] != 411 && bct[n] != 11 && bct[n] != 23 && bct[n] != 12)
       return fail(nullptr, ASTR_ERR_UNSUPPORTED,
-                  "bctype: 11, 21, 23, 41, 42, 411, 421, 50, 51 and 60 are built (0/1: none)");
+                  "bctype: 11, 12, 21, 23, 41, 42, 411, 421, 50, 51 and 60 are built (0/1: none)");
     if (bct[n] == 23 && n != 1 && n != 3)
       return fail(nullptr, ASTR_ERR_UNSUPPORTED, "bctype 23 exists for the xmax and ymax faces only");
-    if (bct[n] == 11 && n != 0)
-      return fail(nullptr, ASTR_ERR_UNSUPPORTED, "bctype 11 exists for the xmin face only");
+    if ((bct[n] == 11 || bct[n] == 12) && n != 0)
+      return fail(nullptr, ASTR_ERR_UNSUPPORTED, "bctypes 11 and 12 exist for the xmin face only");
+    if (bct[n] == 12 && (npdc[1] != 3 || (ndims == 3 && npdc[2] != 3)))
+      return fail(nullptr, ASTR_ERR_UNSUPPORTED,
+                  "bctype 12 (inflow_nscbc) needs periodic y and z: its tangential derivatives (ddfc "
+                  "'222e') have no closure for both ends physical on one rank");
     if (bct[n] == 51 && n < 2)
       return fail(nullptr, ASTR_ERR_UNSUPPORTED, "bctype 51 exists for the y and z faces only");
     if (bct[n] == 21 && n != 1 && n != 3)
@@ -2184,8 +2455,13 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
     c->ycoord = (double*)alloc(nh * 8);
   }
   if (bct[2] == 411) c->slip_mask = (unsigned char*)alloc((size_t)(g.im + 1) * (g.km + 1));
-  const size_t n_inflow = 4 * (size_t)(g.jm + 1) * (g.km + 1) + (size_t)(g.jm + 1);
-  if (bct[0] == 11) c->inflow = (double*)alloc(n_inflow * 8);
+  const size_t n_face0 = (size_t)(g.jm + 1) * (g.km + 1);
+  const size_t n_inflow = 5 * n_face0 + (size_t)(g.jm + 1);
+  if (bct[0] == 11 || bct[0] == 12) c->inflow = (double*)alloc(n_inflow * 8);
+  if (bct[0] == 12) {
+    c->nscbc_b = (double*)alloc(5 * n_face0 * 8);
+    c->nscbc_gm = (unsigned long long*)alloc(8);
+  }
   if (bct[1] == 23) c->gc_dx[0] = (double*)alloc((size_t)(g.jm + 1) * (g.km + 1) * 8);
   if (bct[3] == 23) c->gc_dx[1] = (double*)alloc((size_t)(g.im + 1) * (g.km + 1) * 8);
   // schemes: per direction derivative + filter, in both precisions
@@ -2405,7 +2681,7 @@ int astr_gpu_create(const astr_dims* dims, const astr_params* params, astr_ctx**
     c->mp = true;
   }
   if (c->inflow) {
-    const int rc = inflow_upload(c, nullptr, nullptr, nullptr);
+    const int rc = inflow_upload(c, nullptr, nullptr, nullptr, nullptr);
     if (rc != ASTR_OK) {
       std::string msg = c->err;
       astr_gpu_destroy(c);
@@ -2498,7 +2774,7 @@ int astr_gpu_set_metrics(astr_ctx* c, const double* dxi, const double* jacob) {
 
 int astr_gpu_set_grid(astr_ctx* c, const double* x) {
   if (!c || !x) return fail(c, ASTR_ERR_ARG, "null argument");
-  if (!c->channel && !c->slip_mask && !c->gc_dx[0] && !c->gc_dx[1]) return ASTR_OK;
+  if (!c->channel && !c->slip_mask && !c->gc_dx[0] && !c->gc_dx[1] && !c->nscbc_b) return ASTR_OK;
   const size_t nh = (size_t)c->g.nh;
   const long long NI = c->g.NI, NJ = c->g.NJ;
   auto h = [&](int i, int j, int k) {
@@ -2514,6 +2790,17 @@ int astr_gpu_set_grid(astr_ctx* c, const double* x) {
       for (int i = 0; i <= im; ++i)
         mask[(size_t)i + (size_t)(im + 1) * k] = x[h(i, 0, k)] <= c->pm.xslip ? 1 : 0;
     CK(cudaMemcpyAsync(c->slip_mask, mask.data(), mask.size(), cudaMemcpyHostToDevice, c->st));
+  }
+  if (c->nscbc_b) {
+    // inflow_nscbc's xmax - xmin (gridgeom, src/geom.F90:684-696)
+    double lo = 1e300, hi = -1e300;
+    for (int k = 0; k <= c->g.km; ++k)
+      for (int j = 0; j <= c->g.jm; ++j)
+        for (int i = 0; i <= c->g.im; ++i) {
+          lo = std::min(lo, x[h(i, j, k)]);
+          hi = std::max(hi, x[h(i, j, k)]);
+        }
+    c->nscbc_ext = hi - lo;
   }
   for (int f = 0; f < 2; ++f) {
     // gcnscbc's spacing x(dim-1) - x(dim-2) along the face normal at every
@@ -2549,10 +2836,11 @@ int astr_gpu_set_grid(astr_ctx* c, const double* x) {
   return ASTR_OK;
 }
 
-int astr_gpu_set_inflow(astr_ctx* c, const double* vel_in, const double* tmp_in, const double* tmp_prof) {
+int astr_gpu_set_inflow(astr_ctx* c, const double* vel_in, const double* tmp_in, const double* tmp_prof,
+                        const double* prs_in) {
   if (!c) return fail(c, ASTR_ERR_ARG, "null context");
-  if (!c->inflow) return fail(c, ASTR_ERR_STATE, "no inflow face (bctype 11 on xmin)");
-  return inflow_upload(c, vel_in, tmp_in, tmp_prof);
+  if (!c->inflow) return fail(c, ASTR_ERR_STATE, "no inflow face (bctype 11 or 12 on xmin)");
+  return inflow_upload(c, vel_in, tmp_in, tmp_prof, prs_in);
 }
 
 int astr_gpu_channel_state(astr_ctx* c, double* out) {
@@ -2754,8 +3042,8 @@ static int ready(astr_ctx* c) {
   if (!c->metrics_set && c->pm.order == ASTR_ORDER_MAIN)
     return fail(c, ASTR_ERR_STATE, "metrics not set (astr_gpu_set_metrics)");
   if (!c->state_set) return fail(c, ASTR_ERR_STATE, "state not uploaded (astr_gpu_upload_state)");
-  if ((c->channel || c->slip_mask || c->gc_dx[0] || c->gc_dx[1]) && !c->grid_set)
-    return fail(c, ASTR_ERR_STATE, "grid not set (astr_gpu_set_grid): a channel or bctype 411 or 23");
+  if ((c->channel || c->slip_mask || c->gc_dx[0] || c->gc_dx[1] || c->nscbc_b) && !c->grid_set)
+    return fail(c, ASTR_ERR_STATE, "grid not set (astr_gpu_set_grid): a channel or bctype 411, 23 or 12");
   return ASTR_OK;
 }
 

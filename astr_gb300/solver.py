@@ -119,12 +119,14 @@ class GpuSolver:
         x = _f(x, halo_shape(self.im, self.jm, self.km, 3))
         self._c(self.L.astr_gpu_set_grid(self.h, capi.dptr(x)))
 
-    def set_inflow(self, vel_in=None, tmp_in=None, tmp_prof=None):
-        """Inflow arrays of bctype 11 on xmin: vel_in (jm+1, km+1, 3),
-        tmp_in (jm+1, km+1), tmp_prof (jm+1); None keeps the freestream."""
+    def set_inflow(self, vel_in=None, tmp_in=None, tmp_prof=None, prs_in=None):
+        """Inflow arrays of bctypes 11 and 12 on xmin: vel_in (jm+1, km+1,
+        3), tmp_in (jm+1, km+1), tmp_prof (jm+1), prs_in (jm+1, km+1);
+        None takes the freestream values."""
         nj, nk = self.jm + 1, self.km + 1
         args = []
-        for a, shape in ((vel_in, (nj, nk, 3)), (tmp_in, (nj, nk)), (tmp_prof, (nj,))):
+        for a, shape in ((vel_in, (nj, nk, 3)), (tmp_in, (nj, nk)), (tmp_prof, (nj,)),
+                         (prs_in, (nj, nk))):
             if a is None:
                 args.append(None)
                 continue

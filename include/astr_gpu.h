@@ -138,18 +138,21 @@ int astr_gpu_set_metrics(astr_ctx* ctx, const double* dxi, const double* jacob);
  * integrals of src_chan and massfluxchan; a context with 411 on ymin keeps
  * which of that face's nodes lie at x <= xslip; a context with 23 (gcnscbc)
  * on xmax or ymax keeps that face's normal spacing and the grid's extent
- * along it; others ignore the call. */
+ * along it, one with 12 (inflow_nscbc) the grid's x extent; others ignore
+ * the call. */
 int astr_gpu_set_grid(astr_ctx* ctx, const double* x);
 
-/* Inflow arrays of bctype 11 on xmin (inflow, src/bc.F90:1366-1562):
- * vel_in(0:jm,0:km,1:3), tmp_in(0:jm,0:km) and tmp_prof(0:jm) in Fortran
+/* Inflow arrays of bctypes 11 (inflow, src/bc.F90:1366-1562) and 12
+ * (inflow_nscbc, src/bc.F90:2114-2344) on xmin: vel_in(0:jm,0:km,1:3),
+ * tmp_in(0:jm,0:km), tmp_prof(0:jm) and prs_in(0:jm,0:km) in Fortran
  * layout, the values alloinflow's arrays hold after the profile routine
  * (freestreaminflow, profileinflow, ...).  A NULL array takes
- * freestreaminflow's values (u = 1, v = w = 0, T = 1), which a context
- * with bctype 11 starts from.  The turbulent inflow fluctuations (turbinf)
- * are not applied.  ASTR_ERR_STATE without an inflow face. */
+ * freestreaminflow's values (u = 1, v = w = 0, T = 1, p = pinf), which a
+ * context with an inflow face starts from.  11 reads vel_in, tmp_in and
+ * tmp_prof; 12 reads vel_in and prs_in.  The turbulent inflow fluctuations
+ * (turbinf) are not applied.  ASTR_ERR_STATE without an inflow face. */
 int astr_gpu_set_inflow(astr_ctx* ctx, const double* vel_in, const double* tmp_in,
-                        const double* tmp_prof);
+                        const double* tmp_prof, const double* prs_in);
 
 /* Asynchronous stepping (no counterpart in the reference; used by the
  * request loop that serves many independent cases on one GPU): enqueue

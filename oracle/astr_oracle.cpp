@@ -79,10 +79,11 @@ struct orc_ctx {
   std::vector<double> qrhs, qsave, dvel, dtmp;
   std::vector<double> ssf;              // shock-sensor function (halo array)
   std::vector<unsigned char> lshock;    // lshock(0:im,0:jm,0:km)
-  // inflow (bctype 11 on xmin): vel_in(0:jm,0:km,1:3), tmp_in(0:jm,0:km),
-  // tmp_prof(0:jm) (alloinflow, src/bc.F90:69-83; freestreaminflow's
-  // values, src/bc.F90:7950-8003, until the host sets a profile)
-  std::vector<double> vel_in, tmp_in, tmp_prof;
+  // inflow (bctypes 11 and 12 on xmin): vel_in(0:jm,0:km,1:3),
+  // tmp_in(0:jm,0:km), tmp_prof(0:jm), prs_in(0:jm,0:km) (alloinflow,
+  // src/bc.F90:69-83; freestreaminflow's values, src/bc.F90:7950-8003,
+  // until the host sets a profile)
+  std::vector<double> vel_in, tmp_in, tmp_prof, prs_in;
   bool sson = false;                    // allocated(lshock)
   double force[3] = {0, 0, 0};
   double massflux_target = 0.0;
@@ -861,6 +862,7 @@ orc_ctx* orc_create(const orc_config* cfg) {
   for (size_t t = 0; t < nf; ++t) c->vel_in[t] = c->uinf;  // (uinf, vinf = 0, winf = 0)
   c->tmp_in.assign(nf, c->tinf);
   c->tmp_prof.assign((size_t)c->jm + 1, c->tinf);
+  c->prs_in.assign(nf, c->roinf * c->tinf / c->const2);  // thermal(density, temperature)
   return c;
 }
 
@@ -877,6 +879,7 @@ double* orc_field(orc_ctx* c, const char* name) {
   if (s == "vel_in") return c->vel_in.data();
   if (s == "tmp_in") return c->tmp_in.data();
   if (s == "tmp_prof") return c->tmp_prof.data();
+  if (s == "prs_in") return c->prs_in.data();
   if (s == "dxi") return c->dxi.data();
   if (s == "jacob") return c->jacob.data();
   if (s == "sigma") return c->sigma.data();
@@ -1598,11 +1601,174 @@ void face_node(orc_ctx& c, int n, int type, double tw, int i, int j, int k, doub
   }
 }
 
+// pmatrix (src/bc.F90:5516-5611): the characteristic matrix of the face
+// whose metric row is ddi (inv false) or its inverse (inv true).
+void pmatrix(double rho, double u, double v, double w, double t, const double ddi[3], bool inv,
+             double mach, double P[5][5]) {
+  const double c = std::sqrt(t) / mach;  // sos, nondimensional
+  const double var1 = 1.0 / std::sqrt(ddi[0] * ddi[0] + ddi[1] * ddi[1] + ddi[2] * ddi[2]);
+  const double nx = ddi[0] * var1, ny = ddi[1] * var1, nz = ddi[2] * var1;
+  const double phi = 0.5 * (GAMMA - 1.0) * (u * u + v * v + w * w);
+  const double VV = nx * u + ny * v + nz * w;
+  const double a1 = GAMMA - 1.0;
+  const double a2 = 1.0 / (std::sqrt(2.0) * rho * c);
+  const double a3 = rho / (c * std::sqrt(2.0));
+  const double a4 = (phi + c * c) / (GAMMA - 1.0);
+  const double a5 = 1.0 - phi / (c * c);
+  const double a6 = phi / (GAMMA - 1.0);
+  if (inv) {
+    const double n3[3] = {nx, ny, nz};
+    P[0][0] = nx * a5 - (nz * v - ny * w) / rho;
+    P[0][1] = nx * a1 * u / (c * c);
+    P[0][2] = nx * a1 * v / (c * c) + nz / rho;
+    P[0][3] = nx * a1 * w / (c * c) - ny / rho;
+    P[1][0] = ny * a5 - (nx * w - nz * u) / rho;
+    P[1][1] = ny * a1 * u / (c * c) - nz / rho;
+    P[1][2] = ny * a1 * v / (c * c);
+    P[1][3] = ny * a1 * w / (c * c) + nx / rho;
+    P[2][0] = nz * a5 - (ny * u - nx * v) / rho;
+    P[2][1] = nz * a1 * u / (c * c) + ny / rho;
+    P[2][2] = nz * a1 * v / (c * c) - nx / rho;
+    P[2][3] = nz * a1 * w / (c * c);
+    for (int r = 0; r < 3; ++r) P[r][4] = -(n3[r] * a1 / (c * c));
+    P[3][0] = a2 * (phi - c * VV);
+    P[3][1] = -(a2 * (a1 * u - nx * c));
+    P[3][2] = -(a2 * (a1 * v - ny * c));
+    P[3][3] = -(a2 * (a1 * w - nz * c));
+    P[3][4] = a1 * a2;
+    P[4][0] = a2 * (phi + c * VV);
+    P[4][1] = -(a2 * (a1 * u + nx * c));
+    P[4][2] = -(a2 * (a1 * v + ny * c));
+    P[4][3] = -(a2 * (a1 * w + nz * c));
+    P[4][4] = a1 * a2;
+  } else {
+    P[0][0] = nx; P[0][1] = ny; P[0][2] = nz; P[0][3] = a3; P[0][4] = a3;
+    P[1][0] = nx * u; P[1][1] = ny * u - nz * rho; P[1][2] = nz * u + ny * rho;
+    P[1][3] = a3 * (u + nx * c); P[1][4] = a3 * (u - nx * c);
+    P[2][0] = nx * v + nz * rho; P[2][1] = ny * v; P[2][2] = nz * v - nx * rho;
+    P[2][3] = a3 * (v + ny * c); P[2][4] = a3 * (v - ny * c);
+    P[3][0] = nx * w - ny * rho; P[3][1] = ny * w + nx * rho; P[3][2] = nz * w;
+    P[3][3] = a3 * (w + nz * c); P[3][4] = a3 * (w - nz * c);
+    P[4][0] = nx * a6 + rho * (nz * v - ny * w); P[4][1] = ny * a6 + rho * (nx * w - nz * u);
+    P[4][2] = nz * a6 + rho * (ny * u - nx * v);
+    P[4][3] = a3 * (a4 + c * VV); P[4][4] = a3 * (a4 - c * VV);
+  }
+}
+
+// The inviscid flux of node p through the metric row d (the Ecs / fcs of
+// inflow_nscbc): J (q u_d + dxi(d,:) p) with u_d = dxi(d,:) . u; dxi(d,m)
+// is array d + 3 m of the Fortran dxi(..,1:3,1:3).
+void row_flux(const orc_ctx& c, long p, int d, double* f) {
+  const long nh = c.nh;
+  const double* X = c.dxi.data() + p;
+  const double x1 = X[(d + 0) * nh], x2 = X[(d + 3) * nh], x3 = X[(d + 6) * nh];
+  const double* V = c.vel.data() + p;
+  const double uu = x1 * V[0] + x2 * V[nh] + x3 * V[2 * nh];
+  const double J = c.jacob[p], pr = c.prs[p];
+  const double* Q = c.q.data() + p;
+  f[0] = J * Q[0] * uu;
+  f[1] = J * (Q[nh] * uu + x1 * pr);
+  f[2] = J * (Q[2 * nh] * uu + x2 * pr);
+  f[3] = J * (Q[3 * nh] * uu + x3 * pr);
+  f[4] = J * (Q[4 * nh] + pr) * uu;
+}
+
+// inflow_nscbc (src/bc.F90:2114-2344) on xmin: adds to qrhs at i = 0 the
+// characteristic residual (LODI: the incoming waves relaxed towards the
+// inflow arrays at rate kin, the outgoing one kept) and the tangential
+// flux derivatives of the face (ddfc '222e' with periodic y and z,
+// diff2ec ntype 3: 0.5 (f(j+1) - f(j-1)), halo values included).
+void inflow_nscbc(orc_ctx& c) {
+  const long nh = c.nh, n0 = c.n0;
+  const int im = c.im, jm = c.jm, km = c.km;
+  const double mach = c.cfg.mach;
+  double gm2 = 0.0;
+  for (int k = 0; k <= km; ++k)
+    for (int j = 0; j <= jm; ++j)
+      for (int i = 0; i <= im; ++i) {
+        const long p = c.h(i, j, k);
+        const double u = c.vel[p], v = c.vel[p + nh], w = c.vel[p + 2 * nh];
+        const double var1 = u * u + v * v + w * w;
+        const double css = std::sqrt(c.tmp[p]) / mach;
+        gm2 = std::max(gm2, var1 / css / css);
+      }
+  const double extent = grid_extent(c, 0);
+  const size_t nf = (size_t)(jm + 1) * (km + 1);
+  for (int k = 0; k <= km; ++k)
+    for (int j = 0; j <= jm; ++j) {
+      const long p = c.h(0, j, k), pa = c.h(1, j, k);
+      const size_t fj = (size_t)j + (size_t)(jm + 1) * k;
+      const double rho = c.rho[p], u = c.vel[p], v = c.vel[p + nh], w = c.vel[p + 2 * nh];
+      const double t = c.tmp[p], pr = c.prs[p], J = c.jacob[p];
+      const double* Q = c.q.data() + p;
+      const double ddi[3] = {c.dxi[p], c.dxi[p + 3 * nh], c.dxi[p + 6 * nh]};  // dxi(i,j,k,1,:)
+      double pnor[5][5], pinv[5][5];
+      pmatrix(rho, u, v, w, t, ddi, false, mach, pnor);
+      pmatrix(rho, u, v, w, t, ddi, true, mach, pinv);
+      double e0[5], e1[5], dE[5];
+      row_flux(c, p, 0, e0);
+      row_flux(c, pa, 0, e1);
+      for (int n = 0; n < 5; ++n) dE[n] = -e0[n] + e1[n];  // deriv(Ecs(0), Ecs(1))
+      const double E[5] = {Q[nh], Q[nh] * u + pr, Q[2 * nh] * u, Q[3 * nh] * u, (Q[4 * nh] + pr) * u};
+      const double F[5] = {Q[2 * nh], Q[nh] * v, Q[2 * nh] * v + pr, Q[3 * nh] * v, (Q[4 * nh] + pr) * v};
+      const double G[5] = {Q[3 * nh], Q[nh] * w, Q[2 * nh] * w, Q[3 * nh] * w + pr, (Q[4 * nh] + pr) * w};
+      double jcbi[3];
+      for (int m = 0; m < 3; ++m)
+        jcbi[m] = -(c.dxi[p + 3 * m * nh] * J) + c.dxi[pa + 3 * m * nh] * c.jacob[pa];
+      double rest[5], l1[5], lodi[5];
+      for (int n = 0; n < 5; ++n) {
+        rest[n] = E[n] * jcbi[0] + F[n] * jcbi[1] + G[n] * jcbi[2];
+        l1[n] = dE[n] - rest[n];
+      }
+      for (int r = 0; r < 5; ++r) {
+        double acc = 0.0;
+        for (int m = 0; m < 5; ++m) acc = acc + pinv[r][m] * l1[m];
+        lodi[r] = acc / J;
+      }
+      const double css = std::sqrt(t) / mach;
+      const double kin = 0.25 * (1.0 - gm2) * css / extent;
+      const double var1 = 1.0 / std::sqrt(ddi[0] * ddi[0] + ddi[1] * ddi[1] + ddi[2] * ddi[2]);
+      const size_t nfv = nf;
+      const double ui = c.vel_in[fj], vi = c.vel_in[fj + nfv], wi = c.vel_in[fj + 2 * nfv];
+      lodi[0] = 0.0;
+      lodi[1] = kin * 0.5 * (ddi[0] * var1 * (w - wi) - ddi[2] * var1 * (u - ui));
+      lodi[2] = kin * 0.5 * (-(ddi[0] * var1 * (v - vi)) + ddi[1] * var1 * (u - ui));
+      lodi[3] = kin * (ddi[0] * var1 * (u - ui) + ddi[1] * var1 * (v - vi) + ddi[2] * var1 * (w - wi) +
+                       (pr - c.prs_in[fj]) / rho / css);
+      for (int r = 0; r < 5; ++r) {
+        double acc = 0.0;
+        for (int m = 0; m < 5; ++m) acc = acc + pnor[r][m] * lodi[m];
+        const double add = acc * J + rest[r];
+        c.qrhs[c.z(0, j, k) + r * n0] += add;
+      }
+    }
+  // tangential derivatives on the face: y for k = ks..ke, z for j = js..je
+  for (int k = c.ks; k <= c.ke; ++k)
+    for (int j = c.js; j <= c.je; ++j) {
+      double fp[5], fm[5];
+      row_flux(c, c.h(0, j + 1, k), 1, fp);
+      row_flux(c, c.h(0, j - 1, k), 1, fm);
+      for (int n = 0; n < 5; ++n) c.qrhs[c.z(0, j, k) + n * n0] += 0.5 * (fp[n] - fm[n]);
+    }
+  if (c.ndims == 3)
+    for (int j = c.js; j <= c.je; ++j)
+      for (int k = c.ks; k <= c.ke; ++k) {
+        double fp[5], fm[5];
+        row_flux(c, c.h(0, j, k + 1), 2, fp);
+        row_flux(c, c.h(0, j, k - 1), 2, fm);
+        for (int n = 0; n < 5; ++n) c.qrhs[c.z(0, j, k) + n * n0] += 0.5 * (fp[n] - fm[n]);
+      }
+}
+
 }  // namespace
 
 void orc_boucon(orc_ctx* c) {
   for (int n = 0; n < 2 * c->ndims; ++n) {
     const int type = face_bctype(*c, n);
+    if (type == 12 && n == 0 && c->npdc(0) == 4) {
+      inflow_nscbc(*c);
+      continue;
+    }
     if (type != 41 && type != 42 && type != 50 && type != 60 && type != 421 && type != 21 &&
         type != 51 && type != 411 && type != 11 && type != 23)
       continue;

@@ -172,11 +172,13 @@ class Oracle:
         return buf.reshape(shape, order="F")
 
     def inflow(self):
-        """Views of the inflow arrays of bctype 11 (freestream values until
-        set): vel_in (jm+1, km+1, 3), tmp_in (jm+1, km+1), tmp_prof (jm+1)."""
+        """Views of the inflow arrays of bctypes 11 and 12 (freestream values
+        until set): vel_in (jm+1, km+1, 3), tmp_in (jm+1, km+1), tmp_prof
+        (jm+1), prs_in (jm+1, km+1)."""
         nj, nk = self.jm + 1, self.km + 1
         out = {}
-        for name, shape in (("vel_in", (nj, nk, 3)), ("tmp_in", (nj, nk)), ("tmp_prof", (nj,))):
+        for name, shape in (("vel_in", (nj, nk, 3)), ("tmp_in", (nj, nk)), ("tmp_prof", (nj,)),
+                            ("prs_in", (nj, nk))):
             p = self.L.orc_field(self.h, name.encode())
             buf = np.ctypeslib.as_array(p, shape=(int(np.prod(shape)),))
             out[name] = buf.reshape(shape, order="F")

@@ -55,7 +55,8 @@ def _params(**kw):
 @pytest.mark.parametrize("npdc, kw, code, text", [
     ((3, 3, 3), dict(bctype=(41, 0, 0, 0, 0, 0), twall=1.0), "ARG", "npdc = 4"),
     ((3, 3, 4), dict(bctype=(0, 0, 0, 0, 42, 0)), "UNSUPPORTED", "x and y faces"),
-    ((4, 3, 3), dict(bctype=(12, 21, 0, 0, 0, 0)), "UNSUPPORTED", "bctype"),
+    ((4, 3, 3), dict(bctype=(22, 21, 0, 0, 0, 0)), "UNSUPPORTED", "bctype"),
+    ((4, 4, 3), dict(bctype=(12, 21, 0, 0, 0, 0)), "UNSUPPORTED", "periodic y and z"),
     ((4, 4, 3), dict(bctype=(0, 0, 11, 0, 0, 0)), "UNSUPPORTED", "xmin"),
     ((4, 3, 3), dict(bctype=(421, 0, 0, 0, 0, 0)), "UNSUPPORTED", "y faces"),
     ((4, 3, 3), dict(bctype=(0, 411, 0, 0, 0, 0), twall=1.0), "UNSUPPORTED", "y faces"),
@@ -198,12 +199,13 @@ def test_plain_c_host_null_arguments(gpu_lib, tmp_path):
 # all faces; noslip_adibatic 6728-7036 x and y; slipisotwall 7038-7229 and
 # slipadibwall 7231-7430 y; outflow 3404-3617 xmax and ymax; farfield
 # 3008-3392 y and z; zeroextrap 2356-2652 and symmetry 2664-2996 all faces;
-# inflow 1366-1562 xmin; gcnscbc 8024-8254 xmax and ymax).
+# inflow 1366-1562 and inflow_nscbc 2114-2344 xmin; gcnscbc 8024-8254 xmax
+# and ymax).
 FACES = {41: range(6), 42: range(4), 411: (2, 3), 421: (2, 3), 21: (1, 3), 51: range(2, 6),
-         50: range(6), 60: range(6), 11: (0,), 23: (1, 3)}
+         50: range(6), 60: range(6), 11: (0,), 12: (0,), 23: (1, 3)}
 
 
-@pytest.mark.parametrize("btype", sorted(FACES) + [12, 22, 31, 52])
+@pytest.mark.parametrize("btype", sorted(FACES) + [22, 31, 52])
 def test_routine_face_table(gpu_lib, btype):
     """create accepts a routine exactly on the faces where the reference
     has it and refuses the routines that are not built.  Accepted contexts

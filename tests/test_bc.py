@@ -346,3 +346,111 @@ def test_gcnscbc_face_values():
         q, rho, vel, prs = (o.field(k) for k in ("q", "rho", "vel", "prs"))
         e = _face(prs, n) * 2.5 + 0.5 * _face(rho, n) * (_face(vel, n) ** 2).sum(axis=-1)
         np.testing.assert_allclose(_face(q[..., 4], n), e, rtol=1e-12)
+
+
+def _pmatrix(rho, u, v, w, t, ddi, inv, mach):
+    """pmatrix (src/bc.F90:5516-5611) on arrays: shape (..., 5, 5)."""
+    g = 1.4
+    c = np.sqrt(t) / mach
+    var1 = 1.0 / np.sqrt(ddi[0] ** 2 + ddi[1] ** 2 + ddi[2] ** 2)
+    nx, ny, nz = ddi[0] * var1, ddi[1] * var1, ddi[2] * var1
+    phi = 0.5 * (g - 1.0) * (u * u + v * v + w * w)
+    VV = nx * u + ny * v + nz * w
+    a1, a2, a3 = g - 1.0, 1.0 / (np.sqrt(2.0) * rho * c), rho / (c * np.sqrt(2.0))
+    a4, a5, a6 = (phi + c * c) / (g - 1.0), 1.0 - phi / (c * c), phi / (g - 1.0)
+    c2 = c * c
+    if inv:
+        rows = [[nx * a5 - (nz * v - ny * w) / rho, nx * a1 * u / c2, nx * a1 * v / c2 + nz / rho,
+                 nx * a1 * w / c2 - ny / rho, -nx * a1 / c2],
+                [ny * a5 - (nx * w - nz * u) / rho, ny * a1 * u / c2 - nz / rho, ny * a1 * v / c2,
+                 ny * a1 * w / c2 + nx / rho, -ny * a1 / c2],
+                [nz * a5 - (ny * u - nx * v) / rho, nz * a1 * u / c2 + ny / rho, nz * a1 * v / c2 - nx / rho,
+                 nz * a1 * w / c2, -nz * a1 / c2],
+                [a2 * (phi - c * VV), -a2 * (a1 * u - nx * c), -a2 * (a1 * v - ny * c),
+                 -a2 * (a1 * w - nz * c), a1 * a2],
+                [a2 * (phi + c * VV), -a2 * (a1 * u + nx * c), -a2 * (a1 * v + ny * c),
+                 -a2 * (a1 * w + nz * c), a1 * a2]]
+    else:
+        rows = [[nx, ny, nz, a3, a3],
+                [nx * u, ny * u - nz * rho, nz * u + ny * rho, a3 * (u + nx * c), a3 * (u - nx * c)],
+                [nx * v + nz * rho, ny * v, nz * v - nx * rho, a3 * (v + ny * c), a3 * (v - ny * c)],
+                [nx * w - ny * rho, ny * w + nx * rho, nz * w, a3 * (w + nz * c), a3 * (w - nz * c)],
+                [nx * a6 + rho * (nz * v - ny * w), ny * a6 + rho * (nx * w - nz * u),
+                 nz * a6 + rho * (ny * u - nx * v), a3 * (a4 + c * VV), a3 * (a4 - c * VV)]]
+    return np.stack([np.stack([np.broadcast_to(x, np.shape(rho)) for x in r], -1) for r in rows], -2)
+
+
+def _row_flux(o, sl, d):
+    """J (q u_d + dxi(d,:) p) at the halo-array slice sl (inflow_nscbc's Ecs / fcs)."""
+    X = o.field("dxi")[sl]
+    x = [X[..., d + 3 * m] for m in range(3)]
+    V, Q = o.field("vel")[sl], o.field("q")[sl]
+    J, p = o.field("jacob")[sl], o.field("prs")[sl]
+    uu = x[0] * V[..., 0] + x[1] * V[..., 1] + x[2] * V[..., 2]
+    return np.stack([J * Q[..., 0] * uu, J * (Q[..., 1] * uu + x[0] * p), J * (Q[..., 2] * uu + x[1] * p),
+                     J * (Q[..., 3] * uu + x[2] * p), J * (Q[..., 4] + p) * uu], -1)
+
+
+def _inflow_nscbc_expected(o, mach, extent):
+    """inflow_nscbc (src/bc.F90:2114-2344) in numpy: the residual added at
+    i = 0 (periodic y and z), shape (jm+1, km+1, 5)."""
+    jm, km = o.jm, o.km
+    inner = (slice(H, H + o.im + 1), slice(H, H + jm + 1), slice(H, H + km + 1))
+    V, T = o.field("vel")[inner], o.field("tmp")[inner]
+    gm2 = ((V[..., 0] ** 2 + V[..., 1] ** 2 + V[..., 2] ** 2) / (np.sqrt(T) / mach) / (np.sqrt(T) / mach)).max()
+    f0 = (H, slice(H, H + jm + 1), slice(H, H + km + 1))
+    f1 = (H + 1,) + f0[1:]
+    rho, vel, t, pr, J = (o.field(k)[f0] for k in ("rho", "vel", "tmp", "prs", "jacob"))
+    Q, X = o.field("q")[f0], o.field("dxi")[f0]
+    u, v, w = vel[..., 0], vel[..., 1], vel[..., 2]
+    ddi = [X[..., 0], X[..., 3], X[..., 6]]
+    pnor, pinv = (_pmatrix(rho, u, v, w, t, ddi, inv, mach) for inv in (False, True))
+    dE = -_row_flux(o, f0, 0) + _row_flux(o, f1, 0)
+    E = np.stack([Q[..., 1], Q[..., 1] * u + pr, Q[..., 2] * u, Q[..., 3] * u, (Q[..., 4] + pr) * u], -1)
+    F = np.stack([Q[..., 2], Q[..., 1] * v, Q[..., 2] * v + pr, Q[..., 3] * v, (Q[..., 4] + pr) * v], -1)
+    G = np.stack([Q[..., 3], Q[..., 1] * w, Q[..., 2] * w, Q[..., 3] * w + pr, (Q[..., 4] + pr) * w], -1)
+    Xa, Ja = o.field("dxi")[f1], o.field("jacob")[f1]
+    jcbi = [-(X[..., 3 * m] * J) + Xa[..., 3 * m] * Ja for m in range(3)]
+    rest = E * jcbi[0][..., None] + F * jcbi[1][..., None] + G * jcbi[2][..., None]
+    lodi = np.einsum("...rc,...c->...r", pinv, dE - rest) / J[..., None]
+    css = np.sqrt(t) / mach
+    kin = 0.25 * (1.0 - gm2) * css / extent
+    var1 = 1.0 / np.sqrt(ddi[0] ** 2 + ddi[1] ** 2 + ddi[2] ** 2)
+    f = o.inflow()
+    ui, vi, wi = f["vel_in"][..., 0], f["vel_in"][..., 1], f["vel_in"][..., 2]
+    lodi[..., 0] = 0.0
+    lodi[..., 1] = kin * 0.5 * (ddi[0] * var1 * (w - wi) - ddi[2] * var1 * (u - ui))
+    lodi[..., 2] = kin * 0.5 * (-ddi[0] * var1 * (v - vi) + ddi[1] * var1 * (u - ui))
+    lodi[..., 3] = kin * (ddi[0] * var1 * (u - ui) + ddi[1] * var1 * (v - vi) + ddi[2] * var1 * (w - wi) +
+                          (pr - f["prs_in"]) / rho / css)
+    out = np.einsum("...rc,...c->...r", pnor, lodi) * J[..., None] + rest
+    ym = (H, slice(H - 1, H + jm), slice(H, H + km + 1))
+    yp = (H, slice(H + 1, H + jm + 2), slice(H, H + km + 1))
+    out = out + 0.5 * (_row_flux(o, yp, 1) - _row_flux(o, ym, 1))
+    if km > 0:
+        zm = (H, slice(H, H + jm + 1), slice(H - 1, H + km))
+        zp = (H, slice(H, H + jm + 1), slice(H + 1, H + km + 2))
+        out = out + 0.5 * (_row_flux(o, zp, 2) - _row_flux(o, zm, 2))
+    return out
+
+
+@pytest.mark.parametrize("profile", [False, True])
+def test_inflow_nscbc_residual(profile):
+    """12 (inflow_nscbc) on xmin, y and z periodic: boucon adds to qrhs at
+    i = 0 the LODI residual and the face's tangential flux derivatives;
+    against a numpy restatement (pmatrix, the one-sided normal flux
+    difference, the relaxation of the incoming waves towards the inflow
+    arrays at the rate kin of the domain-wide Mach number)."""
+    o = bc_oracle((24, 20, 16), (4, 3, 3), (12, 21, 0, 0, 0, 0), deltat=2e-3)
+    if profile:
+        _inflow_profile(o)
+        f = o.inflow()
+        f["prs_in"][...] = cases.refcal(MACH, 400.0)["pinf"] * (1.0 + 0.02 * f["tmp_in"])
+    before = o.field("q").copy()
+    o.call("boucon")
+    assert np.array_equal(o.field("q")[H], before[H])  # the face's state is not touched
+    want = _inflow_nscbc_expected(o, MACH, 2.0 * np.pi)
+    got = o.field("qrhs")[0]
+    scale = np.abs(want).max(axis=(0, 1))
+    np.testing.assert_allclose(got / scale, want / scale, rtol=0, atol=1e-13)
+    assert np.all(o.field("qrhs")[1:] == 0.0)

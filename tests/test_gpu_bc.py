@@ -5,11 +5,12 @@ a slip region, adiabatic) on the y faces, outflow on xmax and ymax, farfield on 
 viscous terms and the
 filter; a skewed curvilinear box where the symmetry faces project on the
 metric normal; inflow on xmin (freestream and a profile) with outflow on
-xmax; gcnscbc on xmax and ymax; and the FP32-storage form against FP64."""
+xmax; inflow_nscbc on xmin (its residual and steps); gcnscbc on xmax and
+ymax; and the FP32-storage form against FP64."""
 import numpy as np
 import pytest
 
-from astr_gb300 import capi
+from astr_gb300 import capi, cases
 from test_bc import H, MACH, bc_oracle
 
 pytestmark = pytest.mark.gpu
@@ -177,8 +178,8 @@ def test_boundary_routine_checks(gpu_lib):
         GpuSolver(16, 16, 16, bctype=(41, 0, 0, 0, 0, 0))
     with pytest.raises(capi.AstrError):   # adiabatic no-slip exists for x and y faces only
         GpuSolver(16, 16, 16, npdc=(3, 3, 4), bctype=(0, 0, 0, 0, 42, 0))
-    with pytest.raises(capi.AstrError):   # not built (inflow_nscbc)
-        GpuSolver(16, 16, 16, npdc=(4, 3, 3), bctype=(12, 21, 0, 0, 0, 0))
+    with pytest.raises(capi.AstrError):   # not built (outflow_nscbc)
+        GpuSolver(16, 16, 16, npdc=(4, 3, 3), bctype=(22, 21, 0, 0, 0, 0))
 
 
 @pytest.mark.parametrize("profile", [False, True])
@@ -191,7 +192,7 @@ def test_inflow_outflow_match_oracle(gpu_lib, profile):
     g = _gpu_from(o)
     if profile:
         f = _inflow_profile(o)
-        g.set_inflow(f["vel_in"], f["tmp_in"], f["tmp_prof"])
+        g.set_inflow(f["vel_in"], f["tmp_in"], f["tmp_prof"], f["prs_in"])
     o.rk3_steps(4)
     g.time_integration_rk(4)
     s = g.download_state()
@@ -249,3 +250,57 @@ def test_gcnscbc_steps_match_oracle(gpu_lib):
     s = g.download_state()
     g.close()
     _cmp(o, s, tol=5e-12)
+
+
+def _nscbc_box(profile):
+    from test_bc import _inflow_profile
+    o = bc_oracle((24, 20, 16), (4, 3, 3), (12, 21, 0, 0, 0, 0), deltat=2e-3, lfilter=True)
+    f = None
+    if profile:
+        _inflow_profile(o)
+        f = o.inflow()
+        f["prs_in"][...] = cases.refcal(MACH, 400.0)["pinf"] * (1.0 + 0.02 * f["tmp_in"])
+        f = {k: v.copy() for k, v in f.items()}
+    return o, f
+
+
+def _nscbc_gpu(o, f):
+    g = _gpu_from(o)
+    with pytest.raises(capi.AstrError, match="grid not set"):
+        g.time_integration_rk(1)
+    g.set_grid(o.field("x").copy(order="F"))
+    if f is not None:
+        g.set_inflow(f["vel_in"], f["tmp_in"], f["tmp_prof"], f["prs_in"])
+    return g
+
+
+def test_inflow_nscbc_residual_matches_oracle(gpu_lib):
+    """12 (inflow_nscbc) on xmin, outflow on xmax, y and z periodic: the
+    routine chain boucon, qswap, gradcal, rhscal gives the oracle's residual
+    (the routine's LODI and tangential terms at i = 0 added under rhscal's
+    negation), every node."""
+    o, f = _nscbc_box(True)
+    g = _nscbc_gpu(o, f)
+    for name in ("boucon", "qswap", "gradcal", "rhscal"):
+        o.call(name)
+        getattr(g, name)()
+    r = g.download_rhs()["qrhs"]
+    g.close()
+    ro = o.field("qrhs")
+    for m in range(5):
+        scale = np.abs(ro[..., m]).max()
+        err = np.abs(r[..., m] - ro[..., m]).max() / scale
+        face = np.abs(r[0, ..., m] - ro[0, ..., m]).max() / np.abs(ro[0, ..., m]).max()
+        print(f"q{m + 1}: {err:.1e} (face {face:.1e})")
+        assert err <= 1e-12 and face <= 1e-12
+
+
+@pytest.mark.parametrize("profile", [False, True])
+def test_inflow_nscbc_steps_match_oracle(gpu_lib, profile):
+    o, f = _nscbc_box(profile)
+    g = _nscbc_gpu(o, f)
+    o.rk3_steps(4)
+    g.time_integration_rk(4)
+    s = g.download_state()
+    g.close()
+    _cmp(o, s)
