@@ -174,3 +174,54 @@ def test_batch_group_joins_and_leaves_between_calls(monkeypatch):
     assert a.finished and c.finished and a.remaining == 0 and c.remaining == 0
     assert [k for k, _ in grp.batch.calls] == [7, 20, 10, 13]
     assert grp.batch.members == []
+
+
+class _FakeSolver:
+    """A case's solver for BatchBackend host tests: records graph steps."""
+
+    def __init__(self, name, batchable=True):
+        self.name, self.batchable = name, batchable
+        self.graph_steps = 0
+
+    def step_async(self, n):
+        self.graph_steps += n
+
+    def poll(self):
+        return True
+
+
+class _RefusingBatch(_FakeBatch):
+    def add(self, g):
+        from astr_gb300 import capi
+        if not g.batchable:
+            raise capi.AstrError(capi.ASTR_ERR_UNSUPPORTED, "not batchable")
+        super().add(g)
+
+
+def test_batch_backend_routes_cases(monkeypatch):
+    """A batchable case joins the batch (or waits for the call in flight);
+    a case the batch refuses runs on its own graphs; one above max_points
+    too; the call cycle finishes every batched case."""
+    from astr_gb300 import capi
+    monkeypatch.setattr(capi, "Batch", _RefusingBatch)
+    be = serve.BatchBackend.__new__(serve.BatchBackend)
+    be.groups = [serve._Group(capi.FP32_STORAGE, 8)]
+    be.max_points = 1000.0
+    a = serve._BatchCase(_FakeSolver("a"), 500.0)
+    b = serve._BatchCase(_FakeSolver("b", batchable=False), 500.0)
+    big = serve._BatchCase(_FakeSolver("big"), 5000.0)
+    be.enqueue(a, 12)
+    be.enqueue(b, 5)
+    be.enqueue(big, 7)
+    assert a.group is be.groups[0] and b.group is None and big.group is None
+    assert (b.g.graph_steps, big.g.graph_steps) == (5, 7)
+    assert be.done(b) and be.done(big)          # own graphs: their stream's poll
+    assert not be.done(a)                        # starts a call of 8 steps
+    c = serve._BatchCase(_FakeSolver("c"), 100.0)
+    be.enqueue(c, 3)                             # call in flight: joins after it
+    assert c in be.groups[0].joining
+    while not (be.done(a) and be.done(c)):
+        pass
+    calls = [(k, [g.name for g in m]) for k, m in be.groups[0].batch.calls]
+    assert calls == [(8, ["a"]), (3, ["a", "c"]), (1, ["a"])]
+    assert be.calls == 3
