@@ -454,3 +454,20 @@ def test_inflow_nscbc_residual(profile):
     scale = np.abs(want).max(axis=(0, 1))
     np.testing.assert_allclose(got / scale, want / scale, rtol=0, atol=1e-13)
     assert np.all(o.field("qrhs")[1:] == 0.0)
+
+
+def test_pmatrix_inverse_pair():
+    """pmatrix's two forms (src/bc.F90:5516-5611) are inverse to each other
+    for any state and metric row (the check the reference leaves commented
+    out as Pmult = MatMul(Pinv, pnor)): the restated entries hold."""
+    rng = np.random.default_rng(7)
+    n = 64
+    rho = 0.5 + rng.random(n)
+    u, v, w = (rng.standard_normal(n) for _ in range(3))
+    t = 0.5 + rng.random(n)
+    ddi = [rng.standard_normal(n) for _ in range(3)]
+    pnor = _pmatrix(rho, u, v, w, t, ddi, False, MACH)
+    pinv = _pmatrix(rho, u, v, w, t, ddi, True, MACH)
+    eye = np.broadcast_to(np.eye(5), pnor.shape)
+    np.testing.assert_allclose(pinv @ pnor, eye, atol=1e-12)
+    np.testing.assert_allclose(pnor @ pinv, eye, atol=1e-12)
