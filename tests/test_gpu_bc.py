@@ -304,3 +304,22 @@ def test_inflow_nscbc_steps_match_oracle(gpu_lib, profile):
     s = g.download_state()
     g.close()
     _cmp(o, s)
+
+
+def test_inflow_nscbc_fp32_storage_against_fp64(gpu_lib):
+    """The FP32-storage form with inflow_nscbc (profile) against FP64, 10
+    steps: relative L2 ≤1e-5 (measured ≤4.7e-7)."""
+    o, f = _nscbc_box(True)
+    out = {}
+    for name, prec in (("fp64", capi.FP64), ("fp32", capi.FP32_STORAGE)):
+        g = _gpu_from(o, precision=prec)
+        g.set_grid(o.field("x").copy(order="F"))
+        g.set_inflow(f["vel_in"], f["tmp_in"], f["tmp_prof"], f["prs_in"])
+        g.time_integration_rk(10)
+        out[name] = g.download_state()["q"]
+        g.close()
+    sl = (slice(H, H + o.im + 1), slice(H, H + o.jm + 1), slice(H, H + o.km + 1))
+    a, b = out["fp32"][sl], out["fp64"][sl]
+    for m in range(5):
+        e = np.linalg.norm(a[..., m] - b[..., m]) / np.linalg.norm(b[..., m])
+        assert e <= 1e-5, (m, e)
